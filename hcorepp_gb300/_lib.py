@@ -1,0 +1,119 @@
+"""ctypes binding of libhcgb.so (include/hcgb.h).
+
+The library is the product: there is no fallback.  Importing a function from here on a
+machine without the built library raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libhcgb.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "hcgb.h")
+
+HCGB_OK, HCGB_CUDA_ERROR, HCGB_BAD_ARG, HCGB_POOL_TOO_SMALL = 0, 1, 2, 3
+HCGB_RANK_OVERFLOW, HCGB_NOT_CONVERGED, HCGB_UNSUPPORTED = 4, 5, 6
+STATUS_NAMES = {0: "OK", 1: "CUDA_ERROR", 2: "BAD_ARG", 3: "POOL_TOO_SMALL", 4: "RANK_OVERFLOW",
+                5: "NOT_CONVERGED", 6: "UNSUPPORTED"}
+DENSE, COMPRESSED = 0, 1
+NOTRANS, TRANS = 0, 1
+
+
+class HcgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Tile(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("rank", C.c_void_p), ("rows", C.c_int), ("cols", C.c_int),
+                ("max_rank", C.c_int), ("kind", C.c_int)]
+
+
+class Update(C.Structure):
+    _fields_ = [("a", Tile), ("b", Tile), ("c", Tile)]
+
+
+class Params(C.Structure):
+    _fields_ = [("accuracy", C.c_double), ("truncated_svd", C.c_int), ("fixed_rank", C.c_int),
+                ("use_trmm", C.c_int), ("use_ungqr", C.c_int), ("op_type", C.c_int)]
+
+
+_LIB = None
+
+
+def header_functions():
+    """Names of the functions declared in include/hcgb.h."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char \*)\s*(hcgb_\w+)\s*\(", text, re.M)))
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is not built; run `python -m hcorepp_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        vp, ip = C.c_void_p, C.c_int
+        L.hcgb_context_create.argtypes = [ip, vp, C.POINTER(vp)]
+        L.hcgb_context_destroy.argtypes = [vp]
+        L.hcgb_context_set_stream.argtypes = [vp, vp]
+        L.hcgb_sync.argtypes = [vp]
+        L.hcgb_last_error.argtypes = [vp]
+        L.hcgb_last_error.restype = C.c_char_p
+        L.hcgb_workspace_bytes.argtypes = [ip] * 5
+        L.hcgb_workspace_bytes.restype = C.c_size_t
+        L.hcgb_gemm_batch.argtypes = [vp, C.c_double, C.c_double, ip, C.POINTER(Update), C.POINTER(Params), vp]
+        L.hcgb_tlr_gemm.argtypes = [vp, ip, ip, ip, C.c_double, C.POINTER(Tile), C.POINTER(Tile), C.c_double,
+                                    C.POINTER(Tile), C.POINTER(Params), vp]
+        L.hcgb_tile_gemm.argtypes = [vp, C.c_double, C.POINTER(Tile), ip, C.POINTER(Tile), ip, C.c_double,
+                                     C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_ulonglong)]
+        for name in ("hcgb_context_create", "hcgb_context_destroy", "hcgb_context_set_stream", "hcgb_sync",
+                     "hcgb_gemm_batch", "hcgb_tlr_gemm", "hcgb_tile_gemm"):
+            getattr(L, name).restype = C.c_int
+        _LIB = L
+    return _LIB
+
+
+class Context:
+    """One device + stream + workspace (kernels::RunContext's role)."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self._h = C.c_void_p()
+        rc = lib().hcgb_context_create(device, C.c_void_p(stream or 0), C.byref(self._h))
+        if rc:
+            raise HcgbError(rc, "hcgb_context_create failed")
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int):
+        self.check(lib().hcgb_context_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    def check(self, rc: int, allow=(HCGB_OK,)):
+        if rc not in allow:
+            raise HcgbError(rc, lib().hcgb_last_error(self._h).decode())
+        return rc
+
+    def sync(self):
+        self.check(lib().hcgb_sync(self._h))
+
+    def close(self):
+        if self._h:
+            lib().hcgb_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_params(accuracy=1e-4, truncated_svd=False, fixed_rank=0, use_trmm=False, use_ungqr=True, op_type=1):
+    return Params(float(accuracy), int(truncated_svd), int(fixed_rank), int(use_trmm), int(use_ungqr), int(op_type))

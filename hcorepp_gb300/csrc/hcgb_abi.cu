@@ -1,0 +1,503 @@
+// C ABI of libhcgb (declared in include/hcgb.h): contexts, workspace sizing and the
+// batched / tile-matrix / single-tile GEMM entry points.  Host code only; the kernels
+// live in tlr_plan.cu, tlr_qr.cu and tlr_svd.cu.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.cuh"
+
+using namespace hcgb;
+
+struct hcgb_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void *ws = nullptr;          // workspace slots + meta
+    size_t ws_bytes = 0;
+    void *desc = nullptr;        // DevUpdate[] followed by GemmJob[3 * n]
+    size_t desc_bytes = 0;
+    void *stage = nullptr;       // pinned host staging for descriptors
+    size_t stage_bytes = 0;
+    cudaEvent_t stage_done = nullptr;
+    std::string last_error;
+};
+
+namespace {
+
+int fail(hcgb_context *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+#define HCGB_CUDA(ctx, call)                                                                       \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail((ctx), HCGB_CUDA_ERROR, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+int ensure_device(hcgb_context *ctx, void **buf, size_t *have, size_t want) {
+    if (*have >= want) return HCGB_OK;
+    if (*buf) {
+        HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        HCGB_CUDA(ctx, cudaFree(*buf));
+        *buf = nullptr;
+        *have = 0;
+    }
+    size_t sz = want + want / 8;
+    HCGB_CUDA(ctx, cudaMalloc(buf, sz));
+    *have = sz;
+    return HCGB_OK;
+}
+
+int ensure_stage(hcgb_context *ctx, size_t want) {
+    // The previous descriptor upload must have left the staging buffer before it is reused.
+    HCGB_CUDA(ctx, cudaEventSynchronize(ctx->stage_done));
+    if (ctx->stage_bytes >= want) return HCGB_OK;
+    if (ctx->stage) HCGB_CUDA(ctx, cudaFreeHost(ctx->stage));
+    ctx->stage = nullptr;
+    size_t sz = want + want / 8;
+    HCGB_CUDA(ctx, cudaMallocHost(&ctx->stage, sz));
+    ctx->stage_bytes = sz;
+    return HCGB_OK;
+}
+
+DevTile to_dev(const hcgb_tile &t) {
+    DevTile d;
+    d.data = t.data;
+    d.rank = t.rank;
+    d.rows = t.rows;
+    d.cols = t.cols;
+    d.max_rank = t.kind == HCGB_COMPRESSED ? t.max_rank : 0;
+    d.kind = t.kind == HCGB_COMPRESSED ? 1 : 0;
+    return d;
+}
+
+int check_tile(hcgb_context *ctx, const hcgb_tile &t, const char *name) {
+    if (!t.data || t.rows <= 0 || t.cols <= 0)
+        return fail(ctx, HCGB_BAD_ARG, std::string(name) + ": null buffer or empty shape");
+    if (t.kind == HCGB_COMPRESSED && (!t.rank || t.max_rank <= 0))
+        return fail(ctx, HCGB_BAD_ARG, std::string(name) + ": compressed tile without rank or capacity");
+    if (t.kind != HCGB_DENSE && t.kind != HCGB_COMPRESSED)
+        return fail(ctx, HCGB_BAD_ARG, std::string(name) + ": unknown tile kind");
+    return HCGB_OK;
+}
+
+// Shapes that size the workspace and the GEMM grids of a batch (host-side maxima from the
+// tile kinds and capacities; the actual ranks are only known on the device).
+struct BatchShape {
+    int ld = 8, kmax = 8, rmax = 8;
+    int p_m[3] = {0, 0, 0}, p_n[3] = {0, 0, 0};
+    bool any_compressed_c = false;
+};
+
+BatchShape shape_of(const hcgb_update *ups, int n) {
+    BatchShape s;
+    for (int i = 0; i < n; i++) {
+        const hcgb_update &u = ups[i];
+        const bool ak = u.a.kind == HCGB_COMPRESSED, bk = u.b.kind == HCGB_COMPRESSED,
+                   ck = u.c.kind == HCGB_COMPRESSED;
+        const int m = u.c.rows, nn = u.c.cols;
+        const int ra = ak ? u.a.max_rank : 0, rb = bk ? u.b.max_rank : 0, rc = ck ? u.c.max_rank : 0;
+        s.ld = std::max({s.ld, m, nn, u.a.cols});
+        s.rmax = std::max({s.rmax, ra, rb});
+        auto grow = [&](int ph, int M, int N) {
+            s.p_m[ph] = std::max(s.p_m[ph], M);
+            s.p_n[ph] = std::max(s.p_n[ph], N);
+        };
+        if (ck) {
+            s.any_compressed_c = true;
+            if (ak && bk) {
+                s.kmax = std::max(s.kmax, rc + std::max(ra, rb));
+                grow(0, ra, rb);
+                grow(1, std::max(m, nn), std::max(ra, rb));
+            } else if (!ak && bk) {
+                s.kmax = std::max(s.kmax, rc + rb);
+                grow(0, m, rb);
+            } else if (ak && !bk) {
+                s.kmax = std::max(s.kmax, rc + ra);
+                grow(0, nn, ra);
+            }
+        } else {
+            if (ak && bk) {
+                grow(0, ra, rb);
+                grow(1, std::max(ra, m), std::max(nn, rb));
+            } else if (!ak && bk) {
+                grow(0, m, rb);
+            } else if (ak && !bk) {
+                grow(0, ra, nn);
+            }
+            grow(2, m, nn);
+        }
+    }
+    s.ld = (s.ld + 7) / 8 * 8;
+    return s;
+}
+
+size_t workspace_bytes_for(const Workspace &w, int n) {
+    return sizeof(double) * w.slot_doubles * (size_t) n + sizeof(int) * META_INTS * (size_t) n + 256;
+}
+
+Params to_params(const hcgb_params *p) {
+    Params q;
+    q.accuracy = p ? p->accuracy : 1e-9;
+    q.truncated = p ? p->truncated_svd : 0;
+    q.fixed_rank = p ? p->fixed_rank : 0;
+    q.side_mode = 1;
+    return q;
+}
+
+// Launch the full pipeline for n updates whose descriptors are already on the device.
+void launch_pipeline(const DevUpdate *dups, GemmJob *djobs, int n, double alpha, double beta, const Workspace &ws,
+                     const BatchShape &sh, const Params &p, int *status_dev, cudaStream_t st) {
+    launch_plan(dups, n, alpha, beta, ws, p, djobs, st);
+    if (sh.any_compressed_c) launch_stack(dups, n, alpha, beta, ws, st);
+    for (int ph = 0; ph < 3; ph++) launch_gemm_jobs(djobs + (size_t) ph * n, n, sh.p_m[ph], sh.p_n[ph], st);
+    if (sh.any_compressed_c) {
+        launch_qr(ws, n, st);
+        launch_core_svd(dups, n, ws, p, st);
+        launch_apply_q(dups, n, ws, st);
+    }
+    launch_finalize(dups, n, ws, status_dev, st);
+}
+
+int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, Workspace *out) {
+    Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, ddc);
+    size_t need = workspace_bytes_for(w, n);
+    int rc = ensure_device(ctx, &ctx->ws, &ctx->ws_bytes, need);
+    if (rc) return rc;
+    w.base = static_cast<double *>(ctx->ws);
+    w.meta = reinterpret_cast<int *>(static_cast<char *>(ctx->ws) + sizeof(double) * w.slot_doubles * (size_t) n);
+    *out = w;
+    return HCGB_OK;
+}
+
+// Upload `n` device update descriptors and make room for 3n jobs; returns device pointers.
+int upload_updates(hcgb_context *ctx, const std::vector<DevUpdate> &dv, DevUpdate **dups, GemmJob **djobs) {
+    const size_t n = dv.size();
+    const size_t ub = sizeof(DevUpdate) * n, jb = sizeof(GemmJob) * 3 * n;
+    const size_t ub_al = (ub + 255) / 256 * 256;
+    int rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb);
+    if (rc) return rc;
+    rc = ensure_stage(ctx, ub);
+    if (rc) return rc;
+    std::memcpy(ctx->stage, dv.data(), ub);
+    HCGB_CUDA(ctx, cudaMemcpyAsync(ctx->desc, ctx->stage, ub, cudaMemcpyHostToDevice, ctx->stream));
+    HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
+    *dups = static_cast<DevUpdate *>(ctx->desc);
+    *djobs = reinterpret_cast<GemmJob *>(static_cast<char *>(ctx->desc) + ub_al);
+    return HCGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hcgb_context_create(int device, void *stream, hcgb_context **out) {
+    if (!out) return HCGB_BAD_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return HCGB_CUDA_ERROR;
+    if (cudaSetDevice(device) != cudaSuccess) return HCGB_CUDA_ERROR;
+    auto *ctx = new hcgb_context();
+    ctx->device = device;
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    if (cudaEventCreateWithFlags(&ctx->stage_done, cudaEventDisableTiming) != cudaSuccess) {
+        delete ctx;
+        return HCGB_CUDA_ERROR;
+    }
+    *out = ctx;
+    return HCGB_OK;
+}
+
+int hcgb_context_destroy(hcgb_context *ctx) {
+    if (!ctx) return HCGB_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->ws) cudaFree(ctx->ws);
+    if (ctx->desc) cudaFree(ctx->desc);
+    if (ctx->stage) cudaFreeHost(ctx->stage);
+    if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
+    delete ctx;
+    return HCGB_OK;
+}
+
+int hcgb_context_set_stream(hcgb_context *ctx, void *stream) {
+    if (!ctx) return HCGB_BAD_ARG;
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    return HCGB_OK;
+}
+
+int hcgb_sync(hcgb_context *ctx) {
+    if (!ctx) return HCGB_BAD_ARG;
+    HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HCGB_OK;
+}
+
+const char *hcgb_last_error(hcgb_context *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+size_t hcgb_workspace_bytes(int n, int max_rows, int max_cols, int max_rank_c, int max_rank_ab) {
+    if (n <= 0) return 0;
+    int ld = std::max(max_rows, max_cols);
+    ld = (ld + 7) / 8 * 8;
+    Workspace w = make_workspace_layout(ld, max_rank_c + max_rank_ab, std::max(8, max_rank_ab), false);
+    return workspace_bytes_for(w, n);
+}
+
+int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const hcgb_update *updates,
+                    const hcgb_params *params, int *status_dev) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (n == 0) return HCGB_OK;
+    if (n < 0 || !updates) return fail(ctx, HCGB_BAD_ARG, "hcgb_gemm_batch: bad update list");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<DevUpdate> dv(n);
+    for (int i = 0; i < n; i++) {
+        int rc;
+        if ((rc = check_tile(ctx, updates[i].a, "A")) || (rc = check_tile(ctx, updates[i].b, "B")) ||
+            (rc = check_tile(ctx, updates[i].c, "C")))
+            return rc;
+        if (updates[i].a.kind == HCGB_DENSE && updates[i].b.kind == HCGB_DENSE &&
+            updates[i].c.kind == HCGB_COMPRESSED)
+            return fail(ctx, HCGB_UNSUPPORTED, "hcgb_gemm_batch: DDC updates go through hcgb_tile_gemm");
+        dv[i] = DevUpdate{to_dev(updates[i].a), to_dev(updates[i].b), to_dev(updates[i].c)};
+    }
+    BatchShape sh = shape_of(updates, n);
+    Workspace ws;
+    int rc = prepare_workspace(ctx, sh, n, false, &ws);
+    if (rc) return rc;
+    DevUpdate *dups;
+    GemmJob *djobs;
+    if ((rc = upload_updates(ctx, dv, &dups, &djobs))) return rc;
+    launch_pipeline(dups, djobs, n, alpha, beta, ws, sh, to_params(params), status_dev, ctx->stream);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const hcgb_tile *a_grid,
+                  const hcgb_tile *b_grid, double beta, const hcgb_tile *c_grid, const hcgb_params *params,
+                  int *status_dev) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (mt <= 0 || nt <= 0 || kt <= 0 || !a_grid || !b_grid || !c_grid)
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_tlr_gemm: bad grid");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int n = mt * nt;
+    // All waves' descriptors in one upload: wave kk holds (A(i,kk), B(kk,j), C(i,j)) for every C tile.
+    std::vector<hcgb_update> all((size_t) n * kt);
+    std::vector<DevUpdate> dv((size_t) n * kt);
+    for (int kk = 0; kk < kt; kk++)
+        for (int j = 0; j < nt; j++)
+            for (int i = 0; i < mt; i++) {
+                const size_t w = (size_t) kk * n + i + (size_t) j * mt;
+                hcgb_update u{a_grid[i + (size_t) kk * mt], b_grid[kk + (size_t) j * kt], c_grid[i + (size_t) j * mt]};
+                int rc;
+                if ((rc = check_tile(ctx, u.a, "A")) || (rc = check_tile(ctx, u.b, "B")) ||
+                    (rc = check_tile(ctx, u.c, "C")))
+                    return rc;
+                if (u.a.kind == HCGB_DENSE && u.b.kind == HCGB_DENSE && u.c.kind == HCGB_COMPRESSED)
+                    return fail(ctx, HCGB_UNSUPPORTED, "hcgb_tlr_gemm: DDC updates are not batched");
+                all[w] = u;
+                dv[w] = DevUpdate{to_dev(u.a), to_dev(u.b), to_dev(u.c)};
+            }
+    BatchShape sh = shape_of(all.data(), (int) all.size());
+    Workspace ws;
+    int rc = prepare_workspace(ctx, sh, n, false, &ws);
+    if (rc) return rc;
+    // Descriptor upload: DevUpdate[n*kt] then jobs for one wave (3n).
+    const size_t ub = sizeof(DevUpdate) * dv.size(), ub_al = (ub + 255) / 256 * 256;
+    const size_t jb = sizeof(GemmJob) * 3 * (size_t) n;
+    if ((rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb))) return rc;
+    if ((rc = ensure_stage(ctx, ub))) return rc;
+    std::memcpy(ctx->stage, dv.data(), ub);
+    HCGB_CUDA(ctx, cudaMemcpyAsync(ctx->desc, ctx->stage, ub, cudaMemcpyHostToDevice, ctx->stream));
+    HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
+    auto *dups = static_cast<DevUpdate *>(ctx->desc);
+    auto *djobs = reinterpret_cast<GemmJob *>(static_cast<char *>(ctx->desc) + ub_al);
+    const Params p = to_params(params);
+    for (int kk = 0; kk < kt; kk++) {
+        BatchShape shw = shape_of(all.data() + (size_t) kk * n, n);
+        shw.ld = sh.ld;
+        shw.kmax = sh.kmax;
+        shw.rmax = sh.rmax;
+        launch_pipeline(dups + (size_t) kk * n, djobs, n, alpha, beta, ws, shw, p,
+                        status_dev ? status_dev + (size_t) kk * n : nullptr, ctx->stream);
+    }
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The reference's flop count of one CompressedTile<T>::Gemm on the default (ungqr, non-trmm,
+// non-Cholesky) path, Compressed.cpp:335-625, including its integer arithmetic.
+unsigned long long reference_recompression_flops(size_t m, size_t n, size_t crk, size_t arank, size_t rk,
+                                                 bool fixed) {
+    const size_t Um = m, Un = arank + crk, Vm = n, Vn = Un;
+    const size_t minU = std::min(Um, Un), minV = std::min(Vm, Vn);
+    const size_t sizeS = std::min(std::min(m, n), Un);
+    size_t f = 0;
+    f += m * crk + m * arank + m * arank;
+    f += 2 * Um * Un * Un - (size_t) (2.0 * (float) Un * (float) Un * (float) Un / 3.0f) + 2 * Um * Un +
+         (size_t) (17 * (float) Un / 3.0f);
+    f += minU * ((Un + 1) / 2) * 2;
+    f += n * crk + n * arank;
+    f += 2 * Vm * Vn * Vn - (size_t) (2 * (float) Vn * (float) Vn * (float) Vn / 3.0f) + 2 * Vm * Vn +
+         (size_t) (17 * (float) Vn / 3.0f);
+    f += minV * ((Vn + 1) / 2) * 2;
+    f += minU * minV * Un;
+    f += 22 * minV * minV * minV;
+    if (!fixed) f += sizeS;
+    f += (8 / 3) * (size_t) ((double) minU * (double) minU) * (3 * Um - minU);
+    f += Um * rk * minU;
+    f += rk;
+    f += (8 / 3) * (size_t) ((double) minV * (double) minV) * (3 * Vm - minV);
+    f += Vm * rk * minV;
+    return f;
+}
+
+struct TempTile {
+    double *buf = nullptr;
+    int *rank = nullptr;
+};
+
+// op(T) as an explicit tile: dense -> transposed copy; compressed (U, V) -> (V^T, U^T).
+int transposed_tile(hcgb_context *ctx, const hcgb_tile &t, int rank, hcgb_tile *out, TempTile *tmp) {
+    *out = t;
+    out->rows = t.cols;
+    out->cols = t.rows;
+    if (t.kind == HCGB_DENSE) {
+        HCGB_CUDA(ctx, cudaMalloc(&tmp->buf, sizeof(double) * (size_t) t.rows * t.cols));
+        launch_transpose(t.data, t.rows, t.rows, t.cols, tmp->buf, t.cols, ctx->stream);
+        out->data = tmp->buf;
+        return HCGB_OK;
+    }
+    const size_t cap = (size_t) t.cols * t.max_rank + (size_t) t.max_rank * t.rows;
+    HCGB_CUDA(ctx, cudaMalloc(&tmp->buf, sizeof(double) * cap));
+    // new U (cols x rank, ld cols) = V^T, new V (rank x rows, ld rank) = U^T
+    const double *U = t.data, *V = t.data + (size_t) t.rows * t.max_rank;
+    launch_transpose(V, rank, rank, t.cols, tmp->buf, t.cols, ctx->stream);
+    launch_transpose(U, t.rows, t.rows, rank, tmp->buf + (size_t) t.cols * t.max_rank, rank, ctx->stream);
+    out->data = tmp->buf;
+    out->rank = t.rank;  // the rank itself is unchanged
+    return HCGB_OK;
+}
+
+int read_rank(hcgb_context *ctx, const hcgb_tile &t, int *r) {
+    *r = 0;
+    if (t.kind != HCGB_COMPRESSED) return HCGB_OK;
+    HCGB_CUDA(ctx, cudaMemcpyAsync(r, t.rank, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HCGB_OK;
+}
+
+}  // namespace
+
+extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *a, int op_a, const hcgb_tile *b,
+                              int op_b, double beta, hcgb_tile *c, const hcgb_params *params, int *new_rank,
+                              unsigned long long *flops) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (!a || !b || !c) return fail(ctx, HCGB_BAD_ARG, "hcgb_tile_gemm: null tile");
+    if ((op_a != HCGB_NOTRANS && op_a != HCGB_TRANS) || (op_b != HCGB_NOTRANS && op_b != HCGB_TRANS))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_tile_gemm: op must be NoTrans or Trans");
+    int rc;
+    if ((rc = check_tile(ctx, *a, "A")) || (rc = check_tile(ctx, *b, "B")) || (rc = check_tile(ctx, *c, "C")))
+        return rc;
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    int ra, rb, rcank;
+    if ((rc = read_rank(ctx, *a, &ra)) || (rc = read_rank(ctx, *b, &rb)) || (rc = read_rank(ctx, *c, &rcank)))
+        return rc;
+    TempTile ta, tb;
+    hcgb_tile A = *a, B = *b;
+    if (op_a == HCGB_TRANS && (rc = transposed_tile(ctx, *a, ra, &A, &ta))) return rc;
+    if (op_b == HCGB_TRANS && (rc = transposed_tile(ctx, *b, rb, &B, &tb))) return rc;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(ctx->stream);
+        if (ta.buf) cudaFree(ta.buf);
+        if (tb.buf) cudaFree(tb.buf);
+    };
+    if (A.cols != B.rows || A.rows != c->rows || B.cols != c->cols) {
+        cleanup();
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_tile_gemm: shapes of op(A), op(B) and C do not match");
+    }
+    const size_t m = c->rows, n = c->cols, kd = A.cols;
+    const bool ak = A.kind == HCGB_COMPRESSED, bk = B.kind == HCGB_COMPRESSED, ck = c->kind == HCGB_COMPRESSED;
+    unsigned long long fl = 0;
+    int out_rank = 0;
+    if (!ak && !bk && ck) {
+        // DDC (HCore.cpp:272-299): W = alpha A B + beta Cu Cv, C <- U = W, V = I at rank min(m, n).
+        const int r = (int) std::min(m, n);
+        if (c->max_rank < r) {
+            cleanup();
+            return fail(ctx, HCGB_RANK_OVERFLOW, "hcgb_tile_gemm: DDC needs max_rank >= min(rows, cols)");
+        }
+        hcgb_update u{A, B, *c};
+        BatchShape sh = shape_of(&u, 1);
+        Workspace ws;
+        if ((rc = prepare_workspace(ctx, sh, 1, true, &ws))) {
+            cleanup();
+            return rc;
+        }
+        std::vector<DevUpdate> dv{DevUpdate{to_dev(A), to_dev(B), to_dev(*c)}};
+        DevUpdate *dups;
+        GemmJob *djobs;
+        if ((rc = upload_updates(ctx, dv, &dups, &djobs))) {
+            cleanup();
+            return rc;
+        }
+        GemmJob j[3];
+        std::memset(j, 0, sizeof(j));
+        double *W = ws.base + ws.off_tmp2;
+        const double *Cu = c->data, *Cv = c->data + m * (size_t) c->max_rank;
+        j[0] = GemmJob{Cu, Cv, W, (int) m, (int) n, rcank, (int) m, std::max(1, rcank), ws.ld, 0, 0, beta, 0.0};
+        j[1] = GemmJob{A.data, B.data, W, (int) m, (int) n, (int) kd, (int) m, (int) kd, ws.ld, 0, 0, alpha, 1.0};
+        if ((rc = ensure_stage(ctx, sizeof(j)))) {
+            cleanup();
+            return rc;
+        }
+        std::memcpy(ctx->stage, j, sizeof(j));
+        HCGB_CUDA(ctx, cudaMemcpyAsync(djobs, ctx->stage, sizeof(j), cudaMemcpyHostToDevice, ctx->stream));
+        HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
+        launch_gemm_jobs(djobs, 1, (int) m, (int) n, ctx->stream);
+        launch_gemm_jobs(djobs + 1, 1, (int) m, (int) n, ctx->stream);
+        launch_ddc_finalize(dups, 1, ws, ctx->stream);
+        HCGB_CUDA(ctx, cudaGetLastError());
+        fl = 2ull * m * n * kd + 2ull * m * n * (unsigned long long) rcank;
+        out_rank = r;
+    } else {
+        hcgb_update u{A, B, *c};
+        int *dstatus = nullptr;
+        HCGB_CUDA(ctx, cudaMalloc(&dstatus, sizeof(int)));
+        rc = hcgb_gemm_batch(ctx, alpha, beta, 1, &u, params, dstatus);
+        int hstatus = HCGB_OK;
+        if (rc == HCGB_OK) {
+            HCGB_CUDA(ctx, cudaMemcpyAsync(&hstatus, dstatus, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            if (ck) HCGB_CUDA(ctx, cudaMemcpyAsync(&out_rank, c->rank, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        }
+        cudaFree(dstatus);
+        if (rc) {
+            cleanup();
+            return rc;
+        }
+        if (hstatus != HCGB_OK && hstatus != HCGB_NOT_CONVERGED) {
+            cleanup();
+            return fail(ctx, hstatus, "hcgb_tile_gemm: update rejected on the device");
+        }
+        // Temporary dense products (Dense.cpp:66-67: 2 * m * n * A.cols each), then the recompression.
+        const size_t arank = ak && bk ? (size_t) ra : (!ak && bk ? (size_t) rb : (size_t) ra);
+        if (ak && bk) fl += 2ull * ra * rb * kd + 2ull * ra * n * rb;
+        else if (!ak && bk) fl += 2ull * m * rb * kd;
+        else if (ak && !bk) fl += 2ull * ra * n * kd;
+        if (ck) fl += reference_recompression_flops(m, n, rcank, arank, out_rank, params && params->fixed_rank);
+        else fl += 2ull * m * n * (ak ? (unsigned long long) ra : (bk ? rb : kd));
+        if (hstatus == HCGB_NOT_CONVERGED) ctx->last_error = "hcgb_tile_gemm: Jacobi sweep limit reached";
+        rc = hstatus;
+    }
+    cleanup();
+    if (new_rank) *new_rank = ck ? out_rank : 0;
+    if (flops) *flops += fl;
+    return rc;
+}

@@ -1,0 +1,124 @@
+// Internal declarations shared by the CUDA translation units of libhcgb.
+//
+// Execution model of one batched call (a "wave" of independent tile updates, one
+// update per C tile):
+//   plan      : read the device-side ranks, choose the stacking side, and resolve
+//               every factor product into a GemmJob (no host round trip)
+//   stack     : copy/scale/transpose the C factors into the stacked bases
+//               U = [Cu | alpha*Ua'] (m x k), V = [beta*Cv^T | Vb'] (n x k)
+//   gemm x3   : the factor products (FP64 DMMA), written straight into the stacks
+//               (or into a dense C)
+//   qr        : blocked Householder QR of both stacks (panel SIMT, trailing DMMA)
+//   core_svd  : M = R_U R_V^T, one-sided Jacobi, rank truncation, new left vectors
+//   apply_q   : new U = Q_U [Ut_r; 0], new V^T = Q_V [M^T Ut_r; 0] (DMMA)
+//   finalize  : transpose V into the tile buffer, publish the new rank
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+#include "hcgb.h"
+
+namespace hcgb {
+
+constexpr int QR_NB = 16;          // Householder panel width (columns)
+constexpr int MAX_JACOBI_SWEEPS = 40;
+
+// FP64 tensor-core MMA (the only FP64 tensor path on sm_103a): {d0,d1} += a * b for an
+// 8x8x4 tile.  Fragment layout (PTX ISA, mma.m8n8k4 .f64):
+//   a : A[lane/4][lane%4]        (8 x 4, row)
+//   b : B[lane%4][lane/4]        (4 x 8, col)
+//   d : D[lane/4][2*(lane%4)+e]  (8 x 8), e = 0, 1
+__device__ __forceinline__ void dmma(double &d0, double &d1, double a, double b) {
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                 : "+d"(d0), "+d"(d1)
+                 : "d"(a), "d"(b));
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// C = alpha * op(A) * op(B) + beta * C  (column-major; op 0 = N, 1 = T).  M <= 0: no job.
+struct GemmJob {
+    const double *A;
+    const double *B;
+    double *C;
+    int M, N, K;
+    int lda, ldb, ldc;
+    int opA, opB;
+    double alpha, beta;
+};
+
+struct DevTile {
+    double *data;
+    int *rank;
+    int rows, cols, max_rank, kind;
+};
+
+struct DevUpdate {
+    DevTile a, b, c;
+};
+
+// Per-update bookkeeping written by the plan kernel and read by the later stages.
+enum MetaField {
+    META_STATUS = 0,
+    META_CKIND,      // 1 when C is compressed (recompression needed)
+    META_RA,
+    META_RB,
+    META_RC,
+    META_SIDE,       // 0: stack [Cu | alpha Au], 1: stack [Cu | alpha Au (Av Bu)]
+    META_K,          // columns of both stacks
+    META_M,          // rows of C / of the U stack
+    META_N,          // cols of C / rows of the V stack
+    META_NEWRANK,
+    META_SWEEPS,
+    META_INTS = 16
+};
+
+// Device workspace: n slots of `slot_doubles` doubles plus an int meta block.
+struct Workspace {
+    double *base;
+    int *meta;            // n * META_INTS
+    size_t slot_doubles;
+    int ld;               // leading dimension of every stack / temporary (>= rows, cols)
+    int kmax;             // max columns of a stack
+    int rmax;             // max rank of an A/B factor
+    size_t off_ustack, off_vstack, off_tmp1, off_tmp2, off_tauu, off_tauv, off_tu, off_tv;
+    size_t off_m, off_mcopy, off_xv, off_sigma;
+
+    __host__ __device__ double *slot(int s) const { return base + slot_doubles * (size_t) s; }
+};
+
+// Layout of one workspace slot for stacks of up to `ld` rows and `kmax` columns; factor ranks
+// up to `rmax`.  ddc_scratch reserves an ld x ld product for the DDC combination.
+Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch);
+
+struct Params {
+    double accuracy;
+    int truncated;
+    int fixed_rank;
+    int side_mode;   // 0: always the reference's [Cu | alpha Au]; 1: pick the smaller stack
+};
+
+// ---- launchers (stream-ordered, asynchronous) ----
+void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p, GemmJob *jobs,
+                 cudaStream_t st);
+void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, cudaStream_t st);
+void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st);
+void launch_qr(Workspace ws, int n, cudaStream_t st);
+void launch_core_svd(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st);
+void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st);
+void launch_finalize(const DevUpdate *ups, int n, Workspace ws, int *status_dev, cudaStream_t st);
+// DDC (dense A, dense B, compressed C): C <- full rank, U = alpha A B + beta Cu Cv, V = I.
+void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st);
+// dst (cols x rows, ld ldd) = src^T (src rows x cols, ld lds); one CTA.
+void launch_transpose(const double *src, int lds, int rows, int cols, double *dst, int ldd, cudaStream_t st);
+
+size_t qr_smem_bytes(int ld, int kmax);
+size_t svd_smem_bytes(int kmax);
+
+}  // namespace hcgb

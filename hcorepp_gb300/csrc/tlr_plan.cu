@@ -1,0 +1,365 @@
+// Planning, stacking, factor products (FP64 DMMA GEMM) and write-back of a batch of
+// TLR tile updates.  Follows HCore<T>::Gemm's dispatch (src/api/HCore.cpp:23-344) and the
+// stacking of CompressedTile<T>::Gemm (src/operators/concrete/Compressed.cpp:331-379).
+#include "internal.cuh"
+
+namespace hcgb {
+
+namespace {
+
+__device__ __forceinline__ GemmJob make_job(const double *A, int lda, int opA, const double *B, int ldb, int opB,
+                                            double *C, int ldc, int M, int N, int K, double alpha, double beta) {
+    GemmJob j;
+    j.A = A;
+    j.B = B;
+    j.C = C;
+    j.M = M;
+    j.N = N;
+    j.K = K;
+    j.lda = lda < 1 ? 1 : lda;
+    j.ldb = ldb < 1 ? 1 : ldb;
+    j.ldc = ldc < 1 ? 1 : ldc;
+    j.opA = opA;
+    j.opB = opB;
+    j.alpha = alpha;
+    j.beta = beta;
+    return j;
+}
+
+// One thread per update: read ranks on the device, validate, choose the stacking side and
+// emit up to three dependent GEMM jobs (phase 1, 2, 3).
+__global__ void plan_kernel(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p,
+                            GemmJob *jobs) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const DevUpdate u = ups[s];
+    int *meta = ws.meta + (size_t) s * META_INTS;
+    GemmJob none;
+    none.M = 0;
+    none.N = 0;
+    none.K = 0;
+    jobs[s] = none;
+    jobs[n + s] = none;
+    jobs[2 * n + s] = none;
+    for (int f = 0; f < META_INTS; f++) meta[f] = 0;
+
+    const int ak = u.a.kind, bk = u.b.kind, ck = u.c.kind;
+    const int rA = ak ? *u.a.rank : 0;
+    const int rB = bk ? *u.b.rank : 0;
+    const int rC = ck ? *u.c.rank : 0;
+    const int m = u.c.rows, nn = u.c.cols, kd = u.a.cols;
+    int status = HCGB_OK;
+    if (u.a.rows != m || u.b.cols != nn || u.b.rows != kd) status = HCGB_BAD_ARG;
+    if ((ak && (rA < 0 || rA > u.a.max_rank)) || (bk && (rB < 0 || rB > u.b.max_rank)) ||
+        (ck && (rC < 0 || rC > u.c.max_rank)))
+        status = HCGB_RANK_OVERFLOW;
+    if (!ak && !bk && ck) status = HCGB_UNSUPPORTED;  // DDC: hcgb_tile_gemm only
+    if (m > ws.ld || nn > ws.ld || rA > ws.rmax || rB > ws.rmax) status = HCGB_POOL_TOO_SMALL;
+    meta[META_CKIND] = ck;
+    meta[META_RA] = rA;
+    meta[META_RB] = rB;
+    meta[META_RC] = rC;
+    meta[META_M] = m;
+    meta[META_N] = nn;
+    if (status != HCGB_OK) {
+        meta[META_STATUS] = status;
+        return;
+    }
+    double *slot = ws.slot(s);
+    double *Us = slot + ws.off_ustack;
+    double *Vs = slot + ws.off_vstack;
+    double *T1 = slot + ws.off_tmp1;  // rmax x rmax, ld rmax
+    double *T2 = slot + ws.off_tmp2;  // ld x rmax (ld ld) or rmax x ld (ld rmax)
+    const int ld = ws.ld, lr = ws.rmax;
+    // Compressed views: U at data (ld rows), V at data + rows*max_rank (ld rank).
+    const double *Au = u.a.data, *Av = u.a.data + (size_t) u.a.rows * u.a.max_rank;
+    const double *Bu = u.b.data, *Bv = u.b.data + (size_t) u.b.rows * u.b.max_rank;
+    const double *Ad = u.a.data, *Bd = u.b.data;
+
+    if (ck) {
+        int side = 0, k = 0;
+        if (ak && bk) {
+            side = (p.side_mode && rB < rA) ? 1 : 0;
+            jobs[s] = make_job(Av, rA, 0, Bu, kd, 0, T1, lr, rA, rB, kd, 1.0, 0.0);  // T1 = Av Bu
+            if (side == 0) {
+                // V[:, rC:rC+rA] = (T1 Bv)^T = Bv^T T1^T   (ProcessVpointer's B part)
+                jobs[n + s] = make_job(Bv, rB, 1, T1, lr, 1, Vs + (size_t) rC * ld, ld, nn, rA, rB, 1.0, 0.0);
+                k = rC + rA;
+            } else {
+                // U[:, rC:rC+rB] = alpha Au T1
+                jobs[n + s] = make_job(Au, m, 0, T1, lr, 0, Us + (size_t) rC * ld, ld, m, rB, rA, alpha, 0.0);
+                k = rC + rB;
+            }
+        } else if (!ak && bk) {
+            side = 1;  // DCC: U[:, rC:] = alpha A Bu, V[:, rC:] = Bv^T (HCore.cpp:234-245)
+            jobs[s] = make_job(Ad, m, 0, Bu, kd, 0, Us + (size_t) rC * ld, ld, m, rB, kd, alpha, 0.0);
+            k = rC + rB;
+        } else {
+            side = 0;  // CDC: U[:, rC:] = alpha Au, V[:, rC:] = (Av B)^T = B^T Av^T (HCore.cpp:246-257)
+            jobs[s] = make_job(Bd, kd, 1, Av, rA, 1, Vs + (size_t) rC * ld, ld, nn, rA, kd, 1.0, 0.0);
+            k = rC + rA;
+        }
+        if (k > ws.kmax) status = HCGB_POOL_TOO_SMALL;
+        if (k == 0) status = HCGB_BAD_ARG;
+        meta[META_SIDE] = side;
+        meta[META_K] = k;
+        if (status != HCGB_OK) {
+            jobs[s] = none;
+            jobs[n + s] = none;
+            meta[META_STATUS] = status;
+        }
+        return;
+    }
+    // Dense C: plain GEMM chains, C <- alpha * left * right + beta * C.
+    double *C = u.c.data;
+    if (ak && bk) {
+        jobs[s] = make_job(Av, rA, 0, Bu, kd, 0, T1, lr, rA, rB, kd, 1.0, 0.0);
+        if (!p.side_mode || rA <= rB) {
+            // HCore.cpp:178-264: T2 = T1 Bv, C = alpha Au T2 + beta C
+            jobs[n + s] = make_job(T1, lr, 0, Bv, rB, 0, T2, lr, rA, nn, rB, 1.0, 0.0);
+            jobs[2 * n + s] = make_job(Au, m, 0, T2, lr, 0, C, m, m, nn, rA, alpha, beta);
+        } else {
+            jobs[n + s] = make_job(Au, m, 0, T1, lr, 0, T2, ld, m, rB, rA, 1.0, 0.0);
+            jobs[2 * n + s] = make_job(T2, ld, 0, Bv, rB, 0, C, m, m, nn, rB, alpha, beta);
+        }
+    } else if (!ak && bk) {
+        jobs[s] = make_job(Ad, m, 0, Bu, kd, 0, T2, ld, m, rB, kd, 1.0, 0.0);  // DCD
+        jobs[2 * n + s] = make_job(T2, ld, 0, Bv, rB, 0, C, m, m, nn, rB, alpha, beta);
+    } else if (ak && !bk) {
+        jobs[s] = make_job(Av, rA, 0, Bd, kd, 0, T2, lr, rA, nn, kd, 1.0, 0.0);  // CDD
+        jobs[2 * n + s] = make_job(Au, m, 0, T2, lr, 0, C, m, m, nn, rA, alpha, beta);
+    } else {
+        jobs[2 * n + s] = make_job(Ad, m, 0, Bd, kd, 0, C, m, m, nn, kd, alpha, beta);  // DDD
+    }
+}
+
+// dst[j + i*ldd] = scale * src[i + j*lds] for i < rows(src), j < cols(src): a transposed copy
+// through a 32x33 shared tile so that both sides stay coalesced.
+__device__ void transpose_scaled(const double *src, int lds, int rows, int cols, double *dst, int ldd,
+                                 double scale, double (*tile)[33]) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
+    for (int i0 = 0; i0 < rows; i0 += 32)
+        for (int j0 = 0; j0 < cols; j0 += 32) {
+            for (int jj = ty; jj < 32; jj += nty) {
+                int i = i0 + tx, j = j0 + jj;
+                tile[jj][tx] = (i < rows && j < cols) ? src[i + (size_t) j * lds] : 0.0;
+            }
+            __syncthreads();
+            for (int ii = ty; ii < 32; ii += nty) {
+                int i = i0 + ii, j = j0 + tx;
+                if (i < rows && j < cols) dst[j + (size_t) i * ldd] = scale * tile[tx][ii];
+            }
+            __syncthreads();
+        }
+}
+
+__device__ void copy_scaled(const double *src, int lds, int rows, int cols, double *dst, int ldd, double scale) {
+    for (int j = 0; j < cols; j++)
+        for (int i = threadIdx.x; i < rows; i += blockDim.x)
+            dst[i + (size_t) j * ldd] = scale * src[i + (size_t) j * lds];
+}
+
+// One CTA per update: the parts of the stacks that are copies of existing factors
+// (LaCpy + MultiplyByAlpha + ProcessVpointer, Compressed.cpp:331-379).
+__global__ void __launch_bounds__(256) stack_kernel(const DevUpdate *ups, double alpha, double beta, Workspace ws) {
+    __shared__ double tile[32][33];
+    const int s = blockIdx.x;
+    const int *meta = ws.meta + (size_t) s * META_INTS;
+    if (meta[META_STATUS] != HCGB_OK || !meta[META_CKIND]) return;
+    const DevUpdate u = ups[s];
+    const int m = meta[META_M], nn = meta[META_N], rA = meta[META_RA], rB = meta[META_RB], rC = meta[META_RC];
+    const int side = meta[META_SIDE];
+    double *slot = ws.slot(s);
+    double *Us = slot + ws.off_ustack;
+    double *Vs = slot + ws.off_vstack;
+    const int ld = ws.ld;
+    const double *Cu = u.c.data, *Cv = u.c.data + (size_t) u.c.rows * u.c.max_rank;
+    copy_scaled(Cu, m, m, rC, Us, ld, 1.0);                                      // U[:, :rC] = Cu
+    if (side == 0 && u.a.kind) copy_scaled(u.a.data, m, m, rA, Us + (size_t) rC * ld, ld, alpha);  // alpha Au
+    transpose_scaled(Cv, rC, rC, nn, Vs, ld, beta, tile);                        // V[:, :rC] = beta Cv^T
+    if (side == 1 && u.b.kind) {
+        const double *Bv = u.b.data + (size_t) u.b.rows * u.b.max_rank;
+        transpose_scaled(Bv, rB, rB, nn, Vs + (size_t) rC * ld, ld, 1.0, tile);  // V[:, rC:] = Bv^T
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Batched FP64 GEMM on DMMA: one 64x64 tile of C per CTA, 4 warps (2x2) of 32x32, k-chunks
+// of 16 staged in shared memory.  Grid: x = tile index within the job, y = job.
+// ---------------------------------------------------------------------------------------
+constexpr int GT = 64, GK = 16, AS_LD = GK + 4, BS_LD = GT + 4;
+
+__global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
+    const GemmJob jb = jobs[blockIdx.y];
+    if (jb.M <= 0 || jb.N <= 0) return;
+    const int ntm = (jb.M + GT - 1) / GT, ntn = (jb.N + GT - 1) / GT;
+    if ((int) blockIdx.x >= ntm * ntn) return;
+    const int m0 = (blockIdx.x % ntm) * GT, n0 = (blockIdx.x / ntm) * GT;
+    __shared__ double As[GT][AS_LD];
+    __shared__ double Bs[GK][BS_LD];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = warp & 1, wn = warp >> 1;
+    const int lr = lane >> 2, lc = lane & 3;
+    double acc[4][4][2];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j][0] = acc[i][j][1] = 0.0;
+
+    for (int k0 = 0; k0 < jb.K; k0 += GK) {
+        for (int e = threadIdx.x; e < GT * GK; e += blockDim.x) {
+            int i, kk;
+            if (jb.opA == 0) {
+                i = e % GT;
+                kk = e / GT;
+            } else {
+                kk = e % GK;
+                i = e / GK;
+            }
+            const int gi = m0 + i, gk = k0 + kk;
+            double v = 0.0;
+            if (gi < jb.M && gk < jb.K)
+                v = jb.opA == 0 ? jb.A[gi + (size_t) gk * jb.lda] : jb.A[gk + (size_t) gi * jb.lda];
+            As[i][kk] = v;
+        }
+        for (int e = threadIdx.x; e < GT * GK; e += blockDim.x) {
+            int j, kk;
+            if (jb.opB == 0) {
+                kk = e % GK;
+                j = e / GK;
+            } else {
+                j = e % GT;
+                kk = e / GT;
+            }
+            const int gj = n0 + j, gk = k0 + kk;
+            double v = 0.0;
+            if (gj < jb.N && gk < jb.K)
+                v = jb.opB == 0 ? jb.B[gk + (size_t) gj * jb.ldb] : jb.B[gj + (size_t) gk * jb.ldb];
+            Bs[kk][j] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GK; kk += 4) {
+            double af[4], bf[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) af[i] = As[wm * 32 + i * 8 + lr][kk + lc];
+#pragma unroll
+            for (int j = 0; j < 4; j++) bf[j] = Bs[kk + lc][wn * 32 + j * 8 + lr];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int row = m0 + wm * 32 + i * 8 + lr;
+                const int col = n0 + wn * 32 + j * 8 + 2 * lc + e;
+                if (row < jb.M && col < jb.N) {
+                    double *c = jb.C + row + (size_t) col * jb.ldc;
+                    double v = jb.alpha * acc[i][j][e];
+                    if (jb.beta != 0.0) v += jb.beta * *c;
+                    *c = v;
+                }
+            }
+}
+
+// One CTA per update: V (r x n, ld r) = XV^T into the tile buffer, publish rank and status.
+__global__ void __launch_bounds__(256) finalize_kernel(const DevUpdate *ups, Workspace ws, int *status_dev) {
+    __shared__ double tile[32][33];
+    const int s = blockIdx.x;
+    const int *meta = ws.meta + (size_t) s * META_INTS;
+    const int status = meta[META_STATUS];
+    if (status_dev && threadIdx.x == 0) status_dev[s] = status;
+    if (status != HCGB_OK && status != HCGB_NOT_CONVERGED) return;
+    if (!meta[META_CKIND]) return;
+    const DevUpdate u = ups[s];
+    const int r = meta[META_NEWRANK], nn = meta[META_N];
+    const double *XV = ws.slot(s) + ws.off_xv;
+    double *Cv = u.c.data + (size_t) u.c.rows * u.c.max_rank;
+    transpose_scaled(XV, ws.ld, nn, r, Cv, r, 1.0, tile);
+    if (threadIdx.x == 0) *u.c.rank = r;
+}
+
+// DDC: W = alpha A B + beta Cu Cv sits in the tmp2 region (ld ws.ld); C <- [U = W | V = I].
+__global__ void __launch_bounds__(256) ddc_finalize_kernel(const DevUpdate *ups, Workspace ws) {
+    const int s = blockIdx.x;
+    const DevUpdate u = ups[s];
+    const int m = u.c.rows, nn = u.c.cols;
+    const int r = m < nn ? m : nn;
+    const double *W = ws.slot(s) + ws.off_tmp2;
+    double *U = u.c.data;
+    double *V = u.c.data + (size_t) m * u.c.max_rank;
+    for (int j = 0; j < r; j++)
+        for (int i = threadIdx.x; i < m; i += blockDim.x) U[i + (size_t) j * m] = W[i + (size_t) j * ws.ld];
+    for (int j = 0; j < nn; j++)
+        for (int i = threadIdx.x; i < r; i += blockDim.x) V[i + (size_t) j * r] = (i == j) ? 1.0 : 0.0;
+    if (threadIdx.x == 0) *u.c.rank = r;
+}
+
+__global__ void __launch_bounds__(256) transpose_kernel(const double *src, int lds, int rows, int cols, double *dst,
+                                                      int ldd) {
+    __shared__ double tile[32][33];
+    transpose_scaled(src, lds, rows, cols, dst, ldd, 1.0, tile);
+}
+
+}  // namespace
+
+void launch_transpose(const double *src, int lds, int rows, int cols, double *dst, int ldd, cudaStream_t st) {
+    transpose_kernel<<<1, 256, 0, st>>>(src, lds, rows, cols, dst, ldd);
+}
+
+void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p, GemmJob *jobs,
+                 cudaStream_t st) {
+    plan_kernel<<<(n + 127) / 128, 128, 0, st>>>(ups, n, alpha, beta, ws, p, jobs);
+}
+
+void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, cudaStream_t st) {
+    stack_kernel<<<n, 256, 0, st>>>(ups, alpha, beta, ws);
+}
+
+void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st) {
+    if (njobs <= 0 || max_m <= 0 || max_n <= 0) return;
+    const int tiles = ((max_m + GT - 1) / GT) * ((max_n + GT - 1) / GT);
+    dim3 grid(tiles, njobs);
+    gemm_jobs_kernel<<<grid, 128, 0, st>>>(jobs);
+}
+
+void launch_finalize(const DevUpdate *ups, int n, Workspace ws, int *status_dev, cudaStream_t st) {
+    finalize_kernel<<<n, 256, 0, st>>>(ups, ws, status_dev);
+}
+
+void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st) {
+    ddc_finalize_kernel<<<n, 256, 0, st>>>(ups, ws);
+}
+
+Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch) {
+    Workspace w{};
+    w.ld = ld;
+    w.kmax = kmax;
+    w.rmax = rmax;
+    auto round = [](size_t x) { return (x + 31) & ~size_t(31); };  // 256-byte aligned sub-buffers
+    size_t off = 0;
+    const int npan = (kmax + QR_NB - 1) / QR_NB;
+    w.off_ustack = off; off += round((size_t) ld * kmax);
+    w.off_vstack = off; off += round((size_t) ld * kmax);
+    w.off_tmp1 = off;   off += round((size_t) rmax * rmax);
+    w.off_tmp2 = off;   off += round((size_t) ld * (size_t) (ddc_scratch ? (rmax > ld ? rmax : ld) : rmax));
+    w.off_tauu = off;   off += round(kmax);
+    w.off_tauv = off;   off += round(kmax);
+    w.off_tu = off;     off += round((size_t) npan * QR_NB * QR_NB);
+    w.off_tv = off;     off += round((size_t) npan * QR_NB * QR_NB);
+    w.off_m = off;      off += round((size_t) kmax * kmax);
+    w.off_mcopy = off;  off += round((size_t) kmax * kmax);
+    w.off_xv = off;     off += round((size_t) ld * kmax);
+    w.off_sigma = off;  off += round(kmax);
+    w.slot_doubles = off;
+    return w;
+}
+
+}  // namespace hcgb

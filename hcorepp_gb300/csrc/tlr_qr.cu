@@ -1,0 +1,324 @@
+// Batched blocked Householder QR of the stacked factors and application of the resulting Q.
+//
+// Replaces HCoreKernels::Geqrf / ungqr / Unmqr on the TLR GEMM path
+// (src/operators/concrete/Compressed.cpp:353, :384, :551, :611; LAPACK dgeqrf/dorgqr semantics:
+// R on and above the diagonal, unit-lower reflectors below it, tau_j = 2 / (v_j^T v_j)).
+//
+// One CTA per matrix.  The matrix stays in device memory (L2-resident working set); each
+// panel of QR_NB columns is staged in shared memory and factored there with SIMT FP64 and
+// warp-shuffle norms; the compact-WY factor T (Q_panel = I - V T V^T, LAPACK dlarft) is
+// kept for the later Q application; the trailing update A <- (I - V T^T V^T) A is two FP64
+// tensor-core (DMMA) products with V and W = V^T A staged in shared memory.
+#include "internal.cuh"
+
+namespace hcgb {
+
+namespace {
+
+constexpr int NB = QR_NB;
+constexpr int QR_THREADS = 256;
+
+__host__ __device__ __forceinline__ int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// Block-wide sum; `red` holds >= 33 doubles.  Must be called by all threads.
+__device__ double block_sum(double v, double *red) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double t = lane < nw ? red[lane] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// Householder QR of the panel in shared memory: column c at Ps + c*ldp, rows 0..mr-1.
+// LAPACK dlarfg convention: beta = -sign(alpha) * ||x||, tau = (beta - alpha) / beta,
+// v = x / (alpha - beta) with v_0 = 1 implicit; tau = 0 when the tail is zero.
+__device__ void factor_panel(double *Ps, int ldp, int mr, int nbp, double *tau_s, double *red) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int j = 0; j < nbp; j++) {
+        double *x = Ps + (size_t) j * ldp;
+        double ss = 0.0;
+        for (int r = j + 1 + threadIdx.x; r < mr; r += blockDim.x) ss = fma(x[r], x[r], ss);
+        ss = block_sum(ss, red);
+        if (threadIdx.x == 0) {
+            const double alpha = x[j];
+            double tau = 0.0, scale = 0.0, beta = alpha;
+            if (ss != 0.0) {
+                beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
+                tau = (beta - alpha) / beta;
+                scale = 1.0 / (alpha - beta);
+            }
+            tau_s[j] = tau;
+            red[40] = scale;
+            x[j] = beta;
+        }
+        __syncthreads();
+        const double scale = red[40], tau = tau_s[j];
+        for (int r = j + 1 + threadIdx.x; r < mr; r += blockDim.x) x[r] *= scale;
+        __syncthreads();
+        if (tau != 0.0) {
+            for (int c = j + 1 + warp; c < nbp; c += nw) {
+                double *y = Ps + (size_t) c * ldp;
+                double w = lane == 0 ? y[j] : 0.0;
+                for (int r = j + 1 + lane; r < mr; r += 32) w = fma(x[r], y[r], w);
+                w = warp_sum(w) * tau;
+                if (lane == 0) y[j] -= w;
+                for (int r = j + 1 + lane; r < mr; r += 32) y[r] = fma(-w, x[r], y[r]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Overwrite the panel with the explicit unit-lower V (zeros above the diagonal, zero padding).
+__device__ void make_explicit_v(double *Ps, int ldp, int nbp) {
+    for (int e = threadIdx.x; e < NB * ldp; e += blockDim.x) {
+        const int c = e / ldp, r = e % ldp;
+        if (c >= nbp) Ps[e] = 0.0;
+        else if (r < c) Ps[e] = 0.0;
+        else if (r == c) Ps[e] = 1.0;
+    }
+}
+
+// Compact-WY T of the panel (LAPACK dlarft, forward / columnwise):
+// T[i][i] = tau_i,  T[0:i, i] = -tau_i * T[0:i, 0:i] * (V[:, 0:i]^T v_i).  Ps holds explicit V.
+__device__ void build_t(const double *Ps, int ldp, int mr, int nbp, const double *tau_s, double *Ts, double *Gs) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) Ts[e] = 0.0;
+    const int npairs = nbp * (nbp - 1) / 2;
+    for (int p = warp; p < npairs; p += nw) {
+        int i = 1, base = 0;
+        while (base + i <= p) {
+            base += i;
+            i++;
+        }
+        const int l = p - base;  // l < i
+        const double *vl = Ps + (size_t) l * ldp, *vi = Ps + (size_t) i * ldp;
+        double s = 0.0;
+        for (int r = i + lane; r < mr; r += 32) s = fma(vl[r], vi[r], s);
+        s = warp_sum(s);
+        if (lane == 0) Gs[l * NB + i] = s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int j = lane;
+        for (int i = 0; i < nbp; i++) {
+            double v = 0.0;
+            if (j < i) {
+                for (int l = j; l < i; l++) v = fma(Ts[j * NB + l], Gs[l * NB + i], v);
+                v *= -tau_s[i];
+            }
+            __syncwarp();
+            if (j < i) Ts[j * NB + i] = v;
+            if (j == i) Ts[i * NB + i] = tau_s[i];
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+}
+
+// X (mr x nt, ld ldx) <- (I - V op(T) V^T) X with V = Ps (explicit, NB columns, ldp), T = Ts.
+// trans_t: op(T) = T^T (applying Q^T, the QR trailing update); else op(T) = T (applying Q).
+__device__ void apply_block_reflector(const double *Ps, int ldp, const double *Ts, bool trans_t, double *X, int ldx,
+                                      int mr, int nt, double *Ws, int ldw) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int lr = lane >> 2, lc = lane & 3;
+    if (nt <= 0 || mr <= 0) return;
+    const int nct = (nt + 7) >> 3;
+    // Step A: W = V^T X  (NB x nt), K = rows.
+    for (int ct = warp; ct < nct; ct += nw) {
+        double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+        const int col = ct * 8 + lr;
+        const bool colok = col < nt;
+        const double *xc = X + (size_t) (colok ? col : 0) * ldx;
+        int r4 = 0;
+        for (; r4 + 16 <= mr; r4 += 16) {
+            double bv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) bv[q] = colok ? xc[r4 + 4 * q + lc] : 0.0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int r = r4 + 4 * q + lc;
+                dmma(a0, a1, Ps[(size_t) lr * ldp + r], bv[q]);
+                dmma(b0, b1, Ps[(size_t) (8 + lr) * ldp + r], bv[q]);
+            }
+        }
+        for (; r4 < mr; r4 += 4) {
+            const int r = r4 + lc;
+            const double bv = (colok && r < mr) ? xc[r] : 0.0;
+            dmma(a0, a1, Ps[(size_t) lr * ldp + r], bv);
+            dmma(b0, b1, Ps[(size_t) (8 + lr) * ldp + r], bv);
+        }
+        const int c0 = ct * 8 + 2 * lc;
+        Ws[lr * ldw + c0] = a0;
+        Ws[lr * ldw + c0 + 1] = a1;
+        Ws[(8 + lr) * ldw + c0] = b0;
+        Ws[(8 + lr) * ldw + c0 + 1] = b1;
+    }
+    __syncthreads();
+    // Step B: W <- -op(T) W, one column per thread.
+    for (int c = threadIdx.x; c < nct * 8; c += blockDim.x) {
+        double w[NB], o[NB];
+#pragma unroll
+        for (int i = 0; i < NB; i++) w[i] = Ws[i * ldw + c];
+#pragma unroll
+        for (int i = 0; i < NB; i++) {
+            double s = 0.0;
+            if (trans_t) {
+#pragma unroll
+                for (int l = 0; l <= i; l++) s = fma(Ts[l * NB + i], w[l], s);
+            } else {
+#pragma unroll
+                for (int l = i; l < NB; l++) s = fma(Ts[i * NB + l], w[l], s);
+            }
+            o[i] = -s;
+        }
+#pragma unroll
+        for (int i = 0; i < NB; i++) Ws[i * ldw + c] = o[i];
+    }
+    __syncthreads();
+    // Step C: X += V W  (mr x nt), K = NB.
+    const int nrt = (mr + 7) >> 3;
+    for (int idx = warp; idx < nrt * nct; idx += nw) {
+        const int rt = idx % nrt, ct = idx / nrt;
+        const int row = rt * 8 + lr, c0 = ct * 8 + 2 * lc;
+        const bool rok = row < mr;
+        double d0 = (rok && c0 < nt) ? X[row + (size_t) c0 * ldx] : 0.0;
+        double d1 = (rok && c0 + 1 < nt) ? X[row + (size_t) (c0 + 1) * ldx] : 0.0;
+#pragma unroll
+        for (int ks = 0; ks < NB; ks += 4) {
+            const double av = Ps[(size_t) (ks + lc) * ldp + rt * 8 + lr];
+            const double bv = Ws[(ks + lc) * ldw + ct * 8 + lr];
+            dmma(d0, d1, av, bv);
+        }
+        if (rok && c0 < nt) X[row + (size_t) c0 * ldx] = d0;
+        if (rok && c0 + 1 < nt) X[row + (size_t) (c0 + 1) * ldx] = d1;
+    }
+    __syncthreads();
+}
+
+struct QrShared {
+    double *Ps, *Ws, *Ts, *Gs, *red, *tau;
+    int ldp, ldw;
+};
+
+__device__ QrShared carve(double *sm, int ld, int kmax) {
+    QrShared s;
+    s.ldp = round_up(ld, 8);
+    s.ldw = round_up(kmax, 8);
+    s.Ps = sm;
+    s.Ws = s.Ps + (size_t) NB * s.ldp;
+    s.Ts = s.Ws + (size_t) NB * s.ldw;
+    s.Gs = s.Ts + NB * NB;
+    s.red = s.Gs + NB * NB;
+    s.tau = s.red + 64;
+    return s;
+}
+
+// grid = 2 * n: block 2s factors the U stack of update s, block 2s+1 its V stack.
+__global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws) {
+    extern __shared__ double sm[];
+    const int slot = blockIdx.x >> 1, side = blockIdx.x & 1;
+    const int *meta = ws.meta + (size_t) slot * META_INTS;
+    if (meta[META_STATUS] != HCGB_OK || !meta[META_CKIND]) return;
+    const int k = meta[META_K];
+    const int m = side ? meta[META_N] : meta[META_M];
+    double *base = ws.slot(slot);
+    double *A = base + (side ? ws.off_vstack : ws.off_ustack);
+    double *tau = base + (side ? ws.off_tauv : ws.off_tauu);
+    double *Tg = base + (side ? ws.off_tv : ws.off_tu);
+    const int lda = ws.ld;
+    QrShared s = carve(sm, ws.ld, ws.kmax);
+    const int kk = m < k ? m : k;
+    for (int j0 = 0; j0 < kk; j0 += NB) {
+        const int nbp = (kk - j0) < NB ? (kk - j0) : NB;
+        const int mr = m - j0;
+        for (int e = threadIdx.x; e < NB * s.ldp; e += blockDim.x) {
+            const int c = e / s.ldp, r = e % s.ldp;
+            s.Ps[e] = (c < nbp && r < mr) ? A[(j0 + r) + (size_t) (j0 + c) * lda] : 0.0;
+        }
+        __syncthreads();
+        factor_panel(s.Ps, s.ldp, mr, nbp, s.tau, s.red);
+        for (int e = threadIdx.x; e < nbp * mr; e += blockDim.x) {
+            const int c = e / mr, r = e % mr;
+            A[(j0 + r) + (size_t) (j0 + c) * lda] = s.Ps[(size_t) c * s.ldp + r];
+        }
+        if (threadIdx.x < nbp) tau[j0 + threadIdx.x] = s.tau[threadIdx.x];
+        __syncthreads();
+        make_explicit_v(s.Ps, s.ldp, nbp);
+        __syncthreads();
+        build_t(s.Ps, s.ldp, mr, nbp, s.tau, s.Ts, s.Gs);
+        for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) Tg[(size_t) (j0 / NB) * NB * NB + e] = s.Ts[e];
+        const int c0 = j0 + nbp;
+        apply_block_reflector(s.Ps, s.ldp, s.Ts, true, A + j0 + (size_t) c0 * lda, lda, mr, k - c0, s.Ws, s.ldw);
+    }
+}
+
+// grid = 2 * n: X <- Q X for the U side (X = the C tile's U, m x r) and the V side (X = XV, n x r).
+__global__ void __launch_bounds__(QR_THREADS) apply_q_kernel(const DevUpdate *ups, Workspace ws) {
+    extern __shared__ double sm[];
+    const int slot = blockIdx.x >> 1, side = blockIdx.x & 1;
+    const int *meta = ws.meta + (size_t) slot * META_INTS;
+    const int st = meta[META_STATUS];
+    if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;
+    const int k = meta[META_K];
+    const int m = side ? meta[META_N] : meta[META_M];
+    const int r = meta[META_NEWRANK];
+    double *base = ws.slot(slot);
+    const double *A = base + (side ? ws.off_vstack : ws.off_ustack);
+    const double *Tg = base + (side ? ws.off_tv : ws.off_tu);
+    double *X;
+    int ldx;
+    if (side == 0) {
+        X = ups[slot].c.data;
+        ldx = ups[slot].c.rows;
+    } else {
+        X = base + ws.off_xv;
+        ldx = ws.ld;
+    }
+    const int lda = ws.ld;
+    QrShared s = carve(sm, ws.ld, ws.kmax);
+    const int kk = m < k ? m : k;
+    const int npan = (kk + NB - 1) / NB;
+    for (int p = npan - 1; p >= 0; p--) {
+        const int j0 = p * NB;
+        const int nbp = (kk - j0) < NB ? (kk - j0) : NB;
+        const int mr = m - j0;
+        for (int e = threadIdx.x; e < NB * s.ldp; e += blockDim.x) {
+            const int c = e / s.ldp, rr = e % s.ldp;
+            double v = 0.0;
+            if (c < nbp && rr < mr) v = rr > c ? A[(j0 + rr) + (size_t) (j0 + c) * lda] : (rr == c ? 1.0 : 0.0);
+            s.Ps[e] = v;
+        }
+        for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) s.Ts[e] = Tg[(size_t) p * NB * NB + e];
+        __syncthreads();
+        apply_block_reflector(s.Ps, s.ldp, s.Ts, false, X + j0, ldx, mr, r, s.Ws, s.ldw);
+    }
+}
+
+}  // namespace
+
+size_t qr_smem_bytes(int ld, int kmax) {
+    const int ldp = round_up(ld, 8), ldw = round_up(kmax, 8);
+    return sizeof(double) * ((size_t) NB * ldp + (size_t) NB * ldw + 2 * NB * NB + 64 + NB);
+}
+
+void launch_qr(Workspace ws, int n, cudaStream_t st) {
+    const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
+    cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws);
+}
+
+void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st) {
+    const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
+    cudaFuncSetAttribute(apply_q_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    apply_q_kernel<<<2 * n, QR_THREADS, smem, st>>>(ups, ws);
+}
+
+}  // namespace hcgb

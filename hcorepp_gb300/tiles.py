@@ -1,0 +1,253 @@
+"""Host-side mirror of HCore++'s operator API for the TLR GEMM, over the C ABI.
+
+Names, argument meaning and error behaviour follow the reference:
+  CompressionParameters   include/hcorepp/operators/helpers/CompressionParameters.hpp:44-127
+  DenseTile               include/hcorepp/operators/concrete/Dense.hpp:56-91
+  CompressedTile          include/hcorepp/operators/concrete/Compressed.hpp:67-151, :169-246
+  HCore.gemm              include/hcorepp/api/HCore.hpp:41-63 (src/api/HCore.cpp:23-344)
+  TileMatrix              src/helpers/TileMatrix.cpp:17-185 (device-resident tile grid)
+Device memory comes from torch (plumbing only); every computation is a libhcgb kernel.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+MAX_RANK_RATIO = 3  # Compressed.hpp:14
+GESVD, GESDD = 0, 1
+
+
+@dataclass(frozen=True)
+class CompressionParameters:
+    """CompressionParameters(aAccuracy=1e-4, aUseTrmm=false, aUseUngqr=true, aTruncatedSvd=false,
+    aFixedRank=0, aOpType=GESDD)."""
+    accuracy: float = 1e-4
+    use_trmm: bool = False
+    use_ungqr: bool = True
+    truncated_svd: bool = False
+    fixed_rank: int = 0
+    op_type: int = GESDD
+
+    def c(self) -> L.Params:
+        return L.make_params(self.accuracy, self.truncated_svd, self.fixed_rank, self.use_trmm, self.use_ungqr,
+                             self.op_type)
+
+
+_CONTEXTS = {}
+
+
+def run_context(device=None) -> L.Context:
+    """The per-device context (ContextManager::GetContext's role), bound to torch's current stream."""
+    dev = torch.cuda.current_device() if device is None else device
+    ctx = _CONTEXTS.get(dev)
+    if ctx is None:
+        ctx = _CONTEXTS[dev] = L.Context(dev)
+    ctx.set_stream(torch.cuda.current_stream(dev).cuda_stream)
+    return ctx
+
+
+def _fortran_flat(a) -> torch.Tensor:
+    a = np.asarray(a, dtype=np.float64)
+    return torch.from_numpy(np.ascontiguousarray(a.ravel(order="F")))
+
+
+class DenseTile:
+    """A dense rows x cols tile, column-major in device memory."""
+    kind = L.DENSE
+
+    def __init__(self, rows: int, cols: int, data=None, buffer: torch.Tensor | None = None, device="cuda"):
+        self.rows, self.cols = rows, cols
+        if buffer is not None:
+            self.buffer = buffer
+        else:
+            self.buffer = torch.zeros(rows * cols, dtype=torch.float64, device=device)
+            if data is not None:
+                self.buffer.copy_(_fortran_flat(data))
+
+    def c_tile(self) -> L.Tile:
+        return L.Tile(self.buffer.data_ptr(), None, self.rows, self.cols, 0, L.DENSE)
+
+    def to_dense(self) -> np.ndarray:
+        return self.buffer.cpu().numpy().reshape((self.rows, self.cols), order="F")
+
+    GetNumOfRows = lambda self: self.rows
+    GetNumOfCols = lambda self: self.cols
+
+
+class CompressedTile:
+    """U (rows x rank) . V (rank x cols) in one buffer [U: rows x max_rank | V: max_rank x cols, ld rank].
+
+    CompressedTile(rows, cols, u, v, rank) mirrors the (pointer, rank) constructor
+    (Compressed.cpp:50-73): the capacity max_rank defaults to the rank, so the rank can
+    never grow.  Pass max_rank to reserve room (the dense constructor uses min(m, n)/3).
+    """
+    kind = L.COMPRESSED
+
+    def __init__(self, rows: int, cols: int, u=None, v=None, rank: int | None = None, max_rank: int | None = None,
+                 buffer: torch.Tensor | None = None, rank_buf: torch.Tensor | None = None, device="cuda"):
+        self.rows, self.cols = rows, cols
+        if rank is None:
+            rank = np.asarray(u).shape[1]
+        self.max_rank = max_rank if max_rank is not None else rank
+        if rank > self.max_rank:
+            raise ValueError("rank exceeds the tile capacity")
+        cap = rows * self.max_rank + self.max_rank * cols
+        self.buffer = buffer if buffer is not None else torch.zeros(cap, dtype=torch.float64, device=device)
+        self.rank_buf = rank_buf if rank_buf is not None else torch.zeros(1, dtype=torch.int32, device=device)
+        if u is not None:
+            self.set_factors(u, v)
+
+    def set_factors(self, u, v):
+        u = np.asarray(u, dtype=np.float64)
+        v = np.asarray(v, dtype=np.float64)
+        r = u.shape[1]
+        if r > self.max_rank:
+            raise ValueError("rank exceeds the tile capacity")
+        self.buffer[:self.rows * r].copy_(_fortran_flat(u))
+        o = self.rows * self.max_rank
+        self.buffer[o:o + r * self.cols].copy_(_fortran_flat(v))
+        self.rank_buf.fill_(r)
+
+    def c_tile(self) -> L.Tile:
+        return L.Tile(self.buffer.data_ptr(), self.rank_buf.data_ptr(), self.rows, self.cols, self.max_rank,
+                      L.COMPRESSED)
+
+    def GetTileRank(self) -> int:
+        return int(self.rank_buf.item())
+
+    rank = property(GetTileRank)
+
+    def u(self) -> np.ndarray:
+        r = self.rank
+        return self.buffer[:self.rows * r].cpu().numpy().reshape((self.rows, r), order="F")
+
+    def v(self) -> np.ndarray:
+        r = self.rank
+        o = self.rows * self.max_rank
+        return self.buffer[o:o + r * self.cols].cpu().numpy().reshape((r, self.cols), order="F")
+
+    def to_dense(self) -> np.ndarray:
+        return self.u() @ self.v()
+
+    GetNumOfRows = lambda self: self.rows
+    GetNumOfCols = lambda self: self.cols
+
+
+class HCore:
+    """HCore<double> (include/hcorepp/api/HCore.hpp:41-63)."""
+
+    @staticmethod
+    def Gemm(alpha, a, a_op, b, b_op, beta, c, params: CompressionParameters = CompressionParameters(1e-9)):
+        """C = alpha op(A) op(B) + beta C; returns the reference's flop count for the update."""
+        ctx = run_context()
+        ta, tb, tc = a.c_tile(), b.c_tile(), c.c_tile()
+        p = params.c()
+        nr = C.c_int(0)
+        fl = C.c_ulonglong(0)
+        rc = L.lib().hcgb_tile_gemm(ctx.handle, float(alpha), C.byref(ta), int(a_op), C.byref(tb), int(b_op),
+                                    float(beta), C.byref(tc), C.byref(p), C.byref(nr), C.byref(fl))
+        ctx.check(rc, allow=(L.HCGB_OK, L.HCGB_NOT_CONVERGED))
+        if c.kind == L.COMPRESSED and ta.kind == L.DENSE and tb.kind == L.DENSE:
+            c.max_rank = min(c.rows, c.cols)  # DDC re-sets the tile at full rank (HCore.cpp:294-298)
+        return fl.value
+
+    gemm = Gemm
+
+
+class TileMatrix:
+    """A grid of mt x nt tiles of nb x nb, resident in one device arena.
+
+    ``kinds[i][j]`` is DENSE or COMPRESSED; compressed tiles get capacity ``max_rank``.
+    Ranks live in one device int array (``ranks``), so a whole multiply runs without the host.
+    """
+
+    def __init__(self, mt: int, nt: int, nb: int, kinds, max_rank: int, device="cuda"):
+        self.mt, self.nt, self.nb, self.max_rank = mt, nt, nb, max_rank
+        self.kinds = [[kinds[i][j] for j in range(nt)] for i in range(mt)]
+        sizes = []
+        for j in range(nt):
+            for i in range(mt):
+                sizes.append(nb * nb if self.kinds[i][j] == L.DENSE else 2 * nb * max_rank)
+        self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        self.arena = torch.zeros(int(self.offsets[-1]), dtype=torch.float64, device=device)
+        self.ranks = torch.zeros(mt * nt, dtype=torch.int32, device=device)
+
+    def index(self, i, j):
+        return i + j * self.mt
+
+    def _view(self, i, j):
+        idx = self.index(i, j)
+        return self.arena[int(self.offsets[idx]):int(self.offsets[idx + 1])]
+
+    def tile(self, i, j):
+        nb = self.nb
+        idx = self.index(i, j)
+        if self.kinds[i][j] == L.DENSE:
+            return DenseTile(nb, nb, buffer=self._view(i, j))
+        return CompressedTile(nb, nb, rank=0, max_rank=self.max_rank, buffer=self._view(i, j),
+                              rank_buf=self.ranks[idx:idx + 1])
+
+    def c_grid(self):
+        nb = self.nb
+        arr = (L.Tile * (self.mt * self.nt))()
+        base = self.arena.data_ptr()
+        rbase = self.ranks.data_ptr()
+        for j in range(self.nt):
+            for i in range(self.mt):
+                idx = self.index(i, j)
+                ptr = base + 8 * int(self.offsets[idx])
+                if self.kinds[i][j] == L.DENSE:
+                    arr[idx] = L.Tile(ptr, None, nb, nb, 0, L.DENSE)
+                else:
+                    arr[idx] = L.Tile(ptr, rbase + 4 * idx, nb, nb, self.max_rank, L.COMPRESSED)
+        return arr
+
+    def set_tile(self, i, j, dense=None, u=None, v=None):
+        t = self.tile(i, j)
+        if self.kinds[i][j] == L.DENSE:
+            t.buffer.copy_(_fortran_flat(dense))
+        else:
+            t.set_factors(u, v)
+
+    def to_dense(self) -> np.ndarray:
+        nb = self.nb
+        out = np.zeros((self.mt * nb, self.nt * nb))
+        arena = self.arena.cpu().numpy()
+        ranks = self.ranks.cpu().numpy()
+        for j in range(self.nt):
+            for i in range(self.mt):
+                idx = self.index(i, j)
+                seg = arena[self.offsets[idx]:self.offsets[idx + 1]]
+                if self.kinds[i][j] == L.DENSE:
+                    blk = seg.reshape((nb, nb), order="F")
+                else:
+                    r = int(ranks[idx])
+                    u = seg[:nb * r].reshape((nb, r), order="F")
+                    v = seg[nb * self.max_rank:nb * self.max_rank + r * nb].reshape((r, nb), order="F")
+                    blk = u @ v
+                out[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb] = blk
+        return out
+
+    def rank_grid(self) -> np.ndarray:
+        return self.ranks.cpu().numpy().reshape((self.nt, self.mt)).T.copy()
+
+
+def tlr_gemm(alpha: float, a: TileMatrix, b: TileMatrix, beta: float, c: TileMatrix,
+             params: CompressionParameters, status: torch.Tensor | None = None, ctx: L.Context | None = None):
+    """C = alpha A B + beta C over tile grids (examples/matrix_multiplication/omp_main.cpp:112-124).
+
+    Asynchronous on torch's current stream.  ``status`` (optional, int32 device tensor of
+    mt*nt*kt entries) receives the per-update status."""
+    ctx = ctx or run_context()
+    if a.nt != b.mt or a.mt != c.mt or b.nt != c.nt:
+        raise ValueError("tile grids do not conform")
+    ga, gb, gc = a.c_grid(), b.c_grid(), c.c_grid()
+    p = params.c()
+    sp = C.c_void_p(status.data_ptr()) if status is not None else None
+    rc = L.lib().hcgb_tlr_gemm(ctx.handle, c.mt, c.nt, a.nt, float(alpha), ga, gb, float(beta), gc, C.byref(p), sp)
+    ctx.check(rc)

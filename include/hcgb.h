@@ -1,0 +1,120 @@
+/*
+ * hcgb.h -- C ABI of the GB300-native TLR GEMM (HCore++'s tile GEMM with recompression).
+ *
+ * The entry points replace, for the TLR GEMM path, what HCore++'s CUDA backend does behind
+ * its C++ API.  Every pointer inside a tile is DEVICE memory; descriptor arrays passed to
+ * the entry points are HOST memory.  No exception crosses this boundary: every entry
+ * point returns an hcgb_status.
+ *
+ * Tile buffers use HCore++'s own DataHolder layout so that a reference tile buffer can be
+ * handed over unchanged:
+ *   dense      : rows x cols, column-major, leading dimension = rows
+ *                (DenseTile, include/hcorepp/operators/concrete/Dense.hpp:90-91)
+ *   compressed : [U: rows x max_rank (ld rows) | V: max_rank x cols (ld = rank)]
+ *                (CompressedTile, src/operators/concrete/Compressed.cpp:50-73, :176-185)
+ * A compressed tile's rank lives in a device int so that batched calls never need the host.
+ */
+#ifndef HCGB_H
+#define HCGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    HCGB_OK = 0,
+    HCGB_CUDA_ERROR = 1,      /* a CUDA runtime call failed (reference: GPU_ERROR_CHECK -> exit,
+                                 include/hcorepp/kernels/cuda/error_checking.h:38-45) */
+    HCGB_BAD_ARG = 2,         /* invalid argument (reference: std::invalid_argument / runtime_error) */
+    HCGB_POOL_TOO_SMALL = 3,  /* scratch does not fit (reference: pool/MemoryHandler.hpp:52-54) */
+    HCGB_RANK_OVERFLOW = 4,   /* a rank exceeds the tile's capacity */
+    HCGB_NOT_CONVERGED = 5,   /* the Jacobi SVD hit its sweep limit */
+    HCGB_UNSUPPORTED = 6      /* combination not available on this entry point */
+} hcgb_status;
+
+typedef enum { HCGB_DENSE = 0, HCGB_COMPRESSED = 1 } hcgb_tile_kind;
+typedef enum { HCGB_NOTRANS = 0, HCGB_TRANS = 1 } hcgb_op;
+typedef enum { HCGB_GESVD = 0, HCGB_GESDD = 1 } hcgb_svd_type;
+
+/* One tile in device memory. */
+typedef struct {
+    double *data;   /* device buffer, layout above */
+    int *rank;      /* compressed: device int with the current rank; dense: NULL */
+    int rows;
+    int cols;
+    int max_rank;   /* compressed: capacity of the buffer in columns of U / rows of V */
+    int kind;       /* hcgb_tile_kind */
+} hcgb_tile;
+
+/* Recompression settings.  Mirrors operators::CompressionParameters
+ * (include/hcorepp/operators/helpers/CompressionParameters.hpp:44-46, :116-127).
+ * use_trmm / use_ungqr / op_type are accepted for interface parity; the GPU path always
+ * forms the same truncated product (QR of both stacks, SVD of the small core, Q applied). */
+typedef struct {
+    double accuracy;
+    int truncated_svd;  /* 1: relative threshold sigma_i < accuracy * sigma_0; 0: absolute */
+    int fixed_rank;     /* > 0: fixed-rank truncation */
+    int use_trmm;
+    int use_ungqr;
+    int op_type;        /* hcgb_svd_type */
+} hcgb_params;
+
+/* One tile update C <- alpha * A * B + beta * C (NoTrans operands). */
+typedef struct {
+    hcgb_tile a;
+    hcgb_tile b;
+    hcgb_tile c;
+} hcgb_update;
+
+typedef struct hcgb_context hcgb_context;
+
+/* Context = one device + one stream + a grow-only device workspace.
+ * Replaces kernels::RunContext for CUDA (include/hcorepp/kernels/cuda/RunContext.hpp:15-53:
+ * GetStream / Sync / RequestWorkBuffer).  stream may be NULL for the legacy default stream. */
+int hcgb_context_create(int device, void *stream, hcgb_context **out);
+int hcgb_context_destroy(hcgb_context *ctx);
+int hcgb_context_set_stream(hcgb_context *ctx, void *stream);
+/* kernels::RunContext::Sync (src/kernels/cuda/RunContext.cpp:52-54) */
+int hcgb_sync(hcgb_context *ctx);
+/* Text of the last error recorded on this context ("" if none). */
+const char *hcgb_last_error(hcgb_context *ctx);
+
+/* Device scratch (bytes) one batched call of n updates needs.  Replaces
+ * HCore<T>::CalculateMemoryPoolSize / CalculateGemmPoolSize (src/api/HCore.cpp:346-480)
+ * and HCoreKernels::CalculateGemmWorkspaceSize (src/kernels/cuda/kernels.cpp:138-265). */
+size_t hcgb_workspace_bytes(int n, int max_rows, int max_cols, int max_rank_c, int max_rank_ab);
+
+/* Batched tile updates: every entry updates a DIFFERENT C tile (the updates are independent).
+ * Replaces n calls of HCore<T>::Gemm (src/api/HCore.cpp:23-344) with NoTrans operands.
+ * Ranks are read and written on the device; nothing is synchronised with the host.
+ * status_dev (optional, device, n ints) receives a per-update hcgb_status.
+ * Supported combinations: CCC, DCC, CDC, CCD, DCD, CDD, DDD (DDC: hcgb_tile_gemm). */
+int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const hcgb_update *updates,
+                    const hcgb_params *params, int *status_dev);
+
+/* Tile-matrix multiply C <- alpha * A * B + beta * C over tile grids (all tiles rows x cols equal
+ * to nb), following examples/matrix_multiplication/omp_main.cpp:112-124: for every C tile the
+ * k-updates run in ascending k, C tiles are independent.  Grids are column-major host arrays of
+ * tile descriptors: A is mt x kt, B is kt x nt, C is mt x nt.  beta is applied on every k step,
+ * as in the reference driver.  Asynchronous on the context stream. */
+int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const hcgb_tile *a_grid,
+                  const hcgb_tile *b_grid, double beta, const hcgb_tile *c_grid, const hcgb_params *params,
+                  int *status_dev);
+
+/* Single tile update, the drop-in for HCore<T>::Gemm (src/api/HCore.cpp:23-344).  op_a/op_b
+ * accept HCGB_NOTRANS and HCGB_TRANS.  Synchronous: on return *c's rank on the device has been
+ * updated; *new_rank (if not NULL) receives it on the host, like CompressedTile::Gemm updating
+ * mRank (src/operators/concrete/Compressed.cpp:656-662).  The DDC combination rewrites C at full
+ * rank with an identity V (HCore.cpp:272-299) and needs max_rank >= min(rows, cols).
+ * flops (if not NULL) is incremented by the reference's count for the update. */
+int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *a, int op_a, const hcgb_tile *b, int op_b,
+                   double beta, hcgb_tile *c, const hcgb_params *params, int *new_rank,
+                   unsigned long long *flops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HCGB_H */
