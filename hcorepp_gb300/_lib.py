@@ -41,6 +41,14 @@ class Params(C.Structure):
                 ("use_trmm", C.c_int), ("use_ungqr", C.c_int), ("op_type", C.c_int)]
 
 
+class UpdateInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("rank_a", C.c_int), ("rank_b", C.c_int), ("rank_c", C.c_int),
+                ("k", C.c_int), ("new_rank", C.c_int), ("sweeps", C.c_int), ("side", C.c_int)]
+
+
+INFO_FIELDS = [f[0] for f in UpdateInfo._fields_]
+STAGES = ["plan", "stack", "gemm", "qr", "core_svd", "apply_q", "finalize"]
+
 _LIB = None
 
 
@@ -71,8 +79,13 @@ def lib():
         L.hcgb_tile_gemm.argtypes = [vp, C.c_double, C.POINTER(Tile), ip, C.POINTER(Tile), ip, C.c_double,
                                      C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int),
                                      C.POINTER(C.c_ulonglong)]
+        L.hcgb_profile_enable.argtypes = [vp, ip]
+        L.hcgb_profile_reset.argtypes = [vp]
+        L.hcgb_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong), ip]
+        L.hcgb_fp64_peak.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         for name in ("hcgb_context_create", "hcgb_context_destroy", "hcgb_context_set_stream", "hcgb_sync",
-                     "hcgb_gemm_batch", "hcgb_tlr_gemm", "hcgb_tile_gemm"):
+                     "hcgb_gemm_batch", "hcgb_tlr_gemm", "hcgb_tile_gemm", "hcgb_profile_enable",
+                     "hcgb_profile_reset", "hcgb_profile_read", "hcgb_fp64_peak"):
             getattr(L, name).restype = C.c_int
         _LIB = L
     return _LIB
@@ -102,6 +115,24 @@ class Context:
 
     def sync(self):
         self.check(lib().hcgb_sync(self._h))
+
+    def profile(self, enable: bool):
+        self.check(lib().hcgb_profile_enable(self._h, int(enable)))
+
+    def profile_reset(self):
+        self.check(lib().hcgb_profile_reset(self._h))
+
+    def profile_read(self):
+        n = len(STAGES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_longlong * n)()
+        self.check(lib().hcgb_profile_read(self._h, ms, cnt, n))
+        return {STAGES[i]: (ms[i], cnt[i]) for i in range(n)}
+
+    def fp64_peak(self):
+        d, f = C.c_double(), C.c_double()
+        self.check(lib().hcgb_fp64_peak(self._h, C.byref(d), C.byref(f)))
+        return d.value, f.value
 
     def close(self):
         if self._h:

@@ -22,6 +22,12 @@ struct hcgb_context {
     size_t stage_bytes = 0;
     cudaEvent_t stage_done = nullptr;
     std::string last_error;
+    // stage profiling
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_free;
+    std::vector<std::vector<cudaEvent_t>> ev_pending;  // one group of HCGB_NUM_STAGES + 1 per pipeline
+    double stage_ms[HCGB_NUM_STAGES] = {0};
+    long long stage_launches[HCGB_NUM_STAGES] = {0};
 };
 
 namespace {
@@ -149,18 +155,65 @@ Params to_params(const hcgb_params *p) {
     return q;
 }
 
+std::vector<cudaEvent_t> take_events(hcgb_context *ctx, int count) {
+    std::vector<cudaEvent_t> ev;
+    for (int i = 0; i < count; i++) {
+        cudaEvent_t e;
+        if (!ctx->ev_free.empty()) {
+            e = ctx->ev_free.back();
+            ctx->ev_free.pop_back();
+        } else {
+            cudaEventCreate(&e);
+        }
+        ev.push_back(e);
+    }
+    return ev;
+}
+
 // Launch the full pipeline for n updates whose descriptors are already on the device.
-void launch_pipeline(const DevUpdate *dups, GemmJob *djobs, int n, double alpha, double beta, const Workspace &ws,
-                     const BatchShape &sh, const Params &p, int *status_dev, cudaStream_t st) {
+void launch_pipeline(hcgb_context *ctx, const DevUpdate *dups, GemmJob *djobs, int n, double alpha, double beta,
+                     const Workspace &ws, const BatchShape &sh, const Params &p, hcgb_update_info *info) {
+    cudaStream_t st = ctx->stream;
+    std::vector<cudaEvent_t> ev;
+    if (ctx->prof) ev = take_events(ctx, HCGB_NUM_STAGES + 1);
+    auto mark = [&](int i) {
+        if (ctx->prof) cudaEventRecord(ev[i], st);
+    };
+    long long *cnt = ctx->stage_launches;
+    mark(HCGB_STAGE_PLAN);
     launch_plan(dups, n, alpha, beta, ws, p, djobs, st);
-    if (sh.any_compressed_c) launch_stack(dups, n, alpha, beta, ws, st);
-    for (int ph = 0; ph < 3; ph++) launch_gemm_jobs(djobs + (size_t) ph * n, n, sh.p_m[ph], sh.p_n[ph], st);
+    cnt[HCGB_STAGE_PLAN]++;
+    mark(HCGB_STAGE_STACK);
+    if (sh.any_compressed_c) {
+        launch_stack(dups, n, alpha, beta, ws, st);
+        cnt[HCGB_STAGE_STACK]++;
+    }
+    mark(HCGB_STAGE_GEMM);
+    for (int ph = 0; ph < 3; ph++)
+        if (sh.p_m[ph] > 0 && sh.p_n[ph] > 0) {
+            launch_gemm_jobs(djobs + (size_t) ph * n, n, sh.p_m[ph], sh.p_n[ph], st);
+            cnt[HCGB_STAGE_GEMM]++;
+        }
+    mark(HCGB_STAGE_QR);
     if (sh.any_compressed_c) {
         launch_qr(ws, n, st);
-        launch_core_svd(dups, n, ws, p, st);
-        launch_apply_q(dups, n, ws, st);
+        cnt[HCGB_STAGE_QR]++;
     }
-    launch_finalize(dups, n, ws, status_dev, st);
+    mark(HCGB_STAGE_CORE_SVD);
+    if (sh.any_compressed_c) {
+        launch_core_svd(dups, n, ws, p, st);
+        cnt[HCGB_STAGE_CORE_SVD]++;
+    }
+    mark(HCGB_STAGE_APPLY_Q);
+    if (sh.any_compressed_c) {
+        launch_apply_q(dups, n, ws, st);
+        cnt[HCGB_STAGE_APPLY_Q]++;
+    }
+    mark(HCGB_STAGE_FINALIZE);
+    launch_finalize(dups, n, ws, info, st);
+    cnt[HCGB_STAGE_FINALIZE]++;
+    mark(HCGB_NUM_STAGES);
+    if (ctx->prof) ctx->ev_pending.push_back(ev);
 }
 
 int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, Workspace *out) {
@@ -220,6 +273,9 @@ int hcgb_context_destroy(hcgb_context *ctx) {
     if (ctx->desc) cudaFree(ctx->desc);
     if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
+    for (auto &g : ctx->ev_pending)
+        for (auto e : g) cudaEventDestroy(e);
+    for (auto e : ctx->ev_free) cudaEventDestroy(e);
     delete ctx;
     return HCGB_OK;
 }
@@ -247,7 +303,7 @@ size_t hcgb_workspace_bytes(int n, int max_rows, int max_cols, int max_rank_c, i
 }
 
 int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const hcgb_update *updates,
-                    const hcgb_params *params, int *status_dev) {
+                    const hcgb_params *params, hcgb_update_info *info_dev) {
     if (!ctx) return HCGB_BAD_ARG;
     if (n == 0) return HCGB_OK;
     if (n < 0 || !updates) return fail(ctx, HCGB_BAD_ARG, "hcgb_gemm_batch: bad update list");
@@ -270,14 +326,14 @@ int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const h
     DevUpdate *dups;
     GemmJob *djobs;
     if ((rc = upload_updates(ctx, dv, &dups, &djobs))) return rc;
-    launch_pipeline(dups, djobs, n, alpha, beta, ws, sh, to_params(params), status_dev, ctx->stream);
+    launch_pipeline(ctx, dups, djobs, n, alpha, beta, ws, sh, to_params(params), info_dev);
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
 }
 
 int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const hcgb_tile *a_grid,
                   const hcgb_tile *b_grid, double beta, const hcgb_tile *c_grid, const hcgb_params *params,
-                  int *status_dev) {
+                  hcgb_update_info *info_dev) {
     if (!ctx) return HCGB_BAD_ARG;
     if (mt <= 0 || nt <= 0 || kt <= 0 || !a_grid || !b_grid || !c_grid)
         return fail(ctx, HCGB_BAD_ARG, "hcgb_tlr_gemm: bad grid");
@@ -320,8 +376,8 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         shw.ld = sh.ld;
         shw.kmax = sh.kmax;
         shw.rmax = sh.rmax;
-        launch_pipeline(dups + (size_t) kk * n, djobs, n, alpha, beta, ws, shw, p,
-                        status_dev ? status_dev + (size_t) kk * n : nullptr, ctx->stream);
+        launch_pipeline(ctx, dups + (size_t) kk * n, djobs, n, alpha, beta, ws, shw, p,
+                        info_dev ? info_dev + (size_t) kk * n : nullptr);
     }
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
@@ -468,16 +524,16 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
         out_rank = r;
     } else {
         hcgb_update u{A, B, *c};
-        int *dstatus = nullptr;
-        HCGB_CUDA(ctx, cudaMalloc(&dstatus, sizeof(int)));
-        rc = hcgb_gemm_batch(ctx, alpha, beta, 1, &u, params, dstatus);
+        hcgb_update_info *dinfo = nullptr;
+        HCGB_CUDA(ctx, cudaMalloc(&dinfo, sizeof(hcgb_update_info)));
+        rc = hcgb_gemm_batch(ctx, alpha, beta, 1, &u, params, dinfo);
         int hstatus = HCGB_OK;
         if (rc == HCGB_OK) {
-            HCGB_CUDA(ctx, cudaMemcpyAsync(&hstatus, dstatus, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            HCGB_CUDA(ctx, cudaMemcpyAsync(&hstatus, &dinfo->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
             if (ck) HCGB_CUDA(ctx, cudaMemcpyAsync(&out_rank, c->rank, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
             HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
-        cudaFree(dstatus);
+        cudaFree(dinfo);
         if (rc) {
             cleanup();
             return rc;
@@ -500,4 +556,51 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
     if (new_rank) *new_rank = ck ? out_rank : 0;
     if (flops) *flops += fl;
     return rc;
+}
+
+extern "C" int hcgb_profile_enable(hcgb_context *ctx, int enable) {
+    if (!ctx) return HCGB_BAD_ARG;
+    ctx->prof = enable != 0;
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_profile_reset(hcgb_context *ctx) {
+    if (!ctx) return HCGB_BAD_ARG;
+    HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (auto &g : ctx->ev_pending)
+        for (auto e : g) ctx->ev_free.push_back(e);
+    ctx->ev_pending.clear();
+    for (int i = 0; i < HCGB_NUM_STAGES; i++) {
+        ctx->stage_ms[i] = 0.0;
+        ctx->stage_launches[i] = 0;
+    }
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_profile_read(hcgb_context *ctx, double *ms_per_stage, long long *launches_per_stage,
+                                 int nstages) {
+    if (!ctx || nstages < 0) return HCGB_BAD_ARG;
+    HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (auto &g : ctx->ev_pending) {
+        for (int i = 0; i < HCGB_NUM_STAGES; i++) {
+            float ms = 0.f;
+            HCGB_CUDA(ctx, cudaEventElapsedTime(&ms, g[i], g[i + 1]));
+            ctx->stage_ms[i] += ms;
+        }
+        for (auto e : g) ctx->ev_free.push_back(e);
+    }
+    ctx->ev_pending.clear();
+    for (int i = 0; i < nstages && i < HCGB_NUM_STAGES; i++) {
+        if (ms_per_stage) ms_per_stage[i] = ctx->stage_ms[i];
+        if (launches_per_stage) launches_per_stage[i] = ctx->stage_launches[i];
+    }
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_fp64_peak(hcgb_context *ctx, double *dmma_tflops, double *dfma_tflops) {
+    if (!ctx) return HCGB_BAD_ARG;
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    int rc = measure_fp64_peak(ctx->stream, dmma_tflops, dfma_tflops);
+    if (rc) return fail(ctx, rc, "hcgb_fp64_peak: probe failed");
+    return HCGB_OK;
 }

@@ -112,7 +112,9 @@ void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cuda
 void launch_qr(Workspace ws, int n, cudaStream_t st);
 void launch_core_svd(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st);
 void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st);
-void launch_finalize(const DevUpdate *ups, int n, Workspace ws, int *status_dev, cudaStream_t st);
+void launch_finalize(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st);
+// FP64 throughput probes (TFLOP/s): tensor-core DMMA and SIMT DFMA.
+int measure_fp64_peak(cudaStream_t st, double *dmma_tflops, double *dfma_tflops);
 // DDC (dense A, dense B, compressed C): C <- full rank, U = alpha A B + beta Cu Cv, V = I.
 void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st);
 // dst (cols x rows, ld ldd) = src^T (src rows x cols, ld lds); one CTA.

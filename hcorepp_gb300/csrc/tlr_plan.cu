@@ -269,15 +269,26 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
             }
 }
 
-// One CTA per update: V (r x n, ld r) = XV^T into the tile buffer, publish rank and status.
-__global__ void __launch_bounds__(256) finalize_kernel(const DevUpdate *ups, Workspace ws, int *status_dev) {
+// One CTA per update: V (r x n, ld r) = XV^T into the tile buffer, publish rank and record.
+__global__ void __launch_bounds__(256) finalize_kernel(const DevUpdate *ups, Workspace ws, hcgb_update_info *info) {
     __shared__ double tile[32][33];
     const int s = blockIdx.x;
     const int *meta = ws.meta + (size_t) s * META_INTS;
     const int status = meta[META_STATUS];
-    if (status_dev && threadIdx.x == 0) status_dev[s] = status;
-    if (status != HCGB_OK && status != HCGB_NOT_CONVERGED) return;
-    if (!meta[META_CKIND]) return;
+    const bool ok = (status == HCGB_OK || status == HCGB_NOT_CONVERGED) && meta[META_CKIND];
+    if (info && threadIdx.x == 0) {
+        hcgb_update_info r;
+        r.status = status;
+        r.rank_a = meta[META_RA];
+        r.rank_b = meta[META_RB];
+        r.rank_c = meta[META_RC];
+        r.k = meta[META_CKIND] ? meta[META_K] : 0;
+        r.new_rank = ok ? meta[META_NEWRANK] : 0;
+        r.sweeps = meta[META_SWEEPS];
+        r.side = meta[META_SIDE];
+        info[s] = r;
+    }
+    if (!ok) return;
     const DevUpdate u = ups[s];
     const int r = meta[META_NEWRANK], nn = meta[META_N];
     const double *XV = ws.slot(s) + ws.off_xv;
@@ -330,8 +341,8 @@ void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cuda
     gemm_jobs_kernel<<<grid, 128, 0, st>>>(jobs);
 }
 
-void launch_finalize(const DevUpdate *ups, int n, Workspace ws, int *status_dev, cudaStream_t st) {
-    finalize_kernel<<<n, 256, 0, st>>>(ups, ws, status_dev);
+void launch_finalize(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st) {
+    finalize_kernel<<<n, 256, 0, st>>>(ups, ws, info);
 }
 
 void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st) {

@@ -17,6 +17,8 @@ path and the CPU oracle.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 MORTON_BITS = 21
@@ -86,3 +88,73 @@ WORKLOADS = {
     "tlr_gemm_n16384_nb512": dict(n=16384, nb=512, d=2, ell=0.1, seed_ab=1, seed_c=2,
                                   accuracy=1e-8, dense_diagonal=True),
 }
+
+
+# ---------------------------------------------------------------------------------------
+# Host-side input compression of the workload tiles (workload preparation, not the measured
+# multiply).  Same rule as CompressedTile(dense, params) (src/operators/concrete/Compressed.cpp:
+# 75-146): SVD, rank = first i >= 1 with sigma_i below the threshold (relative to sigma_0 when
+# truncated), clamped to [1, max(min(m, n) / 3, 1)], V = Sigma_r V_r^T.
+# ---------------------------------------------------------------------------------------
+
+def compress_dense(d: np.ndarray, accuracy: float, truncated: bool = True, max_rank: int | None = None):
+    m, n = d.shape
+    cap = max(min(m, n) // 3, 1) if max_rank is None else max_rank
+    u, s, vt = np.linalg.svd(d, full_matrices=False)
+    thr = accuracy * s[0] if truncated else accuracy
+    small = np.nonzero(s[1:] < thr)[0]
+    r = int(small[0]) + 1 if small.size else len(s)
+    r = min(max(r, 1), cap)
+    return np.asfortranarray(u[:, :r]), np.asfortranarray(s[:r, None] * vt[:r]), cap
+
+
+def _tile_job(args):
+    n, nb, d, ell, seed, diag_shift, i, j, accuracy, dense = args
+    km = _cached_matrix(n, nb, d, ell, seed, diag_shift)
+    blk = km.tile(i, j)
+    if dense:
+        return (i, j), ("D", blk)
+    u, v, cap = compress_dense(blk, accuracy, True)
+    return (i, j), ("C", u, v, cap)
+
+
+_KM_CACHE = {}
+
+
+def _cached_matrix(n, nb, d, ell, seed, diag_shift):
+    key = (n, nb, d, ell, seed, diag_shift)
+    if key not in _KM_CACHE:
+        _KM_CACHE[key] = KernelMatrix(n, nb, d, ell, seed, diag_shift)
+    return _KM_CACHE[key]
+
+
+def build_tiles(n, nb, d, ell, seed, accuracy, dense_diagonal, processes=None, diag_shift=0.0):
+    """All tiles of one matrix: dict (i, j) -> ("D", dense) | ("C", u, v, max_rank)."""
+    import multiprocessing as mp
+    nt = n // nb
+    jobs = [(n, nb, d, ell, seed, diag_shift, i, j, accuracy, dense_diagonal and i == j)
+            for j in range(nt) for i in range(nt)]
+    processes = processes or max(1, min(len(jobs), os.cpu_count() or 1))
+    if processes == 1:
+        return dict(_tile_job(j) for j in jobs)
+    with single_threaded_blas_env(), mp.get_context("spawn").Pool(processes) as pool:
+        return dict(pool.map(_tile_job, jobs, chunksize=max(1, len(jobs) // (4 * processes))))
+
+
+class single_threaded_blas_env:
+    """Spawned worker processes inherit one BLAS thread each (no oversubscription)."""
+    KEYS = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+
+    def __enter__(self):
+        self.saved = {k: os.environ.get(k) for k in self.KEYS}
+        for k in self.KEYS:
+            os.environ[k] = "1"
+        return self
+
+    def __exit__(self, *exc):
+        for k, v in self.saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        return False

@@ -237,17 +237,23 @@ class TileMatrix:
         return self.ranks.cpu().numpy().reshape((self.nt, self.mt)).T.copy()
 
 
+def info_buffer(n_updates: int, device="cuda") -> torch.Tensor:
+    """Device buffer for n hcgb_update_info records (int32, 8 fields each)."""
+    return torch.zeros((n_updates, len(L.INFO_FIELDS)), dtype=torch.int32, device=device)
+
+
 def tlr_gemm(alpha: float, a: TileMatrix, b: TileMatrix, beta: float, c: TileMatrix,
-             params: CompressionParameters, status: torch.Tensor | None = None, ctx: L.Context | None = None):
+             params: CompressionParameters, info: torch.Tensor | None = None, ctx: L.Context | None = None):
     """C = alpha A B + beta C over tile grids (examples/matrix_multiplication/omp_main.cpp:112-124).
 
-    Asynchronous on torch's current stream.  ``status`` (optional, int32 device tensor of
-    mt*nt*kt entries) receives the per-update status."""
+    Asynchronous on torch's current stream.  ``info`` (optional, from ``info_buffer(mt*nt*kt)``)
+    receives the per-update records (status, input ranks, k, new rank, sweeps, side); the
+    record of update (i, j, k) is row k*mt*nt + i + j*mt."""
     ctx = ctx or run_context()
     if a.nt != b.mt or a.mt != c.mt or b.nt != c.nt:
         raise ValueError("tile grids do not conform")
     ga, gb, gc = a.c_grid(), b.c_grid(), c.c_grid()
     p = params.c()
-    sp = C.c_void_p(status.data_ptr()) if status is not None else None
+    sp = C.c_void_p(info.data_ptr()) if info is not None else None
     rc = L.lib().hcgb_tlr_gemm(ctx.handle, c.mt, c.nt, a.nt, float(alpha), ga, gb, float(beta), gc, C.byref(p), sp)
     ctx.check(rc)

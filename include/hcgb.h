@@ -68,6 +68,24 @@ typedef struct {
     hcgb_tile c;
 } hcgb_update;
 
+/* Per-update record a batched call can return (device array, one entry per update). */
+typedef struct {
+    int status;     /* hcgb_status of the update */
+    int rank_a;     /* input ranks (0 for dense operands) */
+    int rank_b;
+    int rank_c;
+    int k;          /* columns of the stacked bases that were recompressed (0 for a dense C) */
+    int new_rank;   /* rank of C after the update (0 for a dense C) */
+    int sweeps;     /* Jacobi sweeps the core SVD took */
+    int side;       /* 0: stacked [Cu | alpha Au]; 1: stacked [Cu | alpha Au (Av Bu)] */
+} hcgb_update_info;
+
+/* Pipeline stages, for hcgb_profile_read. */
+typedef enum {
+    HCGB_STAGE_PLAN = 0, HCGB_STAGE_STACK, HCGB_STAGE_GEMM, HCGB_STAGE_QR, HCGB_STAGE_CORE_SVD,
+    HCGB_STAGE_APPLY_Q, HCGB_STAGE_FINALIZE, HCGB_NUM_STAGES
+} hcgb_stage;
+
 typedef struct hcgb_context hcgb_context;
 
 /* Context = one device + one stream + a grow-only device workspace.
@@ -89,19 +107,20 @@ size_t hcgb_workspace_bytes(int n, int max_rows, int max_cols, int max_rank_c, i
 /* Batched tile updates: every entry updates a DIFFERENT C tile (the updates are independent).
  * Replaces n calls of HCore<T>::Gemm (src/api/HCore.cpp:23-344) with NoTrans operands.
  * Ranks are read and written on the device; nothing is synchronised with the host.
- * status_dev (optional, device, n ints) receives a per-update hcgb_status.
+ * info_dev (optional, device, n records) receives a per-update hcgb_update_info.
  * Supported combinations: CCC, DCC, CDC, CCD, DCD, CDD, DDD (DDC: hcgb_tile_gemm). */
 int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const hcgb_update *updates,
-                    const hcgb_params *params, int *status_dev);
+                    const hcgb_params *params, hcgb_update_info *info_dev);
 
 /* Tile-matrix multiply C <- alpha * A * B + beta * C over tile grids (all tiles rows x cols equal
  * to nb), following examples/matrix_multiplication/omp_main.cpp:112-124: for every C tile the
  * k-updates run in ascending k, C tiles are independent.  Grids are column-major host arrays of
  * tile descriptors: A is mt x kt, B is kt x nt, C is mt x nt.  beta is applied on every k step,
- * as in the reference driver.  Asynchronous on the context stream. */
+ * as in the reference driver.  Asynchronous on the context stream.  info_dev (optional, device,
+ * mt*nt*kt records) receives the record of update (i, j, k) at index k*mt*nt + i + j*mt. */
 int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const hcgb_tile *a_grid,
                   const hcgb_tile *b_grid, double beta, const hcgb_tile *c_grid, const hcgb_params *params,
-                  int *status_dev);
+                  hcgb_update_info *info_dev);
 
 /* Single tile update, the drop-in for HCore<T>::Gemm (src/api/HCore.cpp:23-344).  op_a/op_b
  * accept HCGB_NOTRANS and HCGB_TRANS.  Synchronous: on return *c's rank on the device has been
@@ -112,6 +131,19 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
 int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *a, int op_a, const hcgb_tile *b, int op_b,
                    double beta, hcgb_tile *c, const hcgb_params *params, int *new_rank,
                    unsigned long long *flops);
+
+/* Stage timing with CUDA events on the context stream (the GB300 replacement of the reference's
+ * DebuggingTimer snapshots, src/helpers/debugging-timer/ActiveTimer.cpp:47-60).  While enabled,
+ * every pipeline stage is bracketed by events; hcgb_profile_read synchronises the stream and
+ * returns the accumulated milliseconds and kernel launches per stage since the last reset. */
+int hcgb_profile_enable(hcgb_context *ctx, int enable);
+int hcgb_profile_reset(hcgb_context *ctx);
+int hcgb_profile_read(hcgb_context *ctx, double *ms_per_stage, long long *launches_per_stage, int nstages);
+
+/* Measures this device's FP64 throughput with two probe kernels (~0.1 s): the FP64 tensor-core
+ * MMA (DMMA) rate and the FP64 FMA rate of the SIMT pipes, in TFLOP/s.  These are the roofline
+ * denominators of the FP64 path. */
+int hcgb_fp64_peak(hcgb_context *ctx, double *dmma_tflops, double *dfma_tflops);
 
 #ifdef __cplusplus
 }

@@ -149,13 +149,20 @@ def test_rank_clamp_at_capacity(T):
 
 
 def test_trans_operands(T):
+    # op(A) = A^T, op(B) = B^T (HCore.cpp:73-110 swaps the factor holders); C has room for the full rank.
     rng = np.random.default_rng(5)
     a, b, c = (random_lowrank(48, 48, 12, rng, 0.5) for _ in range(3))
-    oa, ob, oc = (compressed_from_dense(x, 1e-14, True) for x in (a, b, c))
+    oa, ob = (compressed_from_dense(x, 1e-14, True) for x in (a, b))
+    oc = compressed_from_dense(c, 1e-14, True, max_rank=40)
     ga, gb, gc = (_gpu_tile(T, t) for t in (oa, ob, oc))
     T.HCore.Gemm(1.0, ga, 1, gb, 1, 1.0, gc, T.CompressionParameters(1e-12, truncated_svd=True))
     exact = oa.to_dense().T @ ob.to_dense().T + oc.to_dense()
     assert rel_fro(gc.to_dense(), exact) < 1e-10
+    gd = T.DenseTile(48, 48, a)
+    gc2 = _gpu_tile(T, compressed_from_dense(c, 1e-14, True, max_rank=40))
+    T.HCore.Gemm(2.0, gd, 1, gb, 0, 1.0, gc2, T.CompressionParameters(1e-12, truncated_svd=True))
+    exact2 = 2.0 * a.T @ ob.to_dense() + oc.to_dense()
+    assert rel_fro(gc2.to_dense(), exact2) < 1e-10
 
 
 def test_tlr_multiply_vs_oracle(T):
@@ -187,10 +194,11 @@ def test_tlr_multiply_vs_oracle(T):
         mats[name], otiles[name] = tm, og
     a_dense, b_dense, c_dense = (mats[x].to_dense() for x in "ABC")
     exact = a_dense @ b_dense + c_dense
-    status = torch.zeros(nt * nt * nt, dtype=torch.int32, device="cuda")
-    T.tlr_gemm(1.0, mats["A"], mats["B"], 1.0, mats["C"], T.CompressionParameters(acc, truncated_svd=True), status)
+    info = T.info_buffer(nt * nt * nt)
+    T.tlr_gemm(1.0, mats["A"], mats["B"], 1.0, mats["C"], T.CompressionParameters(acc, truncated_svd=True), info)
     torch.cuda.synchronize()
-    assert int(status.max()) == 0, status.cpu().numpy()
+    info = info.cpu().numpy()
+    assert int(info[:, 0].max()) == 0, info
     O.tile_matrix_multiply(otiles["A"], otiles["B"], otiles["C"], 1.0, 1.0, params)
     o_dense = np.block([[otiles["C"][i][j].to_dense() for j in range(nt)] for i in range(nt)])
     g_dense = mats["C"].to_dense()
