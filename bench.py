@@ -195,14 +195,17 @@ def stage_algorithmic_flops(info, nb, kinds_of_update):
     ra, rb, rc = info[:, 1].astype(float), info[:, 2].astype(float), info[:, 3].astype(float)
     k, r, sw = info[:, 4].astype(float), info[:, 5].astype(float), info[:, 6].astype(float)
     side = info[:, 7]
+    rk = info[:, 8].astype(float)
     comp = k > 0
     m = float(nb)
     kk = np.minimum(k, m)
     out = {}
     # QR of both stacks (Householder, 2 m k^2 - 2 k^3 / 3 each)
     out["qr"] = float(np.sum(np.where(comp, 2 * (2 * m * k * k - 2 * kk ** 3 / 3), 0.0)))
-    # Core: triangular product (2 k^3 / 3) + Jacobi (per sweep k(k-1)/2 pairs x 12 kU flops) + Z = M^T U_r
-    out["core_svd"] = float(np.sum(np.where(comp, 2 * kk ** 3 / 3 + sw * kk * (kk - 1) / 2 * 12 * kk
+    # Core: triangular product (2 k^3 / 3), pivoted QR stopped at rk rows (sum_s 4 (k-s)^2),
+    # Jacobi on rk columns of length k (per sweep rk(rk-1)/2 pairs x 12 k flops), U_r = M V_r (2 k^2 r)
+    qrcp = 4.0 * (kk ** 3 - np.maximum(kk - rk, 0) ** 3) / 3.0
+    out["core_svd"] = float(np.sum(np.where(comp, 2 * kk ** 3 / 3 + qrcp + sw * rk * (rk - 1) / 2 * 12 * kk
                                             + 2 * kk * kk * r, 0.0)))
     # Q application on both sides: 4 m k r - 2 k^2 r each
     out["apply_q"] = float(np.sum(np.where(comp, 2 * (4 * m * k * r - 2 * kk * kk * r), 0.0)))
@@ -395,7 +398,9 @@ def gpu_arm(args, rank, world, local):
         "ranks": {"mean_final": float(rk[comp_mask].mean()), "max_final": int(rk[comp_mask].max()),
                   "updates_at_capacity": clamped, "bad_status": bad,
                   "mean_k": float(info_h[info_h[:, 4] > 0, 4].mean()),
-                  "max_sweeps": int(info_h[:, 6].max())},
+                  "max_sweeps": int(info_h[:, 6].max()),
+                  "mean_sweeps": float(info_h[info_h[:, 4] > 0, 6].mean()),
+                  "mean_core_cols": float(info_h[info_h[:, 4] > 0, 8].mean())},
         "check": check,
         "cpu_baseline": cpu,
         "clocks": clocks,

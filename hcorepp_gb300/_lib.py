@@ -43,7 +43,8 @@ class Params(C.Structure):
 
 class UpdateInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("rank_a", C.c_int), ("rank_b", C.c_int), ("rank_c", C.c_int),
-                ("k", C.c_int), ("new_rank", C.c_int), ("sweeps", C.c_int), ("side", C.c_int)]
+                ("k", C.c_int), ("new_rank", C.c_int), ("sweeps", C.c_int), ("side", C.c_int),
+                ("core_cols", C.c_int)]
 
 
 INFO_FIELDS = [f[0] for f in UpdateInfo._fields_]

@@ -76,6 +76,7 @@ enum MetaField {
     META_N,          // cols of C / rows of the V stack
     META_NEWRANK,
     META_SWEEPS,
+    META_CORE_COLS,  // rows of R kept by the rank-revealing QR of the core
     META_INTS = 16
 };
 

@@ -286,6 +286,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(const DevUpdate *ups, Wor
         r.new_rank = ok ? meta[META_NEWRANK] : 0;
         r.sweeps = meta[META_SWEEPS];
         r.side = meta[META_SIDE];
+        r.core_cols = meta[META_CORE_COLS];
         info[s] = r;
     }
     if (!ok) return;

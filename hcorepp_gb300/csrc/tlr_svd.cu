@@ -31,45 +31,258 @@ __device__ __forceinline__ void jacobi_pair(int t, int pp, int n2, int &i, int &
     }
 }
 
-// Rotate columns x, y (length rows <= 32*RPL) so that x^T y = 0; true if a rotation was applied.
-template <int RPL>
-__device__ bool rotate_pair(double *x, double *y, int rows, double tol) {
-    const int lane = threadIdx.x & 31;
-    double xr[RPL], yr[RPL];
-    double a = 0.0, b = 0.0, c = 0.0;
+__device__ __forceinline__ double group_sum(double v, int G) {
+    for (int o = G >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One sweep of one-sided Jacobi over the kV columns (length rows) of X (ld ldx), with G lanes
+// per column pair (32/G pairs per warp at a time) and RPL rows per lane held in registers.
+//
+// A pair (x, y) is rotated when |x^T y| > tol * |x| |y| and both columns are above the numerical
+// noise floor `tiny` (squared norm); columns below it carry only rounding errors of the larger
+// ones, sit far below any truncation threshold, and rotating them never settles.
+// The rotation: zeta = (|y|^2 - |x|^2) / (2 x^T y), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2))
+// (tangent of the smaller angle, Rutishauser's formula), cs = 1/sqrt(1 + t^2), sn = cs t.
+// t only needs to be accurate to single precision for the pair to come out orthogonal to
+// ~1e-7 of its coupling; cs and sn are then formed in double precision from that t, so the
+// rotation itself is orthogonal to working precision.
+template <int G, int RPL>
+__device__ int jacobi_sweep(double *X, int ldx, int rows, int kV, double tol2, double tiny, int n2) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    constexpr int PPW = 32 / G;  // pairs per warp
+    const int gl = lane % G, grp = lane / G;
+    const int npairs = n2 / 2;
+    const int nchunks = (npairs + PPW - 1) / PPW;
+    int rotations = 0;
+    for (int t = 0; t < n2 - 1; t++) {
+        for (int ch = warp; ch < nchunks; ch += nw) {
+            const int pp = ch * PPW + grp;
+            int i = 0, j = 0;
+            bool act = pp < npairs;
+            if (act) {
+                jacobi_pair(t, pp, n2, i, j);
+                act = i < kV && j < kV;
+            }
+            double *x = X + (size_t) (act ? i : 0) * ldx;
+            double *y = X + (size_t) (act ? j : 0) * ldx;
+            double xr[RPL], yr[RPL];
+            double a = 0.0, b = 0.0, c = 0.0;
 #pragma unroll
-    for (int q = 0; q < RPL; q++) {
-        const int r = lane + 32 * q;
-        xr[q] = r < rows ? x[r] : 0.0;
-        yr[q] = r < rows ? y[r] : 0.0;
-        a = fma(xr[q], xr[q], a);
-        b = fma(yr[q], yr[q], b);
-        c = fma(xr[q], yr[q], c);
-    }
-    a = warp_sum(a);
-    b = warp_sum(b);
-    c = warp_sum(c);
-    if (!(fabs(c) > tol * sqrt(a) * sqrt(b))) return false;
-    const double zeta = (b - a) / (2.0 * c);
-    const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(fma(zeta, zeta, 1.0)));
-    const double cs = 1.0 / sqrt(fma(t, t, 1.0));
-    const double sn = cs * t;
+            for (int q = 0; q < RPL; q++) {
+                const int r = gl + G * q;
+                const bool ok = act && r < rows;
+                xr[q] = ok ? x[r] : 0.0;
+                yr[q] = ok ? y[r] : 0.0;
+                a = fma(xr[q], xr[q], a);
+                b = fma(yr[q], yr[q], b);
+                c = fma(xr[q], yr[q], c);
+            }
+            a = group_sum(a, G);
+            b = group_sum(b, G);
+            c = group_sum(c, G);
+            const bool rot = act && a > tiny && b > tiny && c * c > tol2 * a * b;
+            if (rot) {
+                const double zeta = (b - a) / (2.0 * c);
+                const float zf = (float) zeta;
+                float tf;
+                if (fabsf(zf) > 1.0e18f) tf = 0.5f / zf;
+                else tf = copysignf(1.0f, zf) / (fabsf(zf) + sqrtf(fmaf(zf, zf, 1.0f)));
+                const double tt = (double) tf;
+                const double cs = rsqrt(fma(tt, tt, 1.0));
+                const double sn = cs * tt;
 #pragma unroll
-    for (int q = 0; q < RPL; q++) {
-        const int r = lane + 32 * q;
-        if (r < rows) {
-            x[r] = fma(cs, xr[q], -sn * yr[q]);
-            y[r] = fma(sn, xr[q], cs * yr[q]);
+                for (int q = 0; q < RPL; q++) {
+                    const int r = gl + G * q;
+                    if (r < rows) {
+                        x[r] = fma(cs, xr[q], -sn * yr[q]);
+                        y[r] = fma(sn, xr[q], cs * yr[q]);
+                    }
+                }
+                if (gl == 0) rotations++;
+            }
         }
+        __syncthreads();
     }
-    return true;
+    return rotations;
+}
+
+// Full Jacobi iteration on X: sweeps until no pair rotates (or MAX_JACOBI_SWEEPS).
+template <int G, int RPL>
+__device__ void jacobi(double *X, int ldx, int rows, int kV, int *s_rot, double *s_amax, int *sweeps_out,
+                       bool *converged_out) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const double tol = DBL_EPSILON * sqrt((double) (rows > 1 ? rows : 1));
+    const double tol2 = tol * tol;
+    const double noise = DBL_EPSILON * (double) (rows > 1 ? rows : 1);
+    const int n2 = kV + (kV & 1);
+    int sweeps = 0;
+    bool converged = kV < 2;
+    while (!converged && sweeps < MAX_JACOBI_SWEEPS) {
+        // Largest squared column norm: the scale of the numerical noise floor.
+        if (threadIdx.x == 0) {
+            *s_rot = 0;
+            *s_amax = 0.0;
+        }
+        __syncthreads();
+        double amax = 0.0;
+        for (int j = warp; j < kV; j += nw) {
+            const double *col = X + (size_t) j * ldx;
+            double s = 0.0;
+            for (int r = lane; r < rows; r += 32) s = fma(col[r], col[r], s);
+            s = warp_sum(s);
+            amax = fmax(amax, s);
+        }
+        if (lane == 0) atomicMax(reinterpret_cast<unsigned long long *>(s_amax), __double_as_longlong(amax));
+        __syncthreads();
+        const double tiny = *s_amax * noise * noise;
+        const int rot = jacobi_sweep<G, RPL>(X, ldx, rows, kV, tol2, tiny, n2);
+        if (rot) atomicAdd(s_rot, rot);
+        __syncthreads();
+        sweeps++;
+        converged = (*s_rot == 0);
+        __syncthreads();
+    }
+    *sweeps_out = sweeps;
+    *converged_out = converged;
+}
+
+// Householder QR with column pivoting of A (mrows x ncols, ld lda) in place, stopped early once
+// every remaining column is below sqrt(stop2) in norm (LAPACK dgeqp3 semantics for the part that
+// is computed: A P = Q R with R in the upper triangle, pvt[s] = original index of column s).
+// stop2 < 0 disables the early stop; stop2 == 0 with rel > 0 sets stop2 = (rel * |r_00|)^2 after
+// the first pivot.  Column norms are recomputed exactly while each column is updated, so no
+// norm downdating is needed.  Returns the number of rows of R that were computed.
+__device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double stop2, double rel, double *nrm,
+                              int *pvt, double *red, int *redi) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int j = warp; j < ncols; j += nw) {
+        const double *col = A + (size_t) j * lda;
+        double t = 0.0;
+        for (int i = lane; i < mrows; i += 32) t = fma(col[i], col[i], t);
+        t = warp_sum(t);
+        if (lane == 0) nrm[j] = t;
+    }
+    for (int j = threadIdx.x; j < ncols; j += blockDim.x) pvt[j] = j;
+    __syncthreads();
+    const int kk = mrows < ncols ? mrows : ncols;
+    int rkeep = kk;
+    for (int s = 0; s < kk; s++) {
+        // pivot = argmax of the remaining squared norms (ties to the lower index)
+        double bv = -1.0;
+        int bi = s;
+        for (int j = s + threadIdx.x; j < ncols; j += blockDim.x)
+            if (nrm[j] > bv) {
+                bv = nrm[j];
+                bi = j;
+            }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            red[warp] = bv;
+            redi[warp] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double v = red[0];
+            int b = redi[0];
+            for (int w = 1; w < nw; w++)
+                if (red[w] > v || (red[w] == v && redi[w] < b)) {
+                    v = red[w];
+                    b = redi[w];
+                }
+            red[32] = v;
+            redi[32] = b;
+            if (s == 0 && stop2 == 0.0 && rel > 0.0) red[33] = rel * rel * v;
+            else if (s == 0) red[33] = stop2;
+        }
+        __syncthreads();
+        bv = red[32];
+        bi = redi[32];
+        const double lim = red[33];
+        if (bv <= lim || bv <= 0.0) {
+            rkeep = s;
+            break;
+        }
+        if (bi != s) {
+            double *cs = A + (size_t) s * lda, *cb = A + (size_t) bi * lda;
+            for (int i = threadIdx.x; i < mrows; i += blockDim.x) {
+                const double t = cs[i];
+                cs[i] = cb[i];
+                cb[i] = t;
+            }
+            if (threadIdx.x == 0) {
+                const double t = nrm[s];
+                nrm[s] = nrm[bi];
+                nrm[bi] = t;
+                const int ti = pvt[s];
+                pvt[s] = pvt[bi];
+                pvt[bi] = ti;
+            }
+        }
+        __syncthreads();
+        // Householder vector of column s (rows s..mrows-1), dlarfg convention.
+        double *x = A + (size_t) s * lda;
+        double ss = 0.0;
+        for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) ss = fma(x[i], x[i], ss);
+        ss = warp_sum(ss);
+        __syncthreads();
+        if (lane == 0) red[warp] = ss;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < nw; w++) t += red[w];
+            const double alpha = x[s];
+            double tau = 0.0, scale = 0.0, beta = alpha;
+            if (t != 0.0) {
+                beta = -copysign(sqrt(fma(alpha, alpha, t)), alpha);
+                tau = (beta - alpha) / beta;
+                scale = 1.0 / (alpha - beta);
+            }
+            x[s] = beta;
+            red[40] = tau;
+            red[41] = scale;
+        }
+        __syncthreads();
+        const double tau = red[40], scale = red[41];
+        for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) x[i] *= scale;
+        __syncthreads();
+        // Apply H to the remaining columns; recompute their norms below row s exactly.
+        for (int j = s + 1 + warp; j < ncols; j += nw) {
+            double *y = A + (size_t) j * lda;
+            double w = 0.0;
+            if (tau != 0.0) {
+                w = lane == 0 ? y[s] : 0.0;
+                for (int i = s + 1 + lane; i < mrows; i += 32) w = fma(x[i], y[i], w);
+                w = warp_sum(w) * tau;
+            }
+            if (lane == 0) y[s] -= w;
+            double nn = 0.0;
+            for (int i = s + 1 + lane; i < mrows; i += 32) {
+                const double a = fma(-w, x[i], y[i]);
+                y[i] = a;
+                nn = fma(a, a, nn);
+            }
+            nn = warp_sum(nn);
+            if (lane == 0) nrm[j] = nn;
+        }
+        __syncthreads();
+    }
+    return rkeep;
 }
 
 template <int RPL>
-__global__ void __launch_bounds__(SVD_THREADS) core_svd_kernel(const DevUpdate *ups, Workspace ws, Params p,
+__global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdate *ups, Workspace ws, Params p,
                                                                int smem_doubles) {
     extern __shared__ double sm[];
     __shared__ int s_rot, s_rank;
+    __shared__ double s_amax;
     const int slot = blockIdx.x;
     int *meta = ws.meta + (size_t) slot * META_INTS;
     if (meta[META_STATUS] != HCGB_OK || !meta[META_CKIND]) return;
@@ -82,11 +295,16 @@ __global__ void __launch_bounds__(SVD_THREADS) core_svd_kernel(const DevUpdate *
     const double *RU = base + ws.off_ustack;
     const double *RV = base + ws.off_vstack;
     double *Mc = base + ws.off_mcopy;
-    // Aux arrays at the start of shared memory: sigma, 1/sigma (sorted), permutation.
+    // Aux arrays at the start of shared memory: sorted sigma, scratch, column norms, the sort
+    // permutation, the QR pivots and a small reduction area.
     double *sig = sm;
     double *inv = sig + ws.kmax;
-    int *perm = reinterpret_cast<int *>(inv + ws.kmax);
-    double *pool = inv + ws.kmax + (ws.kmax + 1) / 2 + 1;
+    double *nrm = inv + ws.kmax;
+    int *perm = reinterpret_cast<int *>(nrm + ws.kmax);
+    int *pvt = perm + ws.kmax;
+    double *red = nrm + ws.kmax + ws.kmax + 1;
+    int *redi = reinterpret_cast<int *>(red + 48);
+    double *pool = red + 48 + 24;
     const int pool_doubles = smem_doubles - (int) (pool - sm);
     // Working copy of M: shared memory when it fits, else the workspace.
     double *Mw;
@@ -126,42 +344,53 @@ __global__ void __launch_bounds__(SVD_THREADS) core_svd_kernel(const DevUpdate *
     }
     __syncthreads();
 
-    // 2. One-sided Jacobi on the kV columns of M.
-    const double tol = DBL_EPSILON * sqrt((double) (kU > 1 ? kU : 1));
-    const int n2 = kV + (kV & 1);
-    int sweeps = 0;
-    bool converged = (kV < 2);
-    while (!converged && sweeps < MAX_JACOBI_SWEEPS) {
-        if (threadIdx.x == 0) s_rot = 0;
-        __syncthreads();
-        for (int t = 0; t < n2 - 1; t++) {
-            for (int pp = warp; pp < n2 / 2; pp += nw) {
-                int i, j;
-                jacobi_pair(t, pp, n2, i, j);
-                if (i >= kV || j >= kV) continue;
-                const bool rot = rotate_pair<RPL>(Mw + (size_t) i * ldw, Mw + (size_t) j * ldw, kU, tol);
-                if (rot && lane == 0) atomicAdd(&s_rot, 1);
-            }
-            __syncthreads();
+    // 2. Rank-revealing QR with column pivoting, M P = Q R, stopped once every remaining column
+    //    is below 1e-4 of the truncation threshold: the dropped block R22 changes no singular
+    //    value by more than sqrt(kV) * 1e-4 * threshold.  (Fixed-rank mode keeps every row.)
+    double stop2 = -1.0, rel = 0.0;
+    if (p.fixed_rank <= 0) {
+        if (p.truncated) {
+            stop2 = 0.0;
+            rel = 1e-4 * p.accuracy;  // |r_00| <= sigma_0, so this threshold is conservative
+        } else {
+            stop2 = (1e-4 * p.accuracy) * (1e-4 * p.accuracy);
         }
-        sweeps++;
-        converged = (s_rot == 0);
-        __syncthreads();
     }
+    int rk = qrcp_truncated(Mw, ldw, kU, kV, stop2, rel, nrm, pvt, red, redi);
+    if (rk < 1) rk = 1;
+    double *XV = base + ws.off_xv;
+    // 3. X = R(0:rk, :)^T (kV x rk), staged through XV, then into the working buffer (ld kV).
+    for (int i = warp; i < rk; i += nw)
+        for (int l = lane; l < kV; l += 32) XV[l + (size_t) i * ld] = l >= i ? Mw[i + (size_t) l * ldw] : 0.0;
+    __syncthreads();
+    double *X = Mw;
+    const int ldx = kV;
+    for (int i = warp; i < rk; i += nw)
+        for (int l = lane; l < kV; l += 32) X[l + (size_t) i * ldx] = XV[l + (size_t) i * ld];
+    __syncthreads();
 
-    // 3. Singular values, descending order (stable), rank.
-    for (int j = warp; j < kV; j += nw) {
-        const double *col = Mw + (size_t) j * ldw;
-        double s = 0.0;
-        for (int r = lane; r < kU; r += 32) s = fma(col[r], col[r], s);
-        s = warp_sum(s);
-        if (lane == 0) inv[j] = sqrt(s);  // unsorted sigma, temporarily in inv[]
+    // 4. One-sided Jacobi on the rk columns of X (lane group sized to the column length kV).
+    //    X J = W with orthogonal columns: sigma_i = ||w_i||, right singular vectors P W Sigma^-1.
+    int sweeps = 0;
+    bool converged = true;
+    if (kV <= 64) jacobi<8, 8>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
+    else if (kV <= 128) jacobi<16, 8>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
+    else if (kV <= 256 || RPL <= 8) jacobi<32, 8>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
+    else jacobi<32, RPL>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
+
+    // 5. Singular values, descending order (stable), rank rule (omp/kernels.cpp:82-104).
+    for (int j = warp; j < rk; j += nw) {
+        const double *col = X + (size_t) j * ldx;
+        double t = 0.0;
+        for (int r = lane; r < kV; r += 32) t = fma(col[r], col[r], t);
+        t = warp_sum(t);
+        if (lane == 0) inv[j] = sqrt(t);  // unsorted sigma, temporarily in inv[]
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < kV; j += blockDim.x) {
+    for (int j = threadIdx.x; j < rk; j += blockDim.x) {
         const double sj = inv[j];
         int pos = 0;
-        for (int l = 0; l < kV; l++) {
+        for (int l = 0; l < rk; l++) {
             const double sl = inv[l];
             pos += (sl > sj) || (sl == sj && l < j);
         }
@@ -175,9 +404,10 @@ __global__ void __launch_bounds__(SVD_THREADS) core_svd_kernel(const DevUpdate *
         if (p.fixed_rank > 0) {
             r = p.fixed_rank < k ? p.fixed_rank : k;
         } else {
-            r = sizeS;
+            // sigma_i for i >= rk are below the threshold by construction of the QR stop.
+            r = rk < sizeS ? rk : sizeS;
             const double thr = p.truncated ? p.accuracy * sig[0] : p.accuracy;
-            for (int i = 1; i < sizeS; i++)
+            for (int i = 1; i < rk; i++)
                 if (sig[i] < thr) {
                     r = i;
                     break;
@@ -186,56 +416,56 @@ __global__ void __launch_bounds__(SVD_THREADS) core_svd_kernel(const DevUpdate *
         if (r < 1) r = 1;
         const int maxr = ups[slot].c.max_rank;
         if (r > maxr) r = maxr;
-        if (r > sizeS) r = sizeS;
+        if (r > rk) r = rk;
         s_rank = r;
         meta[META_NEWRANK] = r;
         meta[META_SWEEPS] = sweeps;
+        meta[META_CORE_COLS] = rk;
         if (!converged) meta[META_STATUS] = HCGB_NOT_CONVERGED;
     }
     __syncthreads();
     const int r = s_rank;
-    for (int i = threadIdx.x; i < r; i += blockDim.x) inv[i] = sig[i] > 0.0 ? 1.0 / sig[i] : 0.0;
+    for (int i = threadIdx.x; i < r; i += blockDim.x) inv[i] = sig[i] > 1e-150 ? 1.0 / (sig[i] * sig[i]) : 0.0;
+
+    // 6. Right factor in the small basis: XV = P W_r (= V_r Sigma_r), n rows, zero below kV.
+    for (int i = warp; i < r; i += nw) {
+        const double *w = X + (size_t) perm[i] * ldx;
+        for (int l = lane; l < kV; l += 32) XV[pvt[l] + (size_t) i * ld] = w[l];
+        for (int l = kV + lane; l < n; l += 32) XV[l + (size_t) i * ld] = 0.0;
+    }
     __syncthreads();
 
-    // 4. New left factor in the small basis: C.U[:, i] = [w_perm(i) / sigma_i ; 0] (m rows).
+    // 7. Left factor in the small basis: C.U[:, i] = [M XV[:, i] / sigma_i^2 ; 0] (= U_r), on DMMA.
     double *CU = ups[slot].c.data;
     const int ldcu = ups[slot].c.rows;
-    for (int i = warp; i < r; i += nw) {
-        const double *col = Mw + (size_t) perm[i] * ldw;
-        const double s = inv[i];
-        for (int l = lane; l < m; l += 32) CU[l + (size_t) i * ldcu] = l < kU ? col[l] * s : 0.0;
-    }
-    // 5. Right factor Z = M^T Ut_r (kV x r) into XV (n rows, zero below kV), on DMMA.
-    double *XV = base + ws.off_xv;
     {
-        const int ntr = (kV + 7) >> 3, ntc = (r + 7) >> 3;
+        const int ntr = (kU + 7) >> 3, ntc = (r + 7) >> 3;
         for (int idx = warp; idx < ntr * ntc; idx += nw) {
             const int tr = idx % ntr, tc = idx / ntr;
-            const int jrow = tr * 8 + lr, icol = tc * 8 + lr;
-            const double *ucol = Mw + (size_t) perm[icol < r ? icol : 0] * ldw;
-            const double us = icol < r ? inv[icol] : 0.0;
+            const int irow = tr * 8 + lr, icol = tc * 8 + lr;
+            const double *vcol = XV + (size_t) (icol < r ? icol : 0) * ld;
             double d0 = 0.0, d1 = 0.0;
-            for (int l4 = 0; l4 < kU; l4 += 4) {
+            for (int l4 = 0; l4 < kV; l4 += 4) {
                 const int l = l4 + lc;
-                const double av = (jrow < kV && l < kU) ? Mc[l + (size_t) jrow * ldm] : 0.0;
-                const double bv = (l < kU) ? ucol[l] * us : 0.0;
+                const double av = (irow < kU && l < kV) ? Mc[irow + (size_t) l * ldm] : 0.0;
+                const double bv = (icol < r && l < kV) ? vcol[l] : 0.0;
                 dmma(d0, d1, av, bv);
             }
             const int col = tc * 8 + 2 * lc;
-            if (jrow < kV && col < r) XV[jrow + (size_t) col * ld] = d0;
-            if (jrow < kV && col + 1 < r) XV[jrow + (size_t) (col + 1) * ld] = d1;
+            if (irow < kU && col < r) CU[irow + (size_t) col * ldcu] = d0 * inv[col];
+            if (irow < kU && col + 1 < r) CU[irow + (size_t) (col + 1) * ldcu] = d1 * inv[col + 1];
         }
         for (int i = warp; i < r; i += nw)
-            for (int l = kV + lane; l < n; l += 32) XV[l + (size_t) i * ld] = 0.0;
+            for (int l = kU + lane; l < m; l += 32) CU[l + (size_t) i * ldcu] = 0.0;
     }
 }
 
 }  // namespace
 
 size_t svd_smem_bytes(int kmax) {
-    size_t aux = (size_t) 2 * kmax + (kmax + 1) / 2 + 1;
+    size_t aux = (size_t) 4 * kmax + 1 + 48 + 24;
     size_t want = aux + (size_t) kmax * kmax;
-    const size_t cap = 200 * 1024 / sizeof(double);
+    const size_t cap = 110 * 1024 / sizeof(double);  // two CTAs per SM
     if (want > cap) want = cap;
     return want * sizeof(double);
 }

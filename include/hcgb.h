@@ -78,6 +78,7 @@ typedef struct {
     int new_rank;   /* rank of C after the update (0 for a dense C) */
     int sweeps;     /* Jacobi sweeps the core SVD took */
     int side;       /* 0: stacked [Cu | alpha Au]; 1: stacked [Cu | alpha Au (Av Bu)] */
+    int core_cols;  /* rows of R the rank-revealing QR of the core kept (columns Jacobi rotated) */
 } hcgb_update_info;
 
 /* Pipeline stages, for hcgb_profile_read. */
