@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--cpu-tiles", type=int, default=0, help="C tiles in the CPU sample (0: one per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the dense FP64 accuracy check")
+    ap.add_argument("--groups", type=int, default=8, help="independent C-tile groups (streams)")
     return ap.parse_args()
 
 
@@ -251,6 +252,7 @@ def gpu_arm(args, rank, world, local):
     params = T.CompressionParameters(w["accuracy"], truncated_svd=True)
     info = T.info_buffer(n_updates)
     dmma_peak, dfma_peak = ctx.fp64_peak()
+    ctx.set_concurrency(args.groups)
 
     def step(record_info=False):
         Cw.arena.copy_(C0.arena)
@@ -266,8 +268,8 @@ def gpu_arm(args, rank, world, local):
     # ---- timed region (device-resident inputs)
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.profile(False)
     ctx.profile_reset()
-    ctx.profile(True)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -280,14 +282,23 @@ def gpu_arm(args, rank, world, local):
     if world > 1:
         torch.distributed.barrier()
     ms = e0.elapsed_time(e1) / args.steps
-    ctx.profile(False)
-    stages = ctx.profile_read()
-    launches = int(sum(v[1] for v in stages.values()))
+    launches = int(sum(v[1] for v in ctx.profile_read().values()))
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = world * n_updates / (ms * 1e-3)
+
+    # ---- one more multiply, serialised on one stream with CUDA events around every stage:
+    #      the per-kernel durations behind the roofline (not part of the timed region).
+    ctx.set_concurrency(1)
+    ctx.profile_reset()
+    ctx.profile(True)
+    step()
+    ctx.profile(False)
+    stages = ctx.profile_read()
+    ctx.set_concurrency(args.groups)
+    serial_ms = sum(v[0] for v in stages.values())
 
     # ---- end to end through the public API: host (pinned) inputs in, result back to the host
     a_pin = torch.from_numpy(a_host).pin_memory()
@@ -344,7 +355,7 @@ def gpu_arm(args, rank, world, local):
     total_stage_ms = sum(v[0] for v in stages.values())
     dom = max(stages, key=lambda s: stages[s][0])
     dom_ms_per_launch = stages[dom][0] / max(stages[dom][1], 1)
-    dom_flops_per_launch = st_flops.get(dom, 0.0) / max(stages[dom][1] / args.steps, 1)
+    dom_flops_per_launch = st_flops.get(dom, 0.0) / max(stages[dom][1], 1)
     tensor_stages = {"gemm", "qr", "apply_q"}
     peak = dmma_peak if dom in tensor_stages else dfma_peak
     achieved = dom_flops_per_launch / (dom_ms_per_launch * 1e-3) / 1e12
@@ -382,7 +393,7 @@ def gpu_arm(args, rank, world, local):
         "config": {"workload": args.workload, "n": w["n"], "nb": w["nb"], "tiles": f"{nt}x{nt}",
                    "updates_per_step": n_updates, "accuracy": w["accuracy"], "threshold": "relative",
                    "dense_diagonal": w["dense_diagonal"], "max_rank": maxr, "form": "plain_fp64",
-                   "parallelism": "replicas" if world > 1 else "single_gpu",
+                   "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups,
                    "l2": "inputs larger than L2 (A, C arenas 1.4 GB each), no flush"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "tensor" if dom in tensor_stages else "fp64_simt", "kernel": dom,
@@ -392,7 +403,8 @@ def gpu_arm(args, rank, world, local):
                                     "MEASURED_PEAKS.json has no FP64 figure"},
         "fp64": {"pasc_gflops": pasc / (ms * 1e-3) / 1e9, "pasc_frac_of_dmma_peak": pasc / (ms * 1e-3) / 1e12 / dmma_peak,
                  "dmma_peak_tflops": dmma_peak, "dfma_peak_tflops": dfma_peak},
-        "stages_ms_per_step": {s: stages[s][0] / args.steps for s in stages},
+        "stages_ms_serial_step": {s: stages[s][0] for s in stages},
+        "serial_step_ms": serial_ms,
         "stage_share": {s: stages[s][0] / total_stage_ms for s in stages},
         "gpu_launches": launches,
         "ranks": {"mean_final": float(rk[comp_mask].mean()), "max_final": int(rk[comp_mask].max()),
@@ -401,6 +413,8 @@ def gpu_arm(args, rank, world, local):
                   "max_sweeps": int(info_h[:, 6].max()),
                   "mean_sweeps": float(info_h[info_h[:, 4] > 0, 6].mean()),
                   "mean_core_cols": float(info_h[info_h[:, 4] > 0, 8].mean())},
+        "core_kcycles_mean": {nm: float(info_h[info_h[:, 4] > 0, 9 + q].mean())
+                              for q, nm in enumerate(["product", "qrcp", "jacobi", "factors"])},
         "check": check,
         "cpu_baseline": cpu,
         "clocks": clocks,

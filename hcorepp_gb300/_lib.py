@@ -44,7 +44,8 @@ class Params(C.Structure):
 class UpdateInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("rank_a", C.c_int), ("rank_b", C.c_int), ("rank_c", C.c_int),
                 ("k", C.c_int), ("new_rank", C.c_int), ("sweeps", C.c_int), ("side", C.c_int),
-                ("core_cols", C.c_int)]
+                ("core_cols", C.c_int), ("kc_product", C.c_int), ("kc_qrcp", C.c_int), ("kc_jacobi", C.c_int),
+                ("kc_factors", C.c_int)]
 
 
 INFO_FIELDS = [f[0] for f in UpdateInfo._fields_]
@@ -84,9 +85,10 @@ def lib():
         L.hcgb_profile_reset.argtypes = [vp]
         L.hcgb_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong), ip]
         L.hcgb_fp64_peak.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.hcgb_set_concurrency.argtypes = [vp, ip]
         for name in ("hcgb_context_create", "hcgb_context_destroy", "hcgb_context_set_stream", "hcgb_sync",
                      "hcgb_gemm_batch", "hcgb_tlr_gemm", "hcgb_tile_gemm", "hcgb_profile_enable",
-                     "hcgb_profile_reset", "hcgb_profile_read", "hcgb_fp64_peak"):
+                     "hcgb_profile_reset", "hcgb_profile_read", "hcgb_fp64_peak", "hcgb_set_concurrency"):
             getattr(L, name).restype = C.c_int
         _LIB = L
     return _LIB
@@ -129,6 +131,9 @@ class Context:
         cnt = (C.c_longlong * n)()
         self.check(lib().hcgb_profile_read(self._h, ms, cnt, n))
         return {STAGES[i]: (ms[i], cnt[i]) for i in range(n)}
+
+    def set_concurrency(self, groups: int):
+        self.check(lib().hcgb_set_concurrency(self._h, int(groups)))
 
     def fp64_peak(self):
         d, f = C.c_double(), C.c_double()

@@ -28,6 +28,10 @@ struct hcgb_context {
     std::vector<std::vector<cudaEvent_t>> ev_pending;  // one group of HCGB_NUM_STAGES + 1 per pipeline
     double stage_ms[HCGB_NUM_STAGES] = {0};
     long long stage_launches[HCGB_NUM_STAGES] = {0};
+    // independent C-tile groups of hcgb_tlr_gemm, one stream each
+    int groups = 8;
+    std::vector<cudaStream_t> group_streams;
+    std::vector<cudaEvent_t> group_events;  // [0] fork, [1..] joins
 };
 
 namespace {
@@ -171,9 +175,9 @@ std::vector<cudaEvent_t> take_events(hcgb_context *ctx, int count) {
 }
 
 // Launch the full pipeline for n updates whose descriptors are already on the device.
-void launch_pipeline(hcgb_context *ctx, const DevUpdate *dups, GemmJob *djobs, int n, double alpha, double beta,
-                     const Workspace &ws, const BatchShape &sh, const Params &p, hcgb_update_info *info) {
-    cudaStream_t st = ctx->stream;
+void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, GemmJob *djobs, int n, double alpha,
+                     double beta, const Workspace &ws, const BatchShape &sh, const Params &p,
+                     hcgb_update_info *info) {
     std::vector<cudaEvent_t> ev;
     if (ctx->prof) ev = take_events(ctx, HCGB_NUM_STAGES + 1);
     auto mark = [&](int i) {
@@ -276,6 +280,8 @@ int hcgb_context_destroy(hcgb_context *ctx) {
     for (auto &g : ctx->ev_pending)
         for (auto e : g) cudaEventDestroy(e);
     for (auto e : ctx->ev_free) cudaEventDestroy(e);
+    for (auto st : ctx->group_streams) cudaStreamDestroy(st);
+    for (auto e : ctx->group_events) cudaEventDestroy(e);
     delete ctx;
     return HCGB_OK;
 }
@@ -317,7 +323,7 @@ int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const h
         if (updates[i].a.kind == HCGB_DENSE && updates[i].b.kind == HCGB_DENSE &&
             updates[i].c.kind == HCGB_COMPRESSED)
             return fail(ctx, HCGB_UNSUPPORTED, "hcgb_gemm_batch: DDC updates go through hcgb_tile_gemm");
-        dv[i] = DevUpdate{to_dev(updates[i].a), to_dev(updates[i].b), to_dev(updates[i].c)};
+        dv[i] = DevUpdate{to_dev(updates[i].a), to_dev(updates[i].b), to_dev(updates[i].c), i};
     }
     BatchShape sh = shape_of(updates, n);
     Workspace ws;
@@ -326,7 +332,7 @@ int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const h
     DevUpdate *dups;
     GemmJob *djobs;
     if ((rc = upload_updates(ctx, dv, &dups, &djobs))) return rc;
-    launch_pipeline(ctx, dups, djobs, n, alpha, beta, ws, sh, to_params(params), info_dev);
+    launch_pipeline(ctx, ctx->stream, dups, djobs, n, alpha, beta, ws, sh, to_params(params), info_dev);
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
 }
@@ -339,14 +345,26 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         return fail(ctx, HCGB_BAD_ARG, "hcgb_tlr_gemm: bad grid");
     HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
     const int n = mt * nt;
-    // All waves' descriptors in one upload: wave kk holds (A(i,kk), B(kk,j), C(i,j)) for every C tile.
+    // C tiles are split into G groups (tile index mod G); each group runs its own chain of k-waves
+    // on its own stream, so one slow update delays only its group, not every C tile.
+    const int G = std::max(1, std::min(ctx->groups, n));
+    std::vector<int> first(G + 1, 0), members;
+    for (int g = 0; g < G; g++) {
+        first[g] = (int) members.size();
+        for (int idx = g; idx < n; idx += G) members.push_back(idx);
+    }
+    first[G] = n;
+    // Descriptors laid out [group][wave][member]; record uid = wave * n + tile index.
     std::vector<hcgb_update> all((size_t) n * kt);
     std::vector<DevUpdate> dv((size_t) n * kt);
-    for (int kk = 0; kk < kt; kk++)
-        for (int j = 0; j < nt; j++)
-            for (int i = 0; i < mt; i++) {
-                const size_t w = (size_t) kk * n + i + (size_t) j * mt;
-                hcgb_update u{a_grid[i + (size_t) kk * mt], b_grid[kk + (size_t) j * kt], c_grid[i + (size_t) j * mt]};
+    for (int g = 0; g < G; g++) {
+        const int ng = first[g + 1] - first[g];
+        for (int kk = 0; kk < kt; kk++)
+            for (int q = 0; q < ng; q++) {
+                const int idx = members[first[g] + q];
+                const int i = idx % mt, j = idx / mt;
+                const size_t w = (size_t) first[g] * kt + (size_t) kk * ng + q;
+                hcgb_update u{a_grid[i + (size_t) kk * mt], b_grid[kk + (size_t) j * kt], c_grid[idx]};
                 int rc;
                 if ((rc = check_tile(ctx, u.a, "A")) || (rc = check_tile(ctx, u.b, "B")) ||
                     (rc = check_tile(ctx, u.c, "C")))
@@ -354,13 +372,13 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
                 if (u.a.kind == HCGB_DENSE && u.b.kind == HCGB_DENSE && u.c.kind == HCGB_COMPRESSED)
                     return fail(ctx, HCGB_UNSUPPORTED, "hcgb_tlr_gemm: DDC updates are not batched");
                 all[w] = u;
-                dv[w] = DevUpdate{to_dev(u.a), to_dev(u.b), to_dev(u.c)};
+                dv[w] = DevUpdate{to_dev(u.a), to_dev(u.b), to_dev(u.c), kk * n + idx};
             }
+    }
     BatchShape sh = shape_of(all.data(), (int) all.size());
     Workspace ws;
     int rc = prepare_workspace(ctx, sh, n, false, &ws);
     if (rc) return rc;
-    // Descriptor upload: DevUpdate[n*kt] then jobs for one wave (3n).
     const size_t ub = sizeof(DevUpdate) * dv.size(), ub_al = (ub + 255) / 256 * 256;
     const size_t jb = sizeof(GemmJob) * 3 * (size_t) n;
     if ((rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb))) return rc;
@@ -371,15 +389,46 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     auto *dups = static_cast<DevUpdate *>(ctx->desc);
     auto *djobs = reinterpret_cast<GemmJob *>(static_cast<char *>(ctx->desc) + ub_al);
     const Params p = to_params(params);
-    for (int kk = 0; kk < kt; kk++) {
-        BatchShape shw = shape_of(all.data() + (size_t) kk * n, n);
-        shw.ld = sh.ld;
-        shw.kmax = sh.kmax;
-        shw.rmax = sh.rmax;
-        launch_pipeline(ctx, dups + (size_t) kk * n, djobs, n, alpha, beta, ws, shw, p,
-                        info_dev ? info_dev + (size_t) kk * n : nullptr);
+    // Streams and fork/join events for the groups.
+    while ((int) ctx->group_streams.size() < G) {
+        cudaStream_t s;
+        HCGB_CUDA(ctx, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        ctx->group_streams.push_back(s);
+    }
+    while ((int) ctx->group_events.size() < G + 1) {
+        cudaEvent_t e;
+        HCGB_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->group_events.push_back(e);
+    }
+    const bool single = (G == 1);
+    if (!single) HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[0], ctx->stream));
+    for (int g = 0; g < G; g++) {
+        const int ng = first[g + 1] - first[g];
+        cudaStream_t st = single ? ctx->stream : ctx->group_streams[g];
+        if (!single) HCGB_CUDA(ctx, cudaStreamWaitEvent(st, ctx->group_events[0], 0));
+        Workspace wg = ws;
+        wg.base = ws.base + ws.slot_doubles * (size_t) first[g];
+        wg.meta = ws.meta + (size_t) META_INTS * first[g];
+        for (int kk = 0; kk < kt; kk++) {
+            const size_t off = (size_t) first[g] * kt + (size_t) kk * ng;
+            BatchShape shw = shape_of(all.data() + off, ng);
+            shw.ld = sh.ld;
+            shw.kmax = sh.kmax;
+            shw.rmax = sh.rmax;
+            launch_pipeline(ctx, st, dups + off, djobs + 3 * (size_t) first[g], ng, alpha, beta, wg, shw, p, info_dev);
+        }
+        if (!single) {
+            HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[g + 1], st));
+            HCGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->group_events[g + 1], 0));
+        }
     }
     HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+int hcgb_set_concurrency(hcgb_context *ctx, int groups) {
+    if (!ctx || groups < 1) return HCGB_BAD_ARG;
+    ctx->groups = groups;
     return HCGB_OK;
 }
 
@@ -496,7 +545,7 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
             cleanup();
             return rc;
         }
-        std::vector<DevUpdate> dv{DevUpdate{to_dev(A), to_dev(B), to_dev(*c)}};
+        std::vector<DevUpdate> dv{DevUpdate{to_dev(A), to_dev(B), to_dev(*c), 0}};
         DevUpdate *dups;
         GemmJob *djobs;
         if ((rc = upload_updates(ctx, dv, &dups, &djobs))) {

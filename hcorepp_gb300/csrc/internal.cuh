@@ -61,6 +61,7 @@ struct DevTile {
 
 struct DevUpdate {
     DevTile a, b, c;
+    int uid;  // index of this update's record in the caller's hcgb_update_info array
 };
 
 // Per-update bookkeeping written by the plan kernel and read by the later stages.
@@ -77,6 +78,10 @@ enum MetaField {
     META_NEWRANK,
     META_SWEEPS,
     META_CORE_COLS,  // rows of R kept by the rank-revealing QR of the core
+    META_KC_PRODUCT,  // core-kernel phase durations in units of 1024 SM cycles (diagnostics)
+    META_KC_QRCP,
+    META_KC_JACOBI,
+    META_KC_FACTORS,
     META_INTS = 16
 };
 

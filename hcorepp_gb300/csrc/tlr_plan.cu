@@ -287,7 +287,8 @@ __global__ void __launch_bounds__(256) finalize_kernel(const DevUpdate *ups, Wor
         r.sweeps = meta[META_SWEEPS];
         r.side = meta[META_SIDE];
         r.core_cols = meta[META_CORE_COLS];
-        info[s] = r;
+        for (int q = 0; q < 4; q++) r.core_kcycles[q] = meta[META_KC_PRODUCT + q];
+        info[ups[s].uid] = r;
     }
     if (!ok) return;
     const DevUpdate u = ups[s];

@@ -317,6 +317,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         ldw = ldm;
     }
 
+    const long long t0 = clock64();
     // 1. M = R_U R_V^T on DMMA (R_U = triu of the U stack's top kU rows, likewise R_V).
     {
         const int ntr = (kU + 7) >> 3, ntc = (kV + 7) >> 3;
@@ -356,7 +357,9 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
             stop2 = (1e-4 * p.accuracy) * (1e-4 * p.accuracy);
         }
     }
+    const long long t1 = clock64();
     int rk = qrcp_truncated(Mw, ldw, kU, kV, stop2, rel, nrm, pvt, red, redi);
+    const long long t2 = clock64();
     if (rk < 1) rk = 1;
     double *XV = base + ws.off_xv;
     // 3. X = R(0:rk, :)^T (kV x rk), staged through XV, then into the working buffer (ld kV).
@@ -378,6 +381,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     else if (kV <= 256 || RPL <= 8) jacobi<32, 8>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
     else jacobi<32, RPL>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
 
+    const long long t3 = clock64();
     // 5. Singular values, descending order (stable), rank rule (omp/kernels.cpp:82-104).
     for (int j = warp; j < rk; j += nw) {
         const double *col = X + (size_t) j * ldx;
@@ -457,6 +461,13 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         }
         for (int i = warp; i < r; i += nw)
             for (int l = kU + lane; l < m; l += 32) CU[l + (size_t) i * ldcu] = 0.0;
+    }
+    if (threadIdx.x == 0) {
+        const long long t4 = clock64();
+        meta[META_KC_PRODUCT] = (int) ((t1 - t0) >> 10);
+        meta[META_KC_QRCP] = (int) ((t2 - t1) >> 10);
+        meta[META_KC_JACOBI] = (int) ((t3 - t2) >> 10);
+        meta[META_KC_FACTORS] = (int) ((t4 - t3) >> 10);
     }
 }
 

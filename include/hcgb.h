@@ -79,6 +79,8 @@ typedef struct {
     int sweeps;     /* Jacobi sweeps the core SVD took */
     int side;       /* 0: stacked [Cu | alpha Au]; 1: stacked [Cu | alpha Au (Av Bu)] */
     int core_cols;  /* rows of R the rank-revealing QR of the core kept (columns Jacobi rotated) */
+    int core_kcycles[4]; /* core SVD phases in units of 1024 SM cycles: core product, pivoted QR,
+                            Jacobi, new factors (diagnostics) */
 } hcgb_update_info;
 
 /* Pipeline stages, for hcgb_profile_read. */
@@ -122,6 +124,11 @@ int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const h
 int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const hcgb_tile *a_grid,
                   const hcgb_tile *b_grid, double beta, const hcgb_tile *c_grid, const hcgb_params *params,
                   hcgb_update_info *info_dev);
+
+/* Number of independent C-tile groups hcgb_tlr_gemm runs concurrently (one stream each; default 8;
+ * 1 = every k-wave of the whole grid in one stream, the order the reference's driver uses).
+ * The results do not depend on it. */
+int hcgb_set_concurrency(hcgb_context *ctx, int groups);
 
 /* Single tile update, the drop-in for HCore<T>::Gemm (src/api/HCore.cpp:23-344).  op_a/op_b
  * accept HCGB_NOTRANS and HCGB_TRANS.  Synchronous: on return *c's rank on the device has been

@@ -209,3 +209,36 @@ def test_tlr_multiply_vs_oracle(T):
         for j in range(nt):
             if kinds[i][j] == L.COMPRESSED:
                 assert abs(granks[i, j] - otiles["C"][i][j].rank) <= 1
+
+
+def test_tlr_multiply_concurrency_invariant(T):
+    """The C-tile grouping (streams) changes the schedule, never the arithmetic: bitwise equal."""
+    import torch
+    from hcorepp_gb300 import _lib as L
+    from hcorepp_gb300.problems import KernelMatrix
+    nt, nb, acc = 4, 96, 1e-8
+    km = KernelMatrix(nt * nb, nb, 2, 0.1, 1)
+    kc = KernelMatrix(nt * nb, nb, 2, 0.1, 2)
+    kinds = [[L.COMPRESSED] * nt for _ in range(nt)]
+    A = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+    C0 = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+    for i in range(nt):
+        for j in range(nt):
+            ta = compressed_from_dense(km.tile(i, j), acc)
+            tc = compressed_from_dense(kc.tile(i, j), acc)
+            A.set_tile(i, j, u=ta.u, v=ta.v)
+            C0.set_tile(i, j, u=tc.u, v=tc.v)
+    ctx = T.run_context()
+    outs = []
+    for groups in (1, 3, 8):
+        ctx.set_concurrency(groups)
+        C = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+        C.arena.copy_(C0.arena)
+        C.ranks.copy_(C0.ranks)
+        T.tlr_gemm(1.0, A, A, 1.0, C, T.CompressionParameters(acc, truncated_svd=True))
+        torch.cuda.synchronize()
+        outs.append((C.arena.cpu().numpy().copy(), C.ranks.cpu().numpy().copy()))
+    ctx.set_concurrency(8)
+    for arena, ranks in outs[1:]:
+        np.testing.assert_array_equal(ranks, outs[0][1])
+        np.testing.assert_array_equal(arena, outs[0][0])
