@@ -86,6 +86,9 @@ def lib():
         L.hcgb_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong), ip]
         L.hcgb_fp64_peak.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.hcgb_set_concurrency.argtypes = [vp, ip]
+        L.hcgb_tile_gemm_noalloc.argtypes = [C.c_double, C.POINTER(Tile), C.POINTER(Tile), C.c_double,
+                                             C.POINTER(Tile), C.POINTER(Params), vp, vp]
+        L.hcgb_tile_gemm_noalloc.restype = C.c_int
         for name in ("hcgb_context_create", "hcgb_context_destroy", "hcgb_context_set_stream", "hcgb_sync",
                      "hcgb_gemm_batch", "hcgb_tlr_gemm", "hcgb_tile_gemm", "hcgb_profile_enable",
                      "hcgb_profile_reset", "hcgb_profile_read", "hcgb_fp64_peak", "hcgb_set_concurrency"):

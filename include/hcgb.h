@@ -153,6 +153,23 @@ int hcgb_profile_read(hcgb_context *ctx, double *ms_per_stage, long long *launch
  * denominators of the FP64 path. */
 int hcgb_fp64_peak(hcgb_context *ctx, double *dmma_tflops, double *dfma_tflops);
 
+/* One tile update that allocates nothing (no counterpart in the reference; an addition of this
+ * library).  For callers that may not allocate device memory themselves: task-runtime workers whose
+ * runtime owns the device memory and places the tile buffers, and real-time or embedded callers
+ * that forbid allocation after start-up.  Same arithmetic as hcgb_tile_gemm with NoTrans
+ * operands (combinations CCC, DCC, CDC, CCD, DCD, CDD, DDD), but asynchronous on `stream` (NULL =
+ * legacy default stream of the current device), no context, no host synchronisation: the new
+ * rank is written to c->rank on the device, and info_dev (optional, one device record) receives
+ * the update's hcgb_update_info.
+ * Scratch: a fixed 8 MiB array inside the library, one per GPU that loads it, held until the
+ * process exits.  Updates whose scratch layout does not fit are rejected with
+ * HCGB_POOL_TOO_SMALL (tiles up to 512 x 512 with capacities max_rank <= 170 fit).  All calls on a
+ * device share the array: calls that overlap on the GPU race, so order them.  The first call on
+ * each device looks up the array's device address (with that device current); make it before any
+ * stream capture begins. */
+int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hcgb_tile *b, double beta, hcgb_tile *c,
+                           const hcgb_params *params, void *stream, hcgb_update_info *info_dev);
+
 #ifdef __cplusplus
 }
 #endif
