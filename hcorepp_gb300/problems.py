@@ -84,6 +84,9 @@ WORKLOADS = {
     # 4x4 tiles of 512, every tile compressed (diagonals included), accuracy 1e-8 relative.
     "tlr_gemm_n2048_nb512": dict(n=2048, nb=512, d=2, ell=0.1, seed_ab=1, seed_c=2,
                                  accuracy=1e-8, dense_diagonal=False),
+    # 8x8 tiles of 512, dense diagonal tiles: a profiling-size case (inputs above L2, < 1 GB on device).
+    "tlr_gemm_n4096_nb512": dict(n=4096, nb=512, d=2, ell=0.1, seed_ab=1, seed_c=2,
+                                 accuracy=1e-8, dense_diagonal=True),
     # 32x32 tiles of 512, dense diagonal tiles, accuracy 1e-8 relative: 32^3 tile updates.
     "tlr_gemm_n16384_nb512": dict(n=16384, nb=512, d=2, ell=0.1, seed_ab=1, seed_c=2,
                                   accuracy=1e-8, dense_diagonal=True),
