@@ -38,7 +38,7 @@ class Update(C.Structure):
 
 class Params(C.Structure):
     _fields_ = [("accuracy", C.c_double), ("truncated_svd", C.c_int), ("fixed_rank", C.c_int),
-                ("use_trmm", C.c_int), ("use_ungqr", C.c_int), ("op_type", C.c_int)]
+                ("use_trmm", C.c_int), ("use_ungqr", C.c_int), ("op_type", C.c_int), ("mode", C.c_int)]
 
 
 class UpdateInfo(C.Structure):
@@ -155,5 +155,10 @@ class Context:
             pass
 
 
-def make_params(accuracy=1e-4, truncated_svd=False, fixed_rank=0, use_trmm=False, use_ungqr=True, op_type=1):
-    return Params(float(accuracy), int(truncated_svd), int(fixed_rank), int(use_trmm), int(use_ungqr), int(op_type))
+PLAIN_FP64, MIXED = 0, 1
+
+
+def make_params(accuracy=1e-4, truncated_svd=False, fixed_rank=0, use_trmm=False, use_ungqr=True, op_type=1,
+                mode=PLAIN_FP64):
+    return Params(float(accuracy), int(truncated_svd), int(fixed_rank), int(use_trmm), int(use_ungqr), int(op_type),
+                  int(mode))

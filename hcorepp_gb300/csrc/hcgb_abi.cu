@@ -156,6 +156,7 @@ Params to_params(const hcgb_params *p) {
     q.truncated = p ? p->truncated_svd : 0;
     q.fixed_rank = p ? p->fixed_rank : 0;
     q.side_mode = 1;
+    q.mode = p ? p->mode : 0;
     return q;
 }
 

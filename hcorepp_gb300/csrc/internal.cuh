@@ -94,7 +94,7 @@ struct Workspace {
     int kmax;             // max columns of a stack
     int rmax;             // max rank of an A/B factor
     size_t off_ustack, off_vstack, off_tmp1, off_tmp2, off_tauu, off_tauv, off_tu, off_tv;
-    size_t off_m, off_mcopy, off_xv, off_sigma;
+    size_t off_m, off_mcopy, off_xv, off_sigma, off_mixed;
 
     __host__ __device__ double *slot(int s) const { return base + slot_doubles * (size_t) s; }
 };
@@ -108,6 +108,7 @@ struct Params {
     int truncated;
     int fixed_rank;
     int side_mode;   // 0: always the reference's [Cu | alpha Au]; 1: pick the smaller stack
+    int mode;        // 0: plain FP64; 1: mixed (single-precision Jacobi preconditioning of the core)
 };
 
 // ---- launchers (stream-ordered, asynchronous) ----

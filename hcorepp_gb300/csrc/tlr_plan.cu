@@ -371,6 +371,7 @@ Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch) {
     w.off_mcopy = off;  off += round((size_t) kmax * kmax);
     w.off_xv = off;     off += round((size_t) ld * kmax);
     w.off_sigma = off;  off += round(kmax);
+    w.off_mixed = off;  off += round(((size_t) kmax * (size_t) (kmax + ld) + 1) / 2);  // float X32 + J32
     w.slot_doubles = off;
     return w;
 }

@@ -31,26 +31,43 @@ __device__ __forceinline__ void jacobi_pair(int t, int pp, int n2, int &i, int &
     }
 }
 
-__device__ __forceinline__ double group_sum(double v, int G) {
+template <typename T>
+__device__ __forceinline__ T group_sum(T v, int G) {
     for (int o = G >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-// One sweep of one-sided Jacobi over the kV columns (length rows) of X (ld ldx), with G lanes
-// per column pair (32/G pairs per warp at a time) and RPL rows per lane held in registers.
-//
-// A pair (x, y) is rotated when |x^T y| > tol * |x| |y| and both columns are above the numerical
-// noise floor `tiny` (squared norm); columns below it carry only rounding errors of the larger
-// ones, sit far below any truncation threshold, and rotating them never settles.
-// The rotation: zeta = (|y|^2 - |x|^2) / (2 x^T y), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2))
-// (tangent of the smaller angle, Rutishauser's formula), cs = 1/sqrt(1 + t^2), sn = cs t.
-// t only needs to be accurate to single precision for the pair to come out orthogonal to
-// ~1e-7 of its coupling; cs and sn are then formed in double precision from that t, so the
-// rotation itself is orthogonal to working precision.
-template <int G, int RPL>
-__device__ int jacobi_sweep(double *X, int ldx, int rows, int kV, double tol2, double tiny, int n2) {
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+
+// Tangent of the Jacobi angle that orthogonalises a pair with squared norms a, b and inner
+// product c: zeta = (b - a) / (2 c), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)) (Rutishauser).
+// Evaluated in single precision after scaling both terms by the same power of two (read off the
+// exponent of c with integer operations), so no double-precision divide or square root is spent
+// on it; the rotation built from t is orthogonal to working precision whatever t's rounding.
+__device__ __forceinline__ float jacobi_tangent(double a, double b, double c) {
+    const int hi = __double2hiint(c);
+    const int e = ((hi >> 20) & 0x7ff) - 1023;
+    const int se = e < -1000 ? -1000 : (e > 1000 ? 1000 : e);
+    const double scale = __hiloint2double((1023 - se) << 20, 0);  // 2^-se, exact
+    const float num = (float) ((b - a) * scale);
+    const float den = (float) (2.0 * c * scale);
+    const float zf = num / den;
+    if (fabsf(zf) > 1.0e18f) return 0.5f / zf;
+    return copysignf(1.0f, zf) / (fabsf(zf) + sqrtf(fmaf(zf, zf, 1.0f)));
+}
+
+// One sweep of one-sided Jacobi over the `ncols` columns (length `rows`) of X (ld ldx), with G
+// lanes per column pair (32/G pairs per warp at a time) and up to RPL rows per lane in registers.
+// Squared column norms are tracked in nrm[] (a' = a - t c, b' = b + t c), so each pair costs one
+// inner product.  A pair is rotated when c^2 > tol2 a b and both columns are above the noise
+// floor `tiny`; columns below it hold only rounding errors of the larger ones.
+// With ACC the same rotations are accumulated into the columns of J (ncols x ncols, ld ldj).
+template <typename T, int G, int RPL, bool ACC>
+__device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, double tol2, double tiny, int n2,
+                            T *J, int ldj) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    constexpr int PPW = 32 / G;  // pairs per warp
+    constexpr int PPW = 32 / G;
     const int gl = lane % G, grp = lane / G;
     const int npairs = n2 / 2;
     const int nchunks = (npairs + PPW - 1) / PPW;
@@ -62,44 +79,56 @@ __device__ int jacobi_sweep(double *X, int ldx, int rows, int kV, double tol2, d
             bool act = pp < npairs;
             if (act) {
                 jacobi_pair(t, pp, n2, i, j);
-                act = i < kV && j < kV;
+                act = i < ncols && j < ncols;
             }
-            double *x = X + (size_t) (act ? i : 0) * ldx;
-            double *y = X + (size_t) (act ? j : 0) * ldx;
-            double xr[RPL], yr[RPL];
-            double a = 0.0, b = 0.0, c = 0.0;
+            T *x = X + (size_t) (act ? i : 0) * ldx;
+            T *y = X + (size_t) (act ? j : 0) * ldx;
+            T xr[RPL], yr[RPL];
+            T c = T(0);
 #pragma unroll
             for (int q = 0; q < RPL; q++) {
-                const int r = gl + G * q;
-                const bool ok = act && r < rows;
-                xr[q] = ok ? x[r] : 0.0;
-                yr[q] = ok ? y[r] : 0.0;
-                a = fma(xr[q], xr[q], a);
-                b = fma(yr[q], yr[q], b);
-                c = fma(xr[q], yr[q], c);
+                xr[q] = yr[q] = T(0);
+                if (G * q < rows) {  // uniform across the warp: whole row slots beyond `rows` are skipped
+                    const int r = gl + G * q;
+                    if (act && r < rows) {
+                        xr[q] = x[r];
+                        yr[q] = y[r];
+                    }
+                    c = fma(xr[q], yr[q], c);
+                }
             }
-            a = group_sum(a, G);
-            b = group_sum(b, G);
             c = group_sum(c, G);
-            const bool rot = act && a > tiny && b > tiny && c * c > tol2 * a * b;
+            const double a = act ? nrm[i] : 0.0, b = act ? nrm[j] : 0.0;
+            const double cd = (double) c;
+            const bool rot = act && a > tiny && b > tiny && cd * cd > tol2 * a * b;
             if (rot) {
-                const double zeta = (b - a) / (2.0 * c);
-                const float zf = (float) zeta;
-                float tf;
-                if (fabsf(zf) > 1.0e18f) tf = 0.5f / zf;
-                else tf = copysignf(1.0f, zf) / (fabsf(zf) + sqrtf(fmaf(zf, zf, 1.0f)));
-                const double tt = (double) tf;
-                const double cs = rsqrt(fma(tt, tt, 1.0));
-                const double sn = cs * tt;
+                const float tf = jacobi_tangent(a, b, cd);
+                const T tt = (T) tf;
+                const T cs = rsqrt_t(fma(tt, tt, T(1)));
+                const T sn = cs * tt;
 #pragma unroll
                 for (int q = 0; q < RPL; q++) {
-                    const int r = gl + G * q;
-                    if (r < rows) {
-                        x[r] = fma(cs, xr[q], -sn * yr[q]);
-                        y[r] = fma(sn, xr[q], cs * yr[q]);
+                    if (G * q < rows) {
+                        const int r = gl + G * q;
+                        if (r < rows) {
+                            x[r] = fma(cs, xr[q], -sn * yr[q]);
+                            y[r] = fma(sn, xr[q], cs * yr[q]);
+                        }
                     }
                 }
-                if (gl == 0) rotations++;
+                if (ACC) {
+                    T *ji = J + (size_t) i * ldj, *jj = J + (size_t) j * ldj;
+                    for (int r = gl; r < ncols; r += G) {
+                        const T u = ji[r], v = jj[r];
+                        ji[r] = fma(cs, u, -sn * v);
+                        jj[r] = fma(sn, u, cs * v);
+                    }
+                }
+                if (gl == 0) {
+                    nrm[i] = a - (double) tt * cd;
+                    nrm[j] = b + (double) tt * cd;
+                    rotations++;
+                }
             }
         }
         __syncthreads();
@@ -107,36 +136,39 @@ __device__ int jacobi_sweep(double *X, int ldx, int rows, int kV, double tol2, d
     return rotations;
 }
 
-// Full Jacobi iteration on X: sweeps until no pair rotates (or MAX_JACOBI_SWEEPS).
-template <int G, int RPL>
-__device__ void jacobi(double *X, int ldx, int rows, int kV, int *s_rot, double *s_amax, int *sweeps_out,
-                       bool *converged_out) {
+// Jacobi iteration on X: exact squared column norms at the start of every sweep, then sweeps
+// until no pair rotates (or max_sweeps).
+template <typename T, int G, int RPL, bool ACC>
+__device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax, int *sweeps_out,
+                       bool *converged_out, double tol, int max_sweeps, T *J = nullptr, int ldj = 0) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const double tol = DBL_EPSILON * sqrt((double) (rows > 1 ? rows : 1));
     const double tol2 = tol * tol;
-    const double noise = DBL_EPSILON * (double) (rows > 1 ? rows : 1);
-    const int n2 = kV + (kV & 1);
+    const double noise = (sizeof(T) == 8 ? DBL_EPSILON : FLT_EPSILON) * (double) (rows > 1 ? rows : 1);
+    const int n2 = ncols + (ncols & 1);
     int sweeps = 0;
-    bool converged = kV < 2;
-    while (!converged && sweeps < MAX_JACOBI_SWEEPS) {
-        // Largest squared column norm: the scale of the numerical noise floor.
+    bool converged = ncols < 2;
+    while (!converged && sweeps < max_sweeps) {
         if (threadIdx.x == 0) {
             *s_rot = 0;
             *s_amax = 0.0;
         }
         __syncthreads();
         double amax = 0.0;
-        for (int j = warp; j < kV; j += nw) {
-            const double *col = X + (size_t) j * ldx;
-            double s = 0.0;
-            for (int r = lane; r < rows; r += 32) s = fma(col[r], col[r], s);
-            s = warp_sum(s);
-            amax = fmax(amax, s);
+        for (int j = warp; j < ncols; j += nw) {
+            const T *col = X + (size_t) j * ldx;
+            double sq = 0.0;
+            for (int r = lane; r < rows; r += 32) {
+                const double v = (double) col[r];
+                sq = fma(v, v, sq);
+            }
+            sq = warp_sum(sq);
+            if (lane == 0) nrm[j] = sq;
+            amax = fmax(amax, sq);
         }
         if (lane == 0) atomicMax(reinterpret_cast<unsigned long long *>(s_amax), __double_as_longlong(amax));
         __syncthreads();
         const double tiny = *s_amax * noise * noise;
-        const int rot = jacobi_sweep<G, RPL>(X, ldx, rows, kV, tol2, tiny, n2);
+        const int rot = jacobi_sweep<T, G, RPL, ACC>(X, ldx, rows, ncols, nrm, tol2, tiny, n2, J, ldj);
         if (rot) atomicAdd(s_rot, rot);
         __syncthreads();
         sweeps++;
@@ -145,6 +177,17 @@ __device__ void jacobi(double *X, int ldx, int rows, int kV, int *s_rot, double 
     }
     *sweeps_out = sweeps;
     *converged_out = converged;
+}
+
+// Lane-group / register-tile choice for a column length: G lanes per pair, RPL rows per lane.
+template <typename T, bool ACC, int MAXRPL>
+__device__ void jacobi_dispatch(T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax,
+                                int *sweeps, bool *conv, double tol, int max_sweeps, T *J = nullptr, int ldj = 0) {
+    if (rows <= 32) jacobi<T, 8, 4, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
+    else if (rows <= 64) jacobi<T, 8, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
+    else if (rows <= 128) jacobi<T, 16, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
+    else if (rows <= 256 || MAXRPL <= 8) jacobi<T, 32, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
+    else jacobi<T, 32, MAXRPL, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
 }
 
 // Householder QR with column pivoting of A (mrows x ncols, ld lda) in place, stopped early once
@@ -376,10 +419,50 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     //    X J = W with orthogonal columns: sigma_i = ||w_i||, right singular vectors P W Sigma^-1.
     int sweeps = 0;
     bool converged = true;
-    if (kV <= 64) jacobi<8, 8>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
-    else if (kV <= 128) jacobi<16, 8>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
-    else if (kV <= 256 || RPL <= 8) jacobi<32, 8>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
-    else jacobi<32, RPL>(X, ldx, kV, rk, &s_rot, &s_amax, &sweeps, &converged);
+    const double tol64 = 8.0 * DBL_EPSILON * (double) (kV > 1 ? kV : 1);
+    if (p.mode == 1) {
+        // Mixed form: single-precision sweeps on a copy of X accumulate the rotations J32, then
+        // X <- X J32 on DMMA and double-precision sweeps finish (J32 is orthogonal to ~1e-6, so
+        // X J32 keeps the singular values to that relative accuracy and its columns start nearly
+        // orthogonal: typically one or two double-precision sweeps remain).
+        float *X32 = reinterpret_cast<float *>(base + ws.off_mixed);
+        float *J32 = X32 + (size_t) kV * rk;
+        for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) X32[e] = (float) X[(e % kV) + (size_t) (e / kV) * ldx];
+        for (int e = threadIdx.x; e < rk * rk; e += blockDim.x) J32[e] = (e % rk) == (e / rk) ? 1.0f : 0.0f;
+        __syncthreads();
+        int sw32 = 0;
+        bool conv32 = true;
+        jacobi_dispatch<float, true, RPL>(X32, kV, kV, rk, nrm, &s_rot, &s_amax, &sw32, &conv32,
+                                          4.0 * FLT_EPSILON * sqrt((double) kV), MAX_JACOBI_SWEEPS, J32, rk);
+        // W = X J32 (kV x rk) on DMMA into XV, then back into X.
+        {
+            const int ntr = (kV + 7) >> 3, ntc = (rk + 7) >> 3;
+            for (int idx = warp; idx < ntr * ntc; idx += nw) {
+                const int tr = idx % ntr, tc = idx / ntr;
+                const int irow = tr * 8 + lr, icol = tc * 8 + lr;
+                double d0 = 0.0, d1 = 0.0;
+                for (int l4 = 0; l4 < rk; l4 += 4) {
+                    const int l = l4 + lc;
+                    const double av = (irow < kV && l < rk) ? X[irow + (size_t) l * ldx] : 0.0;
+                    const double bv = (icol < rk && l < rk) ? (double) J32[l + (size_t) icol * rk] : 0.0;
+                    dmma(d0, d1, av, bv);
+                }
+                const int col = tc * 8 + 2 * lc;
+                if (irow < kV && col < rk) XV[irow + (size_t) col * ld] = d0;
+                if (irow < kV && col + 1 < rk) XV[irow + (size_t) (col + 1) * ld] = d1;
+            }
+            __syncthreads();
+            for (int i = warp; i < rk; i += nw)
+                for (int l = lane; l < kV; l += 32) X[l + (size_t) i * ldx] = XV[l + (size_t) i * ld];
+            __syncthreads();
+        }
+        jacobi_dispatch<double, false, RPL>(X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
+                                            MAX_JACOBI_SWEEPS);
+        sweeps += 100 * sw32;  // record: single-precision sweeps in the hundreds
+    } else {
+        jacobi_dispatch<double, false, RPL>(X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
+                                            MAX_JACOBI_SWEEPS);
+    }
 
     const long long t3 = clock64();
     // 5. Singular values, descending order (stable), rank rule (omp/kernels.cpp:82-104).

@@ -59,7 +59,15 @@ typedef struct {
     int use_trmm;
     int use_ungqr;
     int op_type;        /* hcgb_svd_type */
+    int mode;           /* hcgb_mode: arithmetic of the recompression core */
 } hcgb_params;
+
+/* HCGB_PLAIN_FP64: every stage in double precision.
+ * HCGB_MIXED: the core SVD's Jacobi is preconditioned by single-precision sweeps (rotations
+ * accumulated in single precision, applied once in double precision, then finished in double
+ * precision); QR, products, Q application and the truncation test stay in double precision.
+ * Singular values agree with the plain form to ~1e-6 relative; the product to working accuracy. */
+typedef enum { HCGB_PLAIN_FP64 = 0, HCGB_MIXED = 1 } hcgb_mode;
 
 /* One tile update C <- alpha * A * B + beta * C (NoTrans operands). */
 typedef struct {

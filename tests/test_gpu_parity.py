@@ -242,3 +242,22 @@ def test_tlr_multiply_concurrency_invariant(T):
     for arena, ranks in outs[1:]:
         np.testing.assert_array_equal(ranks, outs[0][1])
         np.testing.assert_array_equal(arena, outs[0][0])
+
+
+@pytest.mark.parametrize("combo", ["CCC", "DCC", "CDC"])
+def test_mixed_mode_vs_oracle(T, combo):
+    """HCGB_MIXED (single-precision Jacobi preconditioning of the core): same ranks (+-1) and
+    product accuracy as the plain FP64 form."""
+    from hcorepp_gb300 import _lib as L
+    from hcorepp_gb300.problems import KernelMatrix
+    acc, nb = 1e-8, 256
+    km = KernelMatrix(4 * nb, nb, 2, 0.1, 1)
+    kc = KernelMatrix(4 * nb, nb, 2, 0.1, 2)
+    da, db, dc = km.tile(0, 1), km.tile(1, 2), kc.tile(0, 2)
+    oa, ob, oc = _make(combo[0], da, acc), _make(combo[1], db, acc), _make(combo[2], dc, acc)
+    ga, gb, gc = _gpu_tile(T, oa), _gpu_tile(T, ob), _gpu_tile(T, oc)
+    exact = oa.to_dense() @ ob.to_dense() + oc.to_dense()
+    O.hcore_gemm(1.0, oa, ob, 1.0, oc, O.CompressionParameters(acc, truncated_svd=True))
+    T.HCore.Gemm(1.0, ga, 0, gb, 0, 1.0, gc, T.CompressionParameters(acc, truncated_svd=True, mode=L.MIXED))
+    assert abs(gc.rank - oc.rank) <= 1
+    assert rel_fro(gc.to_dense(), exact) <= 2 * max(rel_fro(oc.to_dense(), exact), acc)
