@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the dense FP64 accuracy check")
     ap.add_argument("--groups", type=int, default=8, help="independent C-tile groups (streams)")
+    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"],
+                    help="plain: FP64 throughout; mixed: single-precision Jacobi preconditioning of the core")
     return ap.parse_args()
 
 
@@ -249,7 +251,8 @@ def gpu_arm(args, rank, world, local):
     C0.arena.copy_(torch.from_numpy(c_host))
     C0.ranks.copy_(torch.from_numpy(c_ranks))
     Cw = T.TileMatrix(nt, nt, nb, C0.kinds, maxr)
-    params = T.CompressionParameters(w["accuracy"], truncated_svd=True)
+    params = T.CompressionParameters(w["accuracy"], truncated_svd=True,
+                                     mode=L.MIXED if args.mode == "mixed" else L.PLAIN_FP64)
     info = T.info_buffer(n_updates)
     dmma_peak, dfma_peak = ctx.fp64_peak()
     ctx.set_concurrency(args.groups)
@@ -392,7 +395,8 @@ def gpu_arm(args, rank, world, local):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (Morton-sorted exponential kernel, seeded)",
         "config": {"workload": args.workload, "n": w["n"], "nb": w["nb"], "tiles": f"{nt}x{nt}",
                    "updates_per_step": n_updates, "accuracy": w["accuracy"], "threshold": "relative",
-                   "dense_diagonal": w["dense_diagonal"], "max_rank": maxr, "form": "plain_fp64",
+                   "dense_diagonal": w["dense_diagonal"], "max_rank": maxr,
+                   "form": "plain_fp64" if args.mode == "plain" else "mixed (fp32-preconditioned core Jacobi)",
                    "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups,
                    "l2": "inputs larger than L2 (A, C arenas 1.4 GB each), no flush"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

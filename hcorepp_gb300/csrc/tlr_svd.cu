@@ -143,7 +143,9 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
                        bool *converged_out, double tol, int max_sweeps, T *J = nullptr, int ldj = 0) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const double tol2 = tol * tol;
-    const double noise = (sizeof(T) == 8 ? DBL_EPSILON : FLT_EPSILON) * (double) (rows > 1 ? rows : 1);
+    // Noise floor from double precision also for single-precision sweeps: X is graded (each column
+    // accurate relative to its own norm), so small columns are data, not rounding noise.
+    const double noise = DBL_EPSILON * (double) (rows > 1 ? rows : 1);
     const int n2 = ncols + (ncols & 1);
     int sweeps = 0;
     bool converged = ncols < 2;
@@ -197,14 +199,14 @@ __device__ void jacobi_dispatch(T *X, int ldx, int rows, int ncols, double *nrm,
 // the first pivot.  Column norms are recomputed exactly while each column is updated, so no
 // norm downdating is needed.  Returns the number of rows of R that were computed.
 __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double stop2, double rel, double *nrm,
-                              int *pvt, double *red, int *redi) {
+                              double *nref, int *pvt, double *red, int *redi) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int j = warp; j < ncols; j += nw) {
         const double *col = A + (size_t) j * lda;
         double t = 0.0;
         for (int i = lane; i < mrows; i += 32) t = fma(col[i], col[i], t);
         t = warp_sum(t);
-        if (lane == 0) nrm[j] = t;
+        if (lane == 0) nrm[j] = nref[j] = t;
     }
     for (int j = threadIdx.x; j < ncols; j += blockDim.x) pvt[j] = j;
     __syncthreads();
@@ -264,6 +266,9 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
                 const double t = nrm[s];
                 nrm[s] = nrm[bi];
                 nrm[bi] = t;
+                const double tr = nref[s];
+                nref[s] = nref[bi];
+                nref[bi] = tr;
                 const int ti = pvt[s];
                 pvt[s] = pvt[bi];
                 pvt[bi] = ti;
@@ -296,7 +301,8 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
         const double tau = red[40], scale = red[41];
         for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) x[i] *= scale;
         __syncthreads();
-        // Apply H to the remaining columns; recompute their norms below row s exactly.
+        // Apply H to the remaining columns; downdate their squared norms below row s
+        // (nrm -= y_s^2) and recompute exactly when the downdate cancels (LAPACK dlaqp2's guard).
         for (int j = s + 1 + warp; j < ncols; j += nw) {
             double *y = A + (size_t) j * lda;
             double w = 0.0;
@@ -304,16 +310,23 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
                 w = lane == 0 ? y[s] : 0.0;
                 for (int i = s + 1 + lane; i < mrows; i += 32) w = fma(x[i], y[i], w);
                 w = warp_sum(w) * tau;
+                for (int i = s + 1 + lane; i < mrows; i += 32) y[i] = fma(-w, x[i], y[i]);
             }
-            if (lane == 0) y[s] -= w;
-            double nn = 0.0;
-            for (int i = s + 1 + lane; i < mrows; i += 32) {
-                const double a = fma(-w, x[i], y[i]);
-                y[i] = a;
-                nn = fma(a, a, nn);
+            const double ys = y[s] - w;  // all lanes read the old y[s] before lane 0 writes it
+            __syncwarp();
+            if (lane == 0) y[s] = ys;
+            double nn = nrm[j] - ys * ys;
+            const bool exact = !(nn > 1e-8 * nref[j]);  // lost 4+ digits of the norm since the last exact value
+            if (exact) {
+                nn = 0.0;
+                for (int i = s + 1 + lane; i < mrows; i += 32) nn = fma(y[i], y[i], nn);
+                nn = warp_sum(nn);
             }
-            nn = warp_sum(nn);
-            if (lane == 0) nrm[j] = nn;
+            __syncwarp();
+            if (lane == 0) {
+                nrm[j] = nn;
+                if (exact) nref[j] = nn;
+            }
         }
         __syncthreads();
     }
@@ -401,7 +414,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         }
     }
     const long long t1 = clock64();
-    int rk = qrcp_truncated(Mw, ldw, kU, kV, stop2, rel, nrm, pvt, red, redi);
+    int rk = qrcp_truncated(Mw, ldw, kU, kV, stop2, rel, nrm, inv, pvt, red, redi);
     const long long t2 = clock64();
     if (rk < 1) rk = 1;
     double *XV = base + ws.off_xv;
