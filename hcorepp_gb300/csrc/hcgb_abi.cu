@@ -147,7 +147,7 @@ BatchShape shape_of(const hcgb_update *ups, int n) {
 }
 
 size_t workspace_bytes_for(const Workspace &w, int n) {
-    return sizeof(double) * w.slot_doubles * (size_t) n + sizeof(int) * META_INTS * (size_t) n + 256;
+    return sizeof(double) * w.slot_doubles * (size_t) n + sizeof(int) * (META_INTS + 1) * (size_t) n + 256;
 }
 
 Params to_params(const hcgb_params *p) {
@@ -200,6 +200,7 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
             cnt[HCGB_STAGE_GEMM]++;
         }
     mark(HCGB_STAGE_QR);
+    if (sh.any_compressed_c && ws.order && n > 1) launch_order(n, ws, st);
     if (sh.any_compressed_c) {
         launch_qr(ws, n, st);
         cnt[HCGB_STAGE_QR]++;
@@ -228,6 +229,7 @@ int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, 
     if (rc) return rc;
     w.base = static_cast<double *>(ctx->ws);
     w.meta = reinterpret_cast<int *>(static_cast<char *>(ctx->ws) + sizeof(double) * w.slot_doubles * (size_t) n);
+    w.order = w.meta + (size_t) META_INTS * n;
     *out = w;
     return HCGB_OK;
 }
@@ -410,6 +412,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         Workspace wg = ws;
         wg.base = ws.base + ws.slot_doubles * (size_t) first[g];
         wg.meta = ws.meta + (size_t) META_INTS * first[g];
+        wg.order = ws.order + first[g];
         for (int kk = 0; kk < kt; kk++) {
             const size_t off = (size_t) first[g] * kt + (size_t) kk * ng;
             BatchShape shw = shape_of(all.data() + off, ng);

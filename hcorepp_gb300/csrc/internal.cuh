@@ -89,6 +89,7 @@ enum MetaField {
 struct Workspace {
     double *base;
     int *meta;            // n * META_INTS
+    int *order;           // optional (n ints): heavy-stage CTA b works on update order[b]
     size_t slot_doubles;
     int ld;               // leading dimension of every stack / temporary (>= rows, cols)
     int kmax;             // max columns of a stack
@@ -97,6 +98,9 @@ struct Workspace {
     size_t off_m, off_mcopy, off_xv, off_sigma, off_mixed;
 
     __host__ __device__ double *slot(int s) const { return base + slot_doubles * (size_t) s; }
+    // Update processed by CTA `b` of the QR / core / Q-application launches: largest first, so the
+    // long updates of a launch start at once instead of after the short ones.
+    __device__ int heavy(int b) const { return order ? order[b] : b; }
 };
 
 // Layout of one workspace slot for stacks of up to `ld` rows and `kmax` columns; factor ranks
@@ -115,6 +119,8 @@ struct Params {
 void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p, GemmJob *jobs,
                  cudaStream_t st);
 void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, cudaStream_t st);
+// ws.order <- updates sorted by decreasing stack width k (ties by index); needs ws.order != nullptr.
+void launch_order(int n, Workspace ws, cudaStream_t st);
 void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st);
 void launch_qr(Workspace ws, int n, cudaStream_t st);
 void launch_core_svd(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st);

@@ -88,6 +88,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     if (ck) kmax = rc + (ak && bk ? rmax : (bk ? rb : ra));
     if (kmax < 8) kmax = 8;
     Workspace ws = make_workspace_layout(ld, kmax, rmax, false);
+    ws.order = nullptr;  // a single update: no ordering
     const size_t slot_bytes = round_up_bytes(sizeof(double) * ws.slot_doubles);
     const size_t meta_bytes = round_up_bytes(sizeof(int) * META_INTS);
     const size_t desc_bytes = round_up_bytes(sizeof(DevUpdate));

@@ -315,6 +315,20 @@ __global__ void __launch_bounds__(256) ddc_finalize_kernel(const DevUpdate *ups,
     if (threadIdx.x == 0) *u.c.rank = r;
 }
 
+__global__ void __launch_bounds__(1024) order_kernel(int n, Workspace ws) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int *mi = ws.meta + (size_t) i * META_INTS;
+        const int ki = (mi[META_STATUS] == HCGB_OK && mi[META_CKIND]) ? mi[META_K] : 0;
+        int pos = 0;
+        for (int j = 0; j < n; j++) {
+            const int *mj = ws.meta + (size_t) j * META_INTS;
+            const int kj = (mj[META_STATUS] == HCGB_OK && mj[META_CKIND]) ? mj[META_K] : 0;
+            pos += (kj > ki) || (kj == ki && j < i);
+        }
+        ws.order[pos] = i;
+    }
+}
+
 __global__ void __launch_bounds__(256) transpose_kernel(const double *src, int lds, int rows, int cols, double *dst,
                                                       int ldd) {
     __shared__ double tile[32][33];
@@ -330,6 +344,10 @@ void launch_transpose(const double *src, int lds, int rows, int cols, double *ds
 void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p, GemmJob *jobs,
                  cudaStream_t st) {
     plan_kernel<<<(n + 127) / 128, 128, 0, st>>>(ups, n, alpha, beta, ws, p, jobs);
+}
+
+void launch_order(int n, Workspace ws, cudaStream_t st) {
+    order_kernel<<<1, 1024, 0, st>>>(n, ws);
 }
 
 void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, cudaStream_t st) {

@@ -224,7 +224,7 @@ __device__ QrShared carve(double *sm, int ld, int kmax) {
 // grid = 2 * n: block 2s factors the U stack of update s, block 2s+1 its V stack.
 __global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws) {
     extern __shared__ double sm[];
-    const int slot = blockIdx.x >> 1, side = blockIdx.x & 1;
+    const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
     const int *meta = ws.meta + (size_t) slot * META_INTS;
     if (meta[META_STATUS] != HCGB_OK || !meta[META_CKIND]) return;
     const int k = meta[META_K];
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws) {
 // grid = 2 * n: X <- Q X for the U side (X = the C tile's U, m x r) and the V side (X = XV, n x r).
 __global__ void __launch_bounds__(QR_THREADS) apply_q_kernel(const DevUpdate *ups, Workspace ws) {
     extern __shared__ double sm[];
-    const int slot = blockIdx.x >> 1, side = blockIdx.x & 1;
+    const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
     const int *meta = ws.meta + (size_t) slot * META_INTS;
     const int st = meta[META_STATUS];
     if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;

@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     extern __shared__ double sm[];
     __shared__ int s_rot, s_rank;
     __shared__ double s_amax;
-    const int slot = blockIdx.x;
+    const int slot = ws.heavy(blockIdx.x);
     int *meta = ws.meta + (size_t) slot * META_INTS;
     if (meta[META_STATUS] != HCGB_OK || !meta[META_CKIND]) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
