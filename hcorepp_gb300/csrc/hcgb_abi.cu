@@ -200,7 +200,9 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
             cnt[HCGB_STAGE_GEMM]++;
         }
     mark(HCGB_STAGE_QR);
-    if (sh.any_compressed_c && ws.order && n > 1) launch_order(n, ws, st);
+    // The heavy stages index updates through ws.order: it must be written for every launch
+    // that carries it (a single update included).
+    if (sh.any_compressed_c && ws.order) launch_order(n, ws, st);
     if (sh.any_compressed_c) {
         launch_qr(ws, n, st);
         cnt[HCGB_STAGE_QR]++;
