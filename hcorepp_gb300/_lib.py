@@ -86,6 +86,8 @@ def lib():
         L.hcgb_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong), ip]
         L.hcgb_fp64_peak.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.hcgb_set_concurrency.argtypes = [vp, ip]
+        L.hcgb_compress_tile.argtypes = [vp, vp, ip, ip, C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int)]
+        L.hcgb_compress_tile.restype = C.c_int
         L.hcgb_tile_gemm_noalloc.argtypes = [C.c_double, C.POINTER(Tile), C.POINTER(Tile), C.c_double,
                                              C.POINTER(Tile), C.POINTER(Params), vp, vp]
         L.hcgb_tile_gemm_noalloc.restype = C.c_int

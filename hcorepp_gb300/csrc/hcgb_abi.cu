@@ -659,3 +659,42 @@ extern "C" int hcgb_fp64_peak(hcgb_context *ctx, double *dmma_tflops, double *df
     if (rc) return fail(ctx, rc, "hcgb_fp64_peak: probe failed");
     return HCGB_OK;
 }
+
+namespace {
+
+__global__ void identity_kernel(double *a, int n, int ld) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x)
+        a[(e % n) + (size_t) (e / n) * ld] = (e % n) == (e / n) ? 1.0 : 0.0;
+}
+
+}  // namespace
+
+extern "C" int hcgb_compress_tile(hcgb_context *ctx, const double *dense, int rows, int cols, hcgb_tile *out,
+                                  const hcgb_params *params, int *rank) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (!dense || !out || rows <= 0 || cols <= 0 || out->kind != HCGB_COMPRESSED || out->rows != rows ||
+        out->cols != cols || !out->rank || out->max_rank <= 0)
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_compress_tile: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    // D = D * I: an update with A = the dense tile, B = I (compressed, U = V = I_cols), C = 0 (rank 0)
+    // recompresses exactly the columns of D, i.e. computes its truncated SVD.
+    double *ibuf = nullptr;
+    int *irank = nullptr;
+    const size_t n = (size_t) cols;
+    HCGB_CUDA(ctx, cudaMalloc(&ibuf, sizeof(double) * 2 * n * n));
+    HCGB_CUDA(ctx, cudaMalloc(&irank, sizeof(int)));
+    identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf, cols, cols);
+    identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf + n * n, cols, cols);
+    const int ncols = cols;
+    HCGB_CUDA(ctx, cudaMemcpyAsync(irank, &ncols, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    HCGB_CUDA(ctx, cudaMemsetAsync(out->rank, 0, sizeof(int), ctx->stream));
+    hcgb_tile a{const_cast<double *>(dense), nullptr, rows, cols, 0, HCGB_DENSE};
+    hcgb_tile b{ibuf, irank, cols, cols, cols, HCGB_COMPRESSED};
+    int r = 0;
+    int rc = hcgb_tile_gemm(ctx, 1.0, &a, HCGB_NOTRANS, &b, HCGB_NOTRANS, 0.0, out, params, &r, nullptr);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ibuf);
+    cudaFree(irank);
+    if (rank) *rank = r;
+    return rc;
+}

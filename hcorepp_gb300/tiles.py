@@ -103,6 +103,24 @@ class CompressedTile:
         if u is not None:
             self.set_factors(u, v)
 
+    @classmethod
+    def from_dense(cls, dense, params: "CompressionParameters", max_rank: int | None = None, device="cuda"):
+        """CompressedTile(rows, cols, data, ld, params, ...) (Compressed.cpp:75-146) on the GPU:
+        truncated SVD of the dense tile, rank clamped to max(min(rows, cols)/3, 1) unless
+        max_rank is given."""
+        d = torch.as_tensor(np.asfortranarray(np.asarray(dense, dtype=np.float64)).ravel(order="F"))
+        rows, cols = np.asarray(dense).shape
+        cap = max(min(rows, cols) // MAX_RANK_RATIO, 1) if max_rank is None else max_rank
+        t = cls(rows, cols, rank=0, max_rank=cap, device=device)
+        dd = d.to(device)
+        ctx = run_context()
+        p = params.c()
+        r = C.c_int(0)
+        tc = t.c_tile()
+        ctx.check(L.lib().hcgb_compress_tile(ctx.handle, C.c_void_p(dd.data_ptr()), rows, cols, C.byref(tc),
+                                             C.byref(p), C.byref(r)), allow=(L.HCGB_OK, L.HCGB_NOT_CONVERGED))
+        return t
+
     def set_factors(self, u, v):
         u = np.asarray(u, dtype=np.float64)
         v = np.asarray(v, dtype=np.float64)

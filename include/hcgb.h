@@ -148,6 +148,15 @@ int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *a, int op_a
                    double beta, hcgb_tile *c, const hcgb_params *params, int *new_rank,
                    unsigned long long *flops);
 
+/* Dense -> compressed tile construction, the GPU form of CompressedTile(rows, cols, data, ld, params,
+ * ...) (src/operators/concrete/Compressed.cpp:75-146): truncated SVD of the dense tile `dense`
+ * (device, rows x cols, ld rows) by the same QR + core-SVD route as a tile update, rank by the
+ * params' rule clamped to [1, out->max_rank].  `out` is a compressed tile of the same shape whose
+ * buffer and device rank the call fills (the reference clamps at max(min(rows, cols)/3, 1)).
+ * Synchronous; *rank (if not NULL) receives the rank. */
+int hcgb_compress_tile(hcgb_context *ctx, const double *dense, int rows, int cols, hcgb_tile *out,
+                       const hcgb_params *params, int *rank);
+
 /* Stage timing with CUDA events on the context stream (the GB300 replacement of the reference's
  * DebuggingTimer snapshots, src/helpers/debugging-timer/ActiveTimer.cpp:47-60).  While enabled,
  * every pipeline stage is bracketed by events; hcgb_profile_read synchronises the stream and

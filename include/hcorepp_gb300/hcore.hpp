@@ -1,0 +1,332 @@
+// hcorepp_gb300/hcore.hpp -- C++ mirror of HCore++'s TLR-GEMM API over the C ABI (hcgb.h).
+//
+// Same class names, namespaces, constructor arguments and call signatures as the reference for
+// the tile-GEMM path, so code written against HCore++'s CUDA build recompiles against this header:
+//   hcorepp::operators::CompressionParameters  include/hcorepp/operators/helpers/CompressionParameters.hpp:44-127
+//   hcorepp::operators::Tile / DenseTile / CompressedTile
+//                                              include/hcorepp/operators/interface/Tile.hpp:54-294,
+//                                              include/hcorepp/operators/concrete/{Dense,Compressed}.hpp
+//   hcorepp::kernels::RunContext               include/hcorepp/kernels/cuda/RunContext.hpp:15-53
+//   hcorepp::dataunits::MemoryUnit             include/hcorepp/data-units/memory-handlers/pool/MemoryHandler.hpp:22-157
+//   hcorepp::api::HCore<T>::Gemm               include/hcorepp/api/HCore.hpp:41-63
+// Tile buffers live on the device (as in the reference's CUDA build); constructors accept host or
+// device pointers (cudaMemcpyDefault).  Errors throw std::runtime_error / std::invalid_argument as
+// the reference does.  The GPU path computes in double precision: T = double.
+#ifndef HCOREPP_GB300_HCORE_HPP
+#define HCOREPP_GB300_HCORE_HPP
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "hcgb.h"
+
+#ifdef HCGB_HAVE_BLASPP
+#include <blas.hh>
+#else
+namespace blas {
+enum class Layout : char { ColMajor = 'C', RowMajor = 'R' };
+enum class Op : char { NoTrans = 'N', Trans = 'T', ConjTrans = 'C' };
+}  // namespace blas
+#endif
+
+namespace hcorepp {
+
+namespace common {
+enum CompressionType { LAPACK_GESVD, LAPACK_GESDD };  // Definitions.hpp CompressionType
+}
+
+namespace detail {
+inline void check(int rc, hcgb_context *ctx, const char *what) {
+    if (rc == HCGB_OK || rc == HCGB_NOT_CONVERGED) return;
+    std::string msg = std::string(what) + ": " + (ctx ? hcgb_last_error(ctx) : "") + " (status " +
+                      std::to_string(rc) + ")";
+    if (rc == HCGB_BAD_ARG) throw std::invalid_argument(msg);
+    throw std::runtime_error(msg);
+}
+inline void cuda(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+}  // namespace detail
+
+namespace kernels {
+// One device + stream + library workspace (the CUDA RunContext's GetStream / Sync role).
+class RunContext {
+public:
+    explicit RunContext(int device = 0, cudaStream_t stream = nullptr) {
+        hcgb_context *c = nullptr;
+        detail::check(hcgb_context_create(device, stream, &c), nullptr, "hcgb_context_create");
+        mCtx = std::shared_ptr<hcgb_context>(c, [](hcgb_context *p) { hcgb_context_destroy(p); });
+        mStream = stream;
+    }
+    cudaStream_t GetStream() const { return mStream; }
+    void Sync() const { detail::check(hcgb_sync(mCtx.get()), mCtx.get(), "hcgb_sync"); }
+    RunContext ForkChildContext() { return RunContext(*this); }
+    bool SupportsOMP() const { return false; }
+    hcgb_context *handle() const { return mCtx.get(); }
+
+private:
+    std::shared_ptr<hcgb_context> mCtx;
+    cudaStream_t mStream;
+};
+}  // namespace kernels
+
+namespace dataunits {
+// The library sizes and owns its scratch per context; the unit keeps the reference's interface.
+template <typename T>
+class MemoryUnit {
+public:
+    explicit MemoryUnit(const kernels::RunContext &ctx) : mCtx(&ctx) {}
+    MemoryUnit() = default;
+    bool IsInitialized() const { return true; }
+    void Initialize(size_t) {}
+    void Reset() {}
+    void FreeAllocations() {}
+
+private:
+    const kernels::RunContext *mCtx = nullptr;
+};
+}  // namespace dataunits
+
+namespace operators {
+
+class CompressionParameters {
+public:
+    CompressionParameters(double aAccuracy = 1e-4, bool aUseTrmm = false, bool aUseUngqr = true,
+                          bool aTruncatedSvd = false, size_t aFixedRank = 0,
+                          common::CompressionType aOpType = common::LAPACK_GESDD)
+        : mUseTrmm(aUseTrmm), mUseUngqr(aUseUngqr), mTruncatedSvd(aTruncatedSvd), mFixedRank(aFixedRank),
+          mOpType(aOpType), mAccuracy(aAccuracy) {}
+    bool GetTrmm() const { return mUseTrmm; }
+    bool GetUngqr() const { return mUseUngqr; }
+    bool GetTruncatedSvd() const { return mTruncatedSvd; }
+    size_t GetFixedRank() const { return mFixedRank; }
+    common::CompressionType GetOperationType() const { return mOpType; }
+    double GetAccuracy() const { return mAccuracy; }
+    // GB300 addition: arithmetic of the recompression core (HCGB_PLAIN_FP64 or HCGB_MIXED).
+    void SetMode(int aMode) { mMode = aMode; }
+    hcgb_params c_params() const {
+        return hcgb_params{mAccuracy, mTruncatedSvd ? 1 : 0, (int) mFixedRank, mUseTrmm ? 1 : 0,
+                           mUseUngqr ? 1 : 0, mOpType == common::LAPACK_GESVD ? HCGB_GESVD : HCGB_GESDD, mMode};
+    }
+
+private:
+    bool mUseTrmm, mUseUngqr, mTruncatedSvd;
+    size_t mFixedRank;
+    common::CompressionType mOpType;
+    double mAccuracy;
+    int mMode = HCGB_PLAIN_FP64;
+};
+
+template <typename T>
+class Tile {
+public:
+    static_assert(sizeof(T) == 8, "the GB300 TLR path computes in double precision");
+    virtual ~Tile() = default;
+    size_t GetNumOfRows() const { return mRows; }
+    size_t GetNumOfCols() const { return mCols; }
+    blas::Layout GetLayout() const { return blas::Layout::ColMajor; }
+    virtual int GetNumOfSubMatrices() const = 0;
+    virtual size_t GetTileRank() const = 0;
+    virtual hcgb_tile c_tile() const = 0;
+    bool isDense() const { return GetNumOfSubMatrices() == 1; }
+    bool isCompressed() const { return GetNumOfSubMatrices() == 2; }
+
+protected:
+    size_t mRows = 0, mCols = 0;
+};
+
+template <typename T>
+class DenseTile : public Tile<T> {
+public:
+    // DenseTile(rows, cols, data, ld, layout, ctx, owning) (Dense.hpp:90-91).  With owning = false
+    // the tile wraps the caller's DEVICE buffer; otherwise the data (host or device) is copied.
+    DenseTile(size_t aRows, size_t aCols, T *aData, size_t aLd, blas::Layout aLayout,
+              const kernels::RunContext &aContext, bool aOwning = true) {
+        if (aLayout != blas::Layout::ColMajor) throw std::invalid_argument("DenseTile: column-major only");
+        this->mRows = aRows;
+        this->mCols = aCols;
+        if (!aOwning) {
+            mData = aData;
+            return;
+        }
+        detail::cuda(cudaMalloc(&mData, sizeof(T) * aRows * aCols), "cudaMalloc");
+        mOwn = true;
+        if (aData)
+            detail::cuda(cudaMemcpy2D(mData, sizeof(T) * aRows, aData, sizeof(T) * aLd, sizeof(T) * aRows, aCols,
+                                      cudaMemcpyDefault),
+                         "cudaMemcpy2D");
+        else
+            detail::cuda(cudaMemset(mData, 0, sizeof(T) * aRows * aCols), "cudaMemset");
+    }
+    DenseTile(size_t aRows, size_t aCols, T *aData, size_t aLd, const kernels::RunContext &aContext)
+        : DenseTile(aRows, aCols, aData, aLd, blas::Layout::ColMajor, aContext) {}
+    ~DenseTile() override {
+        if (mOwn) cudaFree(mData);
+    }
+    DenseTile(const DenseTile &) = delete;
+    DenseTile &operator=(const DenseTile &) = delete;
+    int GetNumOfSubMatrices() const override { return 1; }
+    size_t GetTileRank() const override { return 0; }
+    T *GetTileSubMatrix(size_t aIndex) const {
+        if (aIndex != 0) throw std::invalid_argument("GetTileSubMatrix ::Index out of range");
+        return mData;
+    }
+    size_t GetLeadingDim() const { return this->mRows; }
+    hcgb_tile c_tile() const override {
+        return hcgb_tile{mData, nullptr, (int) this->mRows, (int) this->mCols, 0, HCGB_DENSE};
+    }
+
+private:
+    T *mData = nullptr;
+    bool mOwn = false;
+};
+
+template <typename T>
+class CompressedTile : public Tile<T> {
+public:
+    // (rows, cols, data, ld, rank, layout, ctx) (Compressed.cpp:50-73): data = packed [U | V],
+    // max rank = rank (the rank can never grow).
+    CompressedTile(size_t aRows, size_t aCols, T *aData, size_t aLd, size_t aRank, blas::Layout aLayout,
+                   const kernels::RunContext &aContext) {
+        init(aRows, aCols, aRank, aRank);
+        if (aData) {
+            detail::cuda(cudaMemcpy(mData, aData, sizeof(T) * aRows * aRank, cudaMemcpyDefault), "cudaMemcpy");
+            detail::cuda(cudaMemcpy(GetVMatrix(), aData + aRows * aRank, sizeof(T) * aRank * aCols,
+                                    cudaMemcpyDefault),
+                         "cudaMemcpy");
+        }
+        set_rank(aRank);
+    }
+    CompressedTile(size_t aRows, size_t aCols, T *aData, size_t aLd, size_t aRank,
+                   const kernels::RunContext &aContext)
+        : CompressedTile(aRows, aCols, aData, aLd, aRank, blas::Layout::ColMajor, aContext) {}
+    // (rows, cols, dense data, ld, params, layout, ctx) (Compressed.cpp:75-146): truncated SVD on
+    // the GPU, max rank = max(min(rows, cols) / 3, 1).
+    CompressedTile(size_t aRows, size_t aCols, T *aData, size_t aLd, const CompressionParameters &aParameters,
+                   blas::Layout aLayout, const kernels::RunContext &aContext) {
+        const size_t maxr = std::max<size_t>(std::min(aRows, aCols) / 3, 1);
+        init(aRows, aCols, maxr, 0);
+        if (aData) {
+            T *dd = nullptr;
+            detail::cuda(cudaMalloc(&dd, sizeof(T) * aRows * aCols), "cudaMalloc");
+            detail::cuda(cudaMemcpy2D(dd, sizeof(T) * aRows, aData, sizeof(T) * aLd, sizeof(T) * aRows, aCols,
+                                      cudaMemcpyDefault),
+                         "cudaMemcpy2D");
+            hcgb_tile t = c_tile();
+            hcgb_params p = aParameters.c_params();
+            int r = 0;
+            int rc = hcgb_compress_tile(aContext.handle(), dd, (int) aRows, (int) aCols, &t, &p, &r);
+            cudaFree(dd);
+            detail::check(rc, aContext.handle(), "hcgb_compress_tile");
+        }
+    }
+    ~CompressedTile() override {
+        cudaFree(mData);
+        cudaFree(mRank);
+    }
+    CompressedTile(const CompressedTile &) = delete;
+    CompressedTile &operator=(const CompressedTile &) = delete;
+    int GetNumOfSubMatrices() const override { return 2; }
+    size_t GetTileRank() const override {
+        int r = 0;
+        detail::cuda(cudaMemcpy(&r, mRank, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        return (size_t) r;
+    }
+    T *GetUMatrix() const { return mData; }
+    T *GetVMatrix() const { return mData + this->mRows * mMaxRank; }
+    size_t GetULeadingDim() const { return this->mRows; }
+    size_t GetVLeadingDim() const { return GetTileRank(); }
+    size_t GetMaxRank() const { return mMaxRank; }
+    T *GetTileSubMatrix(size_t aIndex) const {
+        if (aIndex > 1) throw std::invalid_argument("CompressedTile::GetTileSubMatrix:: Index out of range");
+        return aIndex == 0 ? GetUMatrix() : GetVMatrix();
+    }
+    int *GetDeviceRank() const { return mRank; }
+    hcgb_tile c_tile() const override {
+        return hcgb_tile{mData, mRank, (int) this->mRows, (int) this->mCols, (int) mMaxRank, HCGB_COMPRESSED};
+    }
+    // Room for the full-rank form a DDC update produces (HCore.cpp:294-298 re-sizes the tile the
+    // same way): grow the buffer to rank min(rows, cols), keeping U and V in place.
+    void EnsureFullRankCapacity() {
+        const size_t r = std::min(this->mRows, this->mCols);
+        if (r <= mMaxRank) return;
+        const size_t rank = GetTileRank();
+        T *nd = nullptr;
+        const size_t cap = this->mRows * r + r * this->mCols;
+        detail::cuda(cudaMalloc(&nd, sizeof(T) * cap), "cudaMalloc");
+        detail::cuda(cudaMemset(nd, 0, sizeof(T) * cap), "cudaMemset");
+        detail::cuda(cudaMemcpy(nd, mData, sizeof(T) * this->mRows * rank, cudaMemcpyDeviceToDevice), "cudaMemcpy");
+        detail::cuda(cudaMemcpy(nd + this->mRows * r, GetVMatrix(), sizeof(T) * rank * this->mCols,
+                                cudaMemcpyDeviceToDevice),
+                     "cudaMemcpy");
+        cudaFree(mData);
+        mData = nd;
+        mMaxRank = r;
+    }
+
+private:
+    void init(size_t rows, size_t cols, size_t maxr, size_t rank) {
+        this->mRows = rows;
+        this->mCols = cols;
+        mMaxRank = maxr;
+        const size_t cap = rows * maxr + maxr * cols;
+        detail::cuda(cudaMalloc(&mData, sizeof(T) * cap), "cudaMalloc");
+        detail::cuda(cudaMemset(mData, 0, sizeof(T) * cap), "cudaMemset");
+        detail::cuda(cudaMalloc(&mRank, sizeof(int)), "cudaMalloc");
+        set_rank(rank);
+    }
+    void set_rank(size_t r) {
+        int v = (int) r;
+        detail::cuda(cudaMemcpy(mRank, &v, sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
+    }
+    T *mData = nullptr;
+    int *mRank = nullptr;
+    size_t mMaxRank = 0;
+};
+
+}  // namespace operators
+
+namespace api {
+
+template <typename T>
+class HCore {
+public:
+    // C = alpha op(A) op(B) + beta C (HCore.cpp:23-344); flops += the reference's count.
+    static void Gemm(T aAlpha, const operators::Tile<T> &aA, const blas::Op &aAOp, const operators::Tile<T> &aB,
+                     const blas::Op &aBOp, T aBeta, operators::Tile<T> &aC, const kernels::RunContext &aContext,
+                     size_t &aFlops, dataunits::MemoryUnit<T> &aMemoryUnit,
+                     const operators::CompressionParameters &aParameters = {1e-9}, bool aCholesky = false) {
+        if (aCholesky) throw std::invalid_argument("HCore::Gemm: the Cholesky variant is not provided on this path");
+        // The DDC combination re-sets C at full rank: make room first.
+        const bool ddc = aA.isDense() && aB.isDense() && aC.isCompressed();
+        if (ddc) static_cast<operators::CompressedTile<T> &>(aC).EnsureFullRankCapacity();
+        hcgb_tile a = aA.c_tile(), b = aB.c_tile(), c = aC.c_tile();
+        hcgb_params p = aParameters.c_params();
+        int r = 0;
+        unsigned long long fl = 0;
+        const int oa = aAOp == blas::Op::NoTrans ? HCGB_NOTRANS : HCGB_TRANS;
+        const int ob = aBOp == blas::Op::NoTrans ? HCGB_NOTRANS : HCGB_TRANS;
+        detail::check(hcgb_tile_gemm(aContext.handle(), aAlpha, &a, oa, &b, ob, aBeta, &c, &p, &r, &fl),
+                      aContext.handle(), "HCore::Gemm");
+        aFlops += (size_t) fl;
+    }
+
+    // Scratch the library needs for one update of these tiles (HCore.cpp:417-480), in elements of T.
+    static size_t CalculateMemoryPoolSize(const operators::Tile<T> &aA, const operators::Tile<T> &aB,
+                                          const operators::Tile<T> &aC, operators::CompressionParameters,
+                                          const kernels::RunContext &) {
+        hcgb_tile a = aA.c_tile(), b = aB.c_tile(), c = aC.c_tile();
+        const int rab = std::max(a.kind == HCGB_COMPRESSED ? a.max_rank : 0, b.kind == HCGB_COMPRESSED ? b.max_rank : 0);
+        return hcgb_workspace_bytes(1, (int) std::max(c.rows, a.cols), c.cols,
+                                    c.kind == HCGB_COMPRESSED ? c.max_rank : 0, rab) / sizeof(T);
+    }
+};
+
+}  // namespace api
+}  // namespace hcorepp
+
+#endif  // HCOREPP_GB300_HCORE_HPP

@@ -261,3 +261,19 @@ def test_mixed_mode_vs_oracle(T, combo):
     T.HCore.Gemm(1.0, ga, 0, gb, 0, 1.0, gc, T.CompressionParameters(acc, truncated_svd=True, mode=L.MIXED))
     assert abs(gc.rank - oc.rank) <= 1
     assert rel_fro(gc.to_dense(), exact) <= 2 * max(rel_fro(oc.to_dense(), exact), acc)
+
+
+@pytest.mark.parametrize("truncated,acc", [(True, 1e-8), (False, 1e-6)])
+def test_compress_tile_vs_oracle(T, truncated, acc):
+    """GPU dense -> compressed construction vs the reference's constructor restated in the oracle
+    (Compressed.cpp:75-146): rank +-1, reconstruction error at the oracle's level."""
+    from hcorepp_gb300.problems import KernelMatrix
+    km = KernelMatrix(1024, 256, 2, 0.1, 4)
+    for (i, j) in [(0, 1), (0, 3), (2, 2)]:
+        d = km.tile(i, j)
+        o = O.CompressedTile.from_dense(d, O.CompressionParameters(acc, truncated_svd=truncated))
+        g = T.CompressedTile.from_dense(d, T.CompressionParameters(acc, truncated_svd=truncated))
+        assert g.max_rank == o.max_rank == 256 // 3
+        assert abs(g.rank - o.rank) <= 1, (i, j, g.rank, o.rank)
+        e_o = rel_fro(o.to_dense(), d)
+        assert rel_fro(g.to_dense(), d) <= 2 * max(e_o, 1e-14), (i, j)
