@@ -3,8 +3,9 @@
 // alpha = 3.5, beta = 2.5, compressed operands built by CompressedTile(dense, params), and the
 // reference's pass rule (AdvancedGemmTest.cpp:245-256):
 //   ||C_ref - C||_inf / (sqrt(k + 2) |alpha| ||A||_inf ||B||_inf + 2 |beta| ||C||_inf) < 3 * accuracy.
-// Inputs: exponential-kernel blocks on seeded random points (the reference's LAPACK dlatms
-// generator is not available here).  Exit status 0 = every case passed.
+// Inputs: Q1 diag(10^-i) Q2^T with seeded random orthogonal Q1, Q2 -- the singular values the
+// reference's generate_dense_matrix asks dlatms for (src/helpers/MatrixHelpers.cpp:22-31); the
+// LAPACK generator itself is not linked here.  Exit status 0 = every case passed.
 #include <hcorepp_gb300/hcore.hpp>
 
 #include <cmath>
@@ -16,17 +17,36 @@
 using namespace hcorepp;
 using M = std::vector<double>;
 
-static M kernel_block(int m, int n, unsigned seed, double ell) {
+static M random_orthogonal(int n, std::mt19937_64 &g) {
+    std::normal_distribution<double> nd(0.0, 1.0);
+    M q((size_t) n * n);
+    for (auto &v : q) v = nd(g);
+    for (int j = 0; j < n; j++) {  // modified Gram-Schmidt, twice for orthogonality to rounding
+        for (int pass = 0; pass < 2; pass++)
+            for (int k = 0; k < j; k++) {
+                double d = 0;
+                for (int i = 0; i < n; i++) d += q[i + (size_t) k * n] * q[i + (size_t) j * n];
+                for (int i = 0; i < n; i++) q[i + (size_t) j * n] -= d * q[i + (size_t) k * n];
+            }
+        double s = 0;
+        for (int i = 0; i < n; i++) s += q[i + (size_t) j * n] * q[i + (size_t) j * n];
+        s = 1.0 / std::sqrt(s);
+        for (int i = 0; i < n; i++) q[i + (size_t) j * n] *= s;
+    }
+    return q;
+}
+
+static M graded_matrix(int n, unsigned seed) {
     std::mt19937_64 g(seed);
-    std::uniform_real_distribution<double> u(0.0, 1.0);
-    std::vector<double> x(2 * (m + n));
-    for (auto &v : x) v = u(g);
-    M a((size_t) m * n);
-    for (int j = 0; j < n; j++)
-        for (int i = 0; i < m; i++) {
-            const double dx = x[2 * i] - x[2 * (m + j)], dy = x[2 * i + 1] - x[2 * (m + j) + 1];
-            a[i + (size_t) j * m] = std::exp(-std::sqrt(dx * dx + dy * dy) / ell);
+    M q1 = random_orthogonal(n, g), q2 = random_orthogonal(n, g), a((size_t) n * n, 0.0);
+    const int r = std::min(n, 20);  // 10^-i below 1e-20 is far under any accuracy tested
+    for (int l = 0; l < r; l++) {
+        const double s = std::pow(10.0, -l);
+        for (int j = 0; j < n; j++) {
+            const double b = s * q2[j + (size_t) l * n];
+            for (int i = 0; i < n; i++) a[i + (size_t) j * n] += q1[i + (size_t) l * n] * b;
         }
+    }
     return a;
 }
 
@@ -70,7 +90,7 @@ int main() {
     std::printf("|%-5s|%-5s|%-14s|%-5s|%-6s|\n", "Gemm", "n", "error", "Crk", "status");
     for (const char *combo : combos) {
         for (int n : {100, 200, 300}) {
-            M ad = kernel_block(n, n, 11 + n, 0.2), bd = kernel_block(n, n, 23 + n, 0.2), cd = kernel_block(n, n, 37 + n, 0.2);
+            M ad = graded_matrix(n, 11 + n), bd = graded_matrix(n, 23 + n), cd = graded_matrix(n, 37 + n);
             operators::CompressionParameters params(accuracy);
             std::unique_ptr<operators::Tile<double>> A, B, C;
             auto make = [&](char kind, M &d) -> std::unique_ptr<operators::Tile<double>> {
