@@ -33,6 +33,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 from hcorepp_gb300.problems import WORKLOADS, build_tiles  # noqa: E402
+from hcorepp_gb300.replicas import job_throughput  # noqa: E402
 
 METRIC = "TLR-GEMM tile-updates/s at 1e-8 rel err: plain FP64 vs batched mixed+learned"
 UNIT = "tile-updates/s"
@@ -286,11 +287,7 @@ def gpu_arm(args, rank, world, local):
         torch.distributed.barrier()
     ms = e0.elapsed_time(e1) / args.steps
     launches = int(sum(v[1] for v in ctx.profile_read().values()))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n_updates / (ms * 1e-3)
+    value, ms = job_throughput(ms, n_updates, device="cuda")
 
     # ---- one more multiply, serialised on one stream with CUDA events around every stage:
     #      the per-kernel durations behind the roofline (not part of the timed region).
@@ -338,11 +335,7 @@ def gpu_arm(args, rank, world, local):
     e2[1].record(stream)
     torch.cuda.synchronize()
     e2e_ms = e2[0].elapsed_time(e2[1]) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * n_updates / (e2e_ms * 1e-3)
+    e2e_value, e2e_ms = job_throughput(e2e_ms, n_updates, device="cuda")
 
     if rank != 0:
         return 0
