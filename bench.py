@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the dense FP64 accuracy check")
     ap.add_argument("--groups", type=int, default=8, help="independent C-tile groups (streams)")
+    ap.add_argument("--k-order", type=int, default=0, choices=[0, 1],
+                    help="0: ascending k per C tile (reference order); 1: costliest updates first")
     ap.add_argument("--mode", default="plain", choices=["plain", "mixed"],
                     help="plain: FP64 throughout; mixed: single-precision Jacobi preconditioning of the core")
     return ap.parse_args()
@@ -257,6 +259,7 @@ def gpu_arm(args, rank, world, local):
     info = T.info_buffer(n_updates)
     dmma_peak, dfma_peak = ctx.fp64_peak()
     ctx.set_concurrency(args.groups)
+    ctx.set_k_order(args.k_order)
 
     def step(record_info=False):
         Cw.arena.copy_(C0.arena)
@@ -390,7 +393,7 @@ def gpu_arm(args, rank, world, local):
                    "updates_per_step": n_updates, "accuracy": w["accuracy"], "threshold": "relative",
                    "dense_diagonal": w["dense_diagonal"], "max_rank": maxr,
                    "form": "plain_fp64" if args.mode == "plain" else "mixed (fp32-preconditioned core Jacobi)",
-                   "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups,
+                   "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups, "k_order": "ascending" if args.k_order == 0 else "cost-descending",
                    "l2": "inputs larger than L2 (A, C arenas 1.4 GB each), no flush"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "tensor" if dom in tensor_stages else "fp64_simt", "kernel": dom,

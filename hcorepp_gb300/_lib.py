@@ -86,6 +86,8 @@ def lib():
         L.hcgb_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong), ip]
         L.hcgb_fp64_peak.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.hcgb_set_concurrency.argtypes = [vp, ip]
+        L.hcgb_set_k_order.argtypes = [vp, ip]
+        L.hcgb_set_k_order.restype = C.c_int
         L.hcgb_compress_tile.argtypes = [vp, vp, ip, ip, C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int)]
         L.hcgb_compress_tile.restype = C.c_int
         L.hcgb_tile_gemm_noalloc.argtypes = [C.c_double, C.POINTER(Tile), C.POINTER(Tile), C.c_double,
@@ -136,6 +138,9 @@ class Context:
         cnt = (C.c_longlong * n)()
         self.check(lib().hcgb_profile_read(self._h, ms, cnt, n))
         return {STAGES[i]: (ms[i], cnt[i]) for i in range(n)}
+
+    def set_k_order(self, policy: int):
+        self.check(lib().hcgb_set_k_order(self._h, int(policy)))
 
     def set_concurrency(self, groups: int):
         self.check(lib().hcgb_set_concurrency(self._h, int(groups)))

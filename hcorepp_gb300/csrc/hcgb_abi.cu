@@ -30,6 +30,7 @@ struct hcgb_context {
     long long stage_launches[HCGB_NUM_STAGES] = {0};
     // independent C-tile groups of hcgb_tlr_gemm, one stream each
     int groups = 8;
+    int k_order = 0;  // 0: ascending k per C tile (reference order); 1: estimated cost, largest first
     std::vector<cudaStream_t> group_streams;
     std::vector<cudaEvent_t> group_events;  // [0] fork, [1..] joins
 };
@@ -359,7 +360,61 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         for (int idx = g; idx < n; idx += G) members.push_back(idx);
     }
     first[G] = n;
-    // Descriptors laid out [group][wave][member]; record uid = wave * n + tile index.
+    // k order per C tile: the reference's ascending k, or (k_order = 1) the updates of each C tile
+    // sorted by estimated recompression cost (stack width cubed), largest first, so that the
+    // expensive updates of all tiles fall into the same few k-waves instead of one per wave.
+    std::vector<int> korder((size_t) n * kt);
+    for (int idx = 0; idx < n; idx++)
+        for (int kk = 0; kk < kt; kk++) korder[(size_t) idx * kt + kk] = kk;
+    if (ctx->k_order == 1) {
+        auto rank_of = [&](const hcgb_tile &t, int *out) -> int {
+            *out = t.kind == HCGB_COMPRESSED ? -1 : t.rows;
+            return HCGB_OK;
+        };
+        // gather device ranks of every compressed tile with one synchronisation
+        std::vector<const int *> src;
+        std::vector<int> ra((size_t) mt * kt), rb((size_t) kt * nt), rcv((size_t) n);
+        for (size_t q = 0; q < ra.size(); q++) rank_of(a_grid[q], &ra[q]);
+        for (size_t q = 0; q < rb.size(); q++) rank_of(b_grid[q], &rb[q]);
+        for (size_t q = 0; q < rcv.size(); q++) rank_of(c_grid[q], &rcv[q]);
+        const size_t ntot = ra.size() + rb.size() + rcv.size();
+        int rc0;
+        if ((rc0 = ensure_stage(ctx, sizeof(int) * ntot))) return rc0;
+        int *hst = static_cast<int *>(ctx->stage);
+        auto fetch = [&](const hcgb_tile *grid, std::vector<int> &dst, size_t off) -> int {
+            for (size_t q = 0; q < dst.size(); q++)
+                if (grid[q].kind == HCGB_COMPRESSED)
+                    HCGB_CUDA(ctx, cudaMemcpyAsync(hst + off + q, grid[q].rank, sizeof(int), cudaMemcpyDeviceToHost,
+                                                   ctx->stream));
+            return HCGB_OK;
+        };
+        if ((rc0 = fetch(a_grid, ra, 0)) || (rc0 = fetch(b_grid, rb, ra.size())) ||
+            (rc0 = fetch(c_grid, rcv, ra.size() + rb.size())))
+            return rc0;
+        HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (size_t q = 0; q < ra.size(); q++) if (ra[q] < 0) ra[q] = hst[q];
+        for (size_t q = 0; q < rb.size(); q++) if (rb[q] < 0) rb[q] = hst[ra.size() + q];
+        for (size_t q = 0; q < rcv.size(); q++) if (rcv[q] < 0) rcv[q] = hst[ra.size() + rb.size() + q];
+        for (int idx = 0; idx < n; idx++) {
+            const int i = idx % mt, j = idx / mt;
+            if (c_grid[idx].kind != HCGB_COMPRESSED) continue;
+            std::vector<std::pair<double, int>> est(kt);
+            for (int kk = 0; kk < kt; kk++) {
+                const hcgb_tile &ta = a_grid[i + (size_t) kk * mt], &tb = b_grid[kk + (size_t) j * kt];
+                const int rA = ra[i + (size_t) kk * mt], rB = rb[kk + (size_t) j * kt];
+                int add;
+                if (ta.kind == HCGB_DENSE && tb.kind == HCGB_DENSE) add = 0;
+                else if (ta.kind == HCGB_DENSE) add = rB;
+                else if (tb.kind == HCGB_DENSE) add = rA;
+                else add = std::min(rA, rB);
+                const double kw = (double) (rcv[idx] + add);
+                est[kk] = {-kw * kw * kw, kk};
+            }
+            std::stable_sort(est.begin(), est.end());
+            for (int kk = 0; kk < kt; kk++) korder[(size_t) idx * kt + kk] = est[kk].second;
+        }
+    }
+    // Descriptors laid out [group][wave][member]; record uid = k * n + tile index.
     std::vector<hcgb_update> all((size_t) n * kt);
     std::vector<DevUpdate> dv((size_t) n * kt);
     for (int g = 0; g < G; g++) {
@@ -368,8 +423,9 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
             for (int q = 0; q < ng; q++) {
                 const int idx = members[first[g] + q];
                 const int i = idx % mt, j = idx / mt;
+                const int kx = korder[(size_t) idx * kt + kk];
                 const size_t w = (size_t) first[g] * kt + (size_t) kk * ng + q;
-                hcgb_update u{a_grid[i + (size_t) kk * mt], b_grid[kk + (size_t) j * kt], c_grid[idx]};
+                hcgb_update u{a_grid[i + (size_t) kx * mt], b_grid[kx + (size_t) j * kt], c_grid[idx]};
                 int rc;
                 if ((rc = check_tile(ctx, u.a, "A")) || (rc = check_tile(ctx, u.b, "B")) ||
                     (rc = check_tile(ctx, u.c, "C")))
@@ -377,7 +433,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
                 if (u.a.kind == HCGB_DENSE && u.b.kind == HCGB_DENSE && u.c.kind == HCGB_COMPRESSED)
                     return fail(ctx, HCGB_UNSUPPORTED, "hcgb_tlr_gemm: DDC updates are not batched");
                 all[w] = u;
-                dv[w] = DevUpdate{to_dev(u.a), to_dev(u.b), to_dev(u.c), kk * n + idx};
+                dv[w] = DevUpdate{to_dev(u.a), to_dev(u.b), to_dev(u.c), kx * n + idx};
             }
     }
     BatchShape sh = shape_of(all.data(), (int) all.size());
@@ -429,6 +485,12 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         }
     }
     HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+int hcgb_set_k_order(hcgb_context *ctx, int policy) {
+    if (!ctx || policy < 0 || policy > 1) return HCGB_BAD_ARG;
+    ctx->k_order = policy;
     return HCGB_OK;
 }
 

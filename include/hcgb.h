@@ -138,6 +138,12 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
  * The results do not depend on it. */
 int hcgb_set_concurrency(hcgb_context *ctx, int groups);
 
+/* Order of the k-updates of each C tile in hcgb_tlr_gemm.  0 (default): ascending k, the order of
+ * the reference's driver.  1: each C tile's updates sorted by estimated recompression cost, largest
+ * first (the sum C + sum_k A_ik B_kj is the same; rounding and truncation happen in another order,
+ * within the accuracy bound).  The expensive updates of all tiles then share a few k-waves. */
+int hcgb_set_k_order(hcgb_context *ctx, int policy);
+
 /* Single tile update, the drop-in for HCore<T>::Gemm (src/api/HCore.cpp:23-344).  op_a/op_b
  * accept HCGB_NOTRANS and HCGB_TRANS.  Synchronous: on return *c's rank on the device has been
  * updated; *new_rank (if not NULL) receives it on the host, like CompressedTile::Gemm updating

@@ -165,8 +165,10 @@ def test_trans_operands(T):
     assert rel_fro(gc2.to_dense(), exact2) < 1e-10
 
 
-def test_tlr_multiply_vs_oracle(T):
-    """A 4x4-tile multiply (nb=128) through hcgb_tlr_gemm against the oracle's tile loop."""
+@pytest.mark.parametrize("k_order", [0, 1])
+def test_tlr_multiply_vs_oracle(T, k_order):
+    """A 4x4-tile multiply (nb=128) through hcgb_tlr_gemm against the oracle's tile loop, in the
+    reference's k order and in the cost-first order (same sum, other rounding order)."""
     import torch
     from hcorepp_gb300 import _lib as L
     from hcorepp_gb300.problems import KernelMatrix
@@ -195,8 +197,11 @@ def test_tlr_multiply_vs_oracle(T):
     a_dense, b_dense, c_dense = (mats[x].to_dense() for x in "ABC")
     exact = a_dense @ b_dense + c_dense
     info = T.info_buffer(nt * nt * nt)
+    ctx = T.run_context()
+    ctx.set_k_order(k_order)
     T.tlr_gemm(1.0, mats["A"], mats["B"], 1.0, mats["C"], T.CompressionParameters(acc, truncated_svd=True), info)
     torch.cuda.synchronize()
+    ctx.set_k_order(0)
     info = info.cpu().numpy()
     assert int(info[:, 0].max()) == 0, info
     O.tile_matrix_multiply(otiles["A"], otiles["B"], otiles["C"], 1.0, 1.0, params)
