@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the dense FP64 accuracy check")
     ap.add_argument("--groups", type=int, default=8, help="independent C-tile groups (streams)")
-    ap.add_argument("--k-order", type=int, default=0, choices=[0, 1],
+    ap.add_argument("--k-order", type=int, default=1, choices=[0, 1],
                     help="0: ascending k per C tile (reference order); 1: costliest updates first")
     ap.add_argument("--mode", default="plain", choices=["plain", "mixed"],
                     help="plain: FP64 throughout; mixed: single-precision Jacobi preconditioning of the core")
