@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tlr_gemm_n16384_nb512", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-tiles", type=int, default=0, help="C tiles in the CPU sample (0: one per core)")
+    ap.add_argument("--cpu-tiles", type=int, default=256, help="C tiles (each with its full k-chain) in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the dense FP64 accuracy check")
     ap.add_argument("--groups", type=int, default=8, help="independent C-tile groups (streams)")
@@ -186,12 +186,13 @@ def load_tiles(T, L, tiles, nt, nb, max_rank):
     return tm, host, ranks
 
 
-def traffic_from_profiles(kernel_stage, workload):
+def traffic_from_profiles(kernel_stage, workload, updates_per_launch):
+    """DRAM bytes per launch of `kernel_stage`: the per-update traffic of an ncu capture on a
+    smaller case (profiles/ncu_traffic.json) times the updates one launch processes."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
-        data = json.load(open(path))
-        ent = data.get(workload, {}).get(kernel_stage)
-        return None if ent is None else float(ent["bytes_per_launch"])
+        ent = json.load(open(path)).get(workload, {}).get(kernel_stage)
+        return None if ent is None else float(ent["bytes_per_update"]) * updates_per_launch
     except Exception:
         return None
 
@@ -209,9 +210,10 @@ def stage_algorithmic_flops(info, nb, kinds_of_update):
     # QR of both stacks (Householder, 2 m k^2 - 2 k^3 / 3 each)
     out["qr"] = float(np.sum(np.where(comp, 2 * (2 * m * k * k - 2 * kk ** 3 / 3), 0.0)))
     # Core: triangular product (2 k^3 / 3), pivoted QR stopped at rk rows (sum_s 4 (k-s)^2),
-    # Jacobi on rk columns of length k (per sweep rk(rk-1)/2 pairs x 12 k flops), U_r = M V_r (2 k^2 r)
+    # Jacobi on rk columns of length k (per sweep rk(rk-1)/2 pairs x 8 k flops: one inner product and
+    # one rotation per pair, the squared norms being tracked), U_r = M V_r (2 k^2 r)
     qrcp = 4.0 * (kk ** 3 - np.maximum(kk - rk, 0) ** 3) / 3.0
-    out["core_svd"] = float(np.sum(np.where(comp, 2 * kk ** 3 / 3 + qrcp + sw * rk * (rk - 1) / 2 * 12 * kk
+    out["core_svd"] = float(np.sum(np.where(comp, 2 * kk ** 3 / 3 + qrcp + sw * rk * (rk - 1) / 2 * 8 * kk
                                             + 2 * kk * kk * r, 0.0)))
     # Q application on both sides: 4 m k r - 2 k^2 r each
     out["apply_q"] = float(np.sum(np.where(comp, 2 * (4 * m * k * r - 2 * kk * kk * r), 0.0)))
@@ -358,7 +360,8 @@ def gpu_arm(args, rank, world, local):
     tensor_stages = {"gemm", "qr", "apply_q"}
     peak = dmma_peak if dom in tensor_stages else dfma_peak
     achieved = dom_flops_per_launch / (dom_ms_per_launch * 1e-3) / 1e12
-    traffic = traffic_from_profiles(dom, args.workload)
+    comp_updates = int(np.count_nonzero(info_h[:, 4] > 0))
+    traffic = traffic_from_profiles(dom, args.workload, comp_updates / max(stages[dom][1], 1))
 
     # ---- accuracy against the FP64 dense product of the TLR inputs (cuBLAS, outside the timing)
     check = {}
