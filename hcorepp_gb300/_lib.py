@@ -18,6 +18,9 @@ HCGB_RANK_OVERFLOW, HCGB_NOT_CONVERGED, HCGB_UNSUPPORTED = 4, 5, 6
 STATUS_NAMES = {0: "OK", 1: "CUDA_ERROR", 2: "BAD_ARG", 3: "POOL_TOO_SMALL", 4: "RANK_OVERFLOW",
                 5: "NOT_CONVERGED", 6: "UNSUPPORTED"}
 DENSE, COMPRESSED = 0, 1
+LOWER, UPPER = 0, 1
+LEFT, RIGHT = 0, 1
+NONUNIT, UNIT = 0, 1
 NOTRANS, TRANS = 0, 1
 
 
@@ -87,6 +90,11 @@ def lib():
         L.hcgb_fp64_peak.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.hcgb_set_concurrency.argtypes = [vp, ip]
         L.hcgb_set_k_order.argtypes = [vp, ip]
+        L.hcgb_potrf.argtypes = [vp, ip, ip, vp, ip, C.POINTER(C.c_int)]
+        L.hcgb_trsm.argtypes = [vp, ip, ip, ip, ip, ip, ip, C.c_double, vp, ip, vp, ip]
+        L.hcgb_syrk.argtypes = [vp, ip, ip, ip, ip, C.c_double, vp, ip, C.c_double, vp, ip]
+        for nm in ("hcgb_potrf", "hcgb_trsm", "hcgb_syrk"):
+            getattr(L, nm).restype = C.c_int
         L.hcgb_set_k_order.restype = C.c_int
         L.hcgb_compress_tile.argtypes = [vp, vp, ip, ip, C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int)]
         L.hcgb_compress_tile.restype = C.c_int

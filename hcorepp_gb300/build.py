@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhcgb.so")
 
-CU_SOURCES = ["hcgb_abi.cu", "tlr_plan.cu", "tlr_qr.cu", "tlr_svd.cu", "probe.cu", "noalloc.cu"]
+CU_SOURCES = ["hcgb_abi.cu", "tlr_plan.cu", "tlr_qr.cu", "tlr_svd.cu", "probe.cu", "noalloc.cu", "chol.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -760,3 +760,53 @@ extern "C" int hcgb_compress_tile(hcgb_context *ctx, const double *dense, int ro
     if (rank) *rank = r;
     return rc;
 }
+
+extern "C" int hcgb_potrf(hcgb_context *ctx, int uplo, int n, double *A, int lda, int *info) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (!A || n < 0 || lda < (n > 1 ? n : 1) || (uplo != HCGB_LOWER && uplo != HCGB_UPPER))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_potrf: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (n == 0) {
+        if (info) *info = 0;
+        return HCGB_OK;
+    }
+    int *dinfo = nullptr;
+    HCGB_CUDA(ctx, cudaMalloc(&dinfo, sizeof(int)));
+    launch_potrf(A, n, lda, uplo, dinfo, ctx->stream);
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dinfo);
+    if (e != cudaSuccess) return fail(ctx, HCGB_CUDA_ERROR, std::string("hcgb_potrf: ") + cudaGetErrorString(e));
+    if (info) *info = h;
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_trsm(hcgb_context *ctx, int side, int uplo, int trans, int diag, int m, int n, double alpha,
+                         const double *A, int lda, double *B, int ldb) {
+    if (!ctx) return HCGB_BAD_ARG;
+    const int na = side == HCGB_LEFT ? m : n;
+    if (!A || !B || m < 0 || n < 0 || lda < (na > 1 ? na : 1) || ldb < (m > 1 ? m : 1) ||
+        (side != HCGB_LEFT && side != HCGB_RIGHT) || (uplo != HCGB_LOWER && uplo != HCGB_UPPER) ||
+        (trans != HCGB_NOTRANS && trans != HCGB_TRANS) || (diag != HCGB_NONUNIT && diag != HCGB_UNIT))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_trsm: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (m == 0 || n == 0) return HCGB_OK;
+    launch_trsm(side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb, ctx->stream);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_syrk(hcgb_context *ctx, int uplo, int trans, int n, int k, double alpha, const double *A, int lda,
+                         double beta, double *C, int ldc) {
+    if (!ctx) return HCGB_BAD_ARG;
+    const int rows_a = trans ? k : n;
+    if (!A || !C || n < 0 || k < 0 || lda < (rows_a > 1 ? rows_a : 1) || ldc < (n > 1 ? n : 1) ||
+        (uplo != HCGB_LOWER && uplo != HCGB_UPPER) || (trans != HCGB_NOTRANS && trans != HCGB_TRANS))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_syrk: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (n == 0) return HCGB_OK;
+    launch_syrk(uplo, trans, n, k, alpha, A, lda, beta, C, ldc, ctx->stream);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}

@@ -133,6 +133,13 @@ void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t
 // dst (cols x rows, ld ldd) = src^T (src rows x cols, ld lds); one CTA.
 void launch_transpose(const double *src, int lds, int rows, int cols, double *dst, int ldd, cudaStream_t st);
 
+// Dense tile building blocks of a tile Cholesky (chol.cu).
+void launch_potrf(double *A, int n, int lda, int uplo, int *info_dev, cudaStream_t st);
+void launch_trsm(int side, int uplo, int trans, int diag, int m, int n, double alpha, const double *A, int lda,
+                 double *B, int ldb, cudaStream_t st);
+void launch_syrk(int uplo, int trans, int n, int k, double alpha, const double *A, int lda, double beta, double *C,
+                 int ldc, cudaStream_t st);
+
 size_t qr_smem_bytes(int ld, int kmax);
 size_t svd_smem_bytes(int kmax);
 

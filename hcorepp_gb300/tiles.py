@@ -178,6 +178,91 @@ class HCore:
     gemm = Gemm
 
 
+def _dptr(t: torch.Tensor):
+    return C.c_void_p(t.data_ptr())
+
+
+class Blas:
+    """Dense per-tile building blocks on the GPU (HCoreKernels<T>::potrf / trsm / syrk)."""
+
+    @staticmethod
+    def potrf(uplo: int, n: int, a: torch.Tensor, lda: int) -> int:
+        ctx = run_context()
+        info = C.c_int(0)
+        ctx.check(L.lib().hcgb_potrf(ctx.handle, int(uplo), int(n), _dptr(a), int(lda), C.byref(info)))
+        return info.value
+
+    @staticmethod
+    def trsm(side, uplo, trans, diag, m, n, alpha, a: torch.Tensor, lda, b: torch.Tensor, ldb):
+        ctx = run_context()
+        ctx.check(L.lib().hcgb_trsm(ctx.handle, int(side), int(uplo), int(trans), int(diag), int(m), int(n),
+                                    float(alpha), _dptr(a), int(lda), _dptr(b), int(ldb)))
+
+    @staticmethod
+    def syrk(uplo, trans, n, k, alpha, a: torch.Tensor, lda, beta, c: torch.Tensor, ldc):
+        ctx = run_context()
+        ctx.check(L.lib().hcgb_syrk(ctx.handle, int(uplo), int(trans), int(n), int(k), float(alpha), _dptr(a),
+                                    int(lda), float(beta), _dptr(c), int(ldc)))
+
+
+def Potrf(a: DenseTile, uplo: int = L.LOWER) -> int:
+    """HCore<T>::Potrf (src/api/HCore.cpp:585-621): dense tiles only."""
+    if a.kind != L.DENSE:
+        raise RuntimeError(" Potrf works only with dense tiles")
+    return Blas.potrf(uplo, a.rows, a.buffer, a.rows)
+
+
+def Trsm(side, uplo, trans, diag, alpha, a: DenseTile, b: CompressedTile):
+    """HCore<T>::Trsm (src/api/HCore.cpp:623-647) with the reference's arguments: the solve runs on
+    the V buffer of the compressed B viewed as a rows x rank matrix with leading dimension rows."""
+    if b.kind != L.COMPRESSED:
+        raise RuntimeError(" TRSM: Tile B must be compressed ")
+    r = b.rank
+    v = b.buffer[b.rows * b.max_rank:]
+    Blas.trsm(side, uplo, trans, diag, b.rows, r, alpha, a.buffer, a.rows, v, b.rows)
+
+
+def Syrk(alpha, a, a_op, uplo, beta, c: DenseTile, params=None):
+    """HCore<T>::Syrk (src/api/HCore.cpp:482-583) for a dense C.  Dense A: dsyrk on the uplo
+    triangle.  Compressed A = U V: C <- beta C - U (V V^T) U^T (the reference hard-codes -1 there),
+    then the other triangle is set to zero (FillMatrixTriangle, HCore.cpp:555-563)."""
+    if c.kind != L.DENSE:
+        raise NotImplementedError("Syrk into a compressed C is not provided")
+    n = c.rows
+    if a.kind == L.DENSE:
+        Blas.syrk(uplo, a_op, n, c.cols, alpha, a.buffer, a.rows, beta, c.buffer, n)
+        return
+    HCore.Gemm(-1.0, a, L.NOTRANS, a, L.TRANS, beta, c, params or CompressionParameters(1e-9))
+    m = c.buffer.view(n, n).t()  # column-major view: m[i, j] = C(i, j)
+    mask = torch.triu(torch.ones(n, n, dtype=torch.bool, device=m.device), 1)
+    m.masked_fill_(mask if uplo == L.LOWER else mask.t(), 0.0)
+
+
+def tile_cholesky(a: "TileMatrix", params: CompressionParameters) -> int:
+    """Right-looking tile Cholesky A = L L^T of a symmetric positive definite tile matrix with dense
+    diagonal tiles and compressed tiles below the diagonal (tiles above are not referenced).
+    The reference provides the per-tile operations (Potrf, Trsm, Syrk, Gemm) but no driver.
+    Returns 0, or the potrf info of the first failing diagonal tile (as k*nb + info)."""
+    nt, nb = a.mt, a.nb
+    for k in range(nt):
+        akk = a.tile(k, k)
+        info = Potrf(akk, L.LOWER)
+        if info:
+            return k * nb + info
+        for i in range(k + 1, nt):
+            # A_ik <- A_ik L_kk^-T on the V factor: V <- V L_kk^-T (rank x nb, ld rank)
+            aik = a.tile(i, k)
+            r = aik.rank
+            v = aik.buffer[nb * aik.max_rank:]
+            Blas.trsm(L.RIGHT, L.LOWER, L.TRANS, L.NONUNIT, r, nb, 1.0, akk.buffer, nb, v, max(r, 1))
+        for i in range(k + 1, nt):
+            aik = a.tile(i, k)
+            HCore.Gemm(-1.0, aik, L.NOTRANS, aik, L.TRANS, 1.0, a.tile(i, i), params)
+            for j in range(k + 1, i):
+                HCore.Gemm(-1.0, aik, L.NOTRANS, a.tile(j, k), L.TRANS, 1.0, a.tile(i, j), params)
+    return 0
+
+
 class TileMatrix:
     """A grid of mt x nt tiles of nb x nb, resident in one device arena.
 

@@ -163,6 +163,25 @@ int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *a, int op_a
 int hcgb_compress_tile(hcgb_context *ctx, const double *dense, int rows, int cols, hcgb_tile *out,
                        const hcgb_params *params, int *rank);
 
+/* ---- Dense per-tile building blocks of a tile Cholesky (device pointers, column-major) ---- */
+typedef enum { HCGB_LOWER = 0, HCGB_UPPER = 1 } hcgb_uplo;
+typedef enum { HCGB_LEFT = 0, HCGB_RIGHT = 1 } hcgb_side;
+typedef enum { HCGB_NONUNIT = 0, HCGB_UNIT = 1 } hcgb_diag;
+
+/* Cholesky factorisation of the uplo triangle of A (n x n, ld lda), LAPACK dpotrf semantics;
+ * replaces HCoreKernels::potrf (src/kernels/cuda/CudaKernels.cu:1019-1049, omp/kernels.cpp:234-243).
+ * Synchronous; *info (if not NULL) receives 0 or the order of the first non-positive minor. */
+int hcgb_potrf(hcgb_context *ctx, int uplo, int n, double *A, int lda, int *info);
+/* op(A) X = alpha B (HCGB_LEFT) or X op(A) = alpha B (HCGB_RIGHT), X overwriting B (m x n);
+ * BLAS dtrsm semantics; replaces HCoreKernels::trsm (src/kernels/cuda/kernels.cpp:290-298).
+ * trans: HCGB_NOTRANS / HCGB_TRANS.  Asynchronous. */
+int hcgb_trsm(hcgb_context *ctx, int side, int uplo, int trans, int diag, int m, int n, double alpha,
+              const double *A, int lda, double *B, int ldb);
+/* C = alpha op(A) op(A)^T + beta C on the uplo triangle (C n x n, op(A) n x k); BLAS dsyrk
+ * semantics; replaces HCoreKernels::syrk (src/kernels/cuda/kernels.cpp:299-306).  Asynchronous. */
+int hcgb_syrk(hcgb_context *ctx, int uplo, int trans, int n, int k, double alpha, const double *A, int lda,
+              double beta, double *C, int ldc);
+
 /* Stage timing with CUDA events on the context stream (the GB300 replacement of the reference's
  * DebuggingTimer snapshots, src/helpers/debugging-timer/ActiveTimer.cpp:47-60).  While enabled,
  * every pipeline stage is bracketed by events; hcgb_profile_read synchronises the stream and

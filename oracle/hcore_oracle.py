@@ -306,3 +306,56 @@ def tile_matrix_multiply(a_tiles, b_tiles, c_tiles, alpha: float, beta: float,
             info = hcore_gemm(alpha, a_tiles[i][k], b_tiles[k][j], beta, c_tiles[i][j], params)
             stats.append((i, j, k, info.get("k"), info.get("rank"), info.get("clamped")))
     return stats
+
+
+# ---------------------------------------------------------------------------
+# Tile Cholesky building blocks (src/api/HCore.cpp:482-647, omp/kernels.cpp:234-282)
+# ---------------------------------------------------------------------------
+
+def potrf_lower(a: np.ndarray):
+    """omp/kernels.cpp:234-243 -> LAPACK dpotrf (lower); returns (L in the lower triangle, info)."""
+    c, info = lapack.dpotrf(np.asfortranarray(a), lower=1, clean=0)
+    return c, info
+
+
+def trsm(side_left: bool, lower: bool, trans: bool, unit: bool, alpha: float, a: np.ndarray, b: np.ndarray):
+    """BLAS dtrsm: op(A) X = alpha B (left) or X op(A) = alpha B (right)."""
+    import scipy.linalg as sl
+    t = np.tril(a) if lower else np.triu(a)
+    if unit:
+        t = t - np.diag(np.diag(t)) + np.eye(t.shape[0])
+    opt = t.T if trans else t
+    if side_left:
+        return sl.solve_triangular(opt, alpha * b, lower=(lower != trans))
+    return sl.solve_triangular(opt.T, alpha * b.T, lower=not (lower != trans)).T
+
+
+def hcore_trsm_compressed(side_left, lower, trans, unit, alpha, a: np.ndarray, b: "CompressedTile") -> None:
+    """HCore<T>::Trsm (HCore.cpp:623-647): trsm on the V buffer viewed as rows x rank (ld rows)."""
+    rows, r = b.rows, b.rank
+    flat = b.v.ravel(order="F").copy()
+    x = flat.reshape((rows, r), order="F")
+    x = trsm(side_left, lower, trans, unit, alpha, a, x)
+    b.v = np.asfortranarray(x.ravel(order="F").reshape((r, b.cols), order="F"))
+
+
+def tile_cholesky(a_tiles, nt, params) -> int:
+    """Right-looking tile Cholesky on a grid of oracle tiles (dense diagonal, compressed below)."""
+    for k in range(nt):
+        c, info = potrf_lower(a_tiles[k][k].data)
+        if info:
+            return k * a_tiles[k][k].rows + info
+        lkk = np.tril(c)
+        a_tiles[k][k].data = np.asfortranarray(np.where(np.tril(np.ones_like(c)) > 0, c, a_tiles[k][k].data))
+        for i in range(k + 1, nt):
+            t = a_tiles[i][k]
+            t.v = np.asfortranarray(trsm(False, True, True, False, 1.0, lkk, t.v))
+        for i in range(k + 1, nt):
+            aik = a_tiles[i][k]
+            d = a_tiles[i][i]
+            d.data = np.asfortranarray(d.data - aik.to_dense() @ aik.to_dense().T)
+            for j in range(k + 1, i):
+                ajk = a_tiles[j][k]
+                hcore_gemm(-1.0, CompressedTile(aik.u, aik.v), CompressedTile(ajk.v.T, ajk.u.T), 1.0, a_tiles[i][j],
+                           params)
+    return 0

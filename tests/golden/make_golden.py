@@ -24,6 +24,9 @@ SOURCES = [
     ("gemm_test9_ccc", "tests/api/TestGemm.cpp", 748, 915, ["matrix_Au", "matrix_Av", "matrix_Bu", "matrix_Bv",
                                                              "output_matrix"]),
     ("gemm_test10_ddc", "tests/api/TestGemm.cpp", 917, 1045, ["matrix_A", "matrix_B", "output_matrix"]),
+    ("potrf", "tests/kernels/TestKernels.cpp", 1070, 1124, ["matrix_A", "matrix_Output"]),
+    ("trsm", "tests/kernels/TestKernels.cpp", 1126, 1184, ["matrix_A", "matrix_B", "matrix_output"]),
+    ("syrk_cross_product", "tests/kernels/TestKernels.cpp", 1185, 1250, ["matrix_A", "matrix_B", "matrix_output"]),
 ]
 
 NUM = re.compile(r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?")

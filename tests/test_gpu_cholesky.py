@@ -1,0 +1,141 @@
+"""GPU tile-Cholesky building blocks (hcgb_potrf / hcgb_trsm / hcgb_syrk) against the reference's
+known answers (tests/kernels/TestKernels.cpp:1070-1250) and LAPACK/BLAS through the oracle, the
+HCore-level Trsm on a compressed tile, and a tile-Cholesky driver's residual ||L L^T - A|| / ||A||."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import hcore_oracle as O
+from tests.helpers import compressed_from_dense, rel_fro
+
+pytestmark = pytest.mark.gpu
+KAT = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "kat.json")))
+
+
+def _rm(entry, name, r, c):
+    return np.array(KAT[entry][name]["values"]).reshape(r, c)
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+
+
+def _host(t, r, c):
+    return t.cpu().numpy().reshape((r, c), order="F")
+
+
+@pytest.fixture(scope="module")
+def T():
+    from hcorepp_gb300 import tiles
+    return tiles
+
+
+def test_potrf_kat(T):
+    a = _dev(_rm("potrf", "matrix_A", 3, 3))
+    assert T.Blas.potrf(0, 3, a, 3) == 0
+    np.testing.assert_allclose(np.tril(_host(a, 3, 3)), _rm("potrf", "matrix_Output", 3, 3), rtol=1e-12)
+
+
+def test_trsm_kat(T):
+    a, b = _dev(_rm("trsm", "matrix_A", 3, 3)), _dev(_rm("trsm", "matrix_B", 3, 1))
+    T.Blas.trsm(0, 1, 0, 0, 3, 1, 1.0, a, 3, b, 3)
+    np.testing.assert_allclose(_host(b, 3, 1), _rm("trsm", "matrix_output", 3, 1), rtol=1e-12)
+
+
+def test_syrk_kat(T):
+    a = _dev(_rm("syrk_cross_product", "matrix_A", 4, 4))
+    c = _dev(_rm("syrk_cross_product", "matrix_B", 4, 4))
+    T.Blas.syrk(0, 0, 4, 4, 1.0, a, 4, 0.0, c, 4)
+    np.testing.assert_allclose(_host(c, 4, 4), _rm("syrk_cross_product", "matrix_output", 4, 4), rtol=1e-9)
+
+
+@pytest.mark.parametrize("uplo", [0, 1])
+def test_potrf_random_and_not_positive(T, uplo):
+    rng = np.random.default_rng(uplo)
+    g = rng.standard_normal((300, 300))
+    a = g @ g.T + 300 * np.eye(300)
+    d = _dev(a)
+    assert T.Blas.potrf(uplo, 300, d, 300) == 0
+    got = _host(d, 300, 300)
+    f = np.tril(got) if uplo == 0 else np.triu(got)
+    ref = np.linalg.cholesky(a)
+    np.testing.assert_allclose(f, ref if uplo == 0 else ref.T, rtol=1e-10, atol=1e-10)
+    bad = a.copy()
+    bad[5, 5] = -1.0
+    assert T.Blas.potrf(uplo, 300, _dev(bad), 300) == 6  # dpotrf's info: order of the failing minor
+
+
+@pytest.mark.parametrize("side", [0, 1])
+@pytest.mark.parametrize("uplo", [0, 1])
+@pytest.mark.parametrize("trans", [0, 1])
+@pytest.mark.parametrize("diag", [0, 1])
+def test_trsm_all_forms(T, side, uplo, trans, diag):
+    rng = np.random.default_rng(7 + side + 2 * uplo + 4 * trans + 8 * diag)
+    m, n = 70, 45
+    na = m if side == 0 else n
+    a = rng.standard_normal((na, na)) + na * np.eye(na)
+    b = rng.standard_normal((m, n))
+    db = _dev(b)
+    T.Blas.trsm(side, uplo, trans, diag, m, n, 0.75, _dev(a), na, db, m)
+    ref = O.trsm(side == 0, uplo == 0, trans == 1, diag == 1, 0.75, a, b)
+    np.testing.assert_allclose(_host(db, m, n), ref, rtol=1e-10, atol=1e-12)
+
+
+def test_hcore_trsm_compressed_matches_oracle(T):
+    """HCore<T>::Trsm on a compressed B, with the reference's arguments (the V buffer viewed as
+    rows x rank, ld rows; src/api/HCore.cpp:623-647)."""
+    rng = np.random.default_rng(3)
+    nb = 64
+    a = np.tril(rng.standard_normal((nb, nb))) + nb * np.eye(nb)
+    d = rng.standard_normal((nb, 8)) @ rng.standard_normal((8, nb))
+    ob = compressed_from_dense(d, 1e-12, True)
+    gb = T.CompressedTile(nb, nb, ob.u, ob.v, max_rank=ob.max_rank)
+    ga = T.DenseTile(nb, nb, a)
+    T.Trsm(0, 0, 0, 0, 2.0, ga, gb)
+    O.hcore_trsm_compressed(True, True, False, False, 2.0, a, ob)
+    np.testing.assert_allclose(gb.v(), ob.v, rtol=1e-10, atol=1e-12)
+
+
+def test_tile_cholesky_residual(T):
+    """Tile Cholesky of an SPD exponential-kernel matrix (3-D points, dense diagonal tiles, 1e-8
+    compressed off-diagonal tiles): residual ||L L^T - A||_F / ||A||_F and agreement with the
+    oracle's driver."""
+    from hcorepp_gb300 import _lib as L
+    from hcorepp_gb300.problems import KernelMatrix
+    nt, nb, acc = 4, 128, 1e-8
+    km = KernelMatrix(nt * nb, nb, 3, 0.2, 5, diag_shift=1e-2)
+    a_dense = km.dense()
+    kinds = [[L.DENSE if i == j else L.COMPRESSED for j in range(nt)] for i in range(nt)]
+    tm = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+    og = [[None] * nt for _ in range(nt)]
+    for i in range(nt):
+        for j in range(nt):
+            blk = km.tile(i, j)
+            if i == j:
+                tm.set_tile(i, j, dense=blk)
+                og[i][j] = O.DenseTile(blk)
+            elif i > j:
+                t = compressed_from_dense(blk, acc)
+                tm.set_tile(i, j, u=t.u, v=t.v)
+                og[i][j] = t
+    params = T.CompressionParameters(acc, truncated_svd=True)
+    assert T.tile_cholesky(tm, params) == 0
+    assert O.tile_cholesky(og, nt, O.CompressionParameters(acc, truncated_svd=True)) == 0
+    full = tm.to_dense()
+    lfac = np.zeros_like(full)
+    ofac = np.zeros_like(full)
+    for i in range(nt):
+        for j in range(i + 1):
+            blk = full[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb]
+            oblk = og[i][j].to_dense()
+            if i == j:
+                blk, oblk = np.tril(blk), np.tril(oblk)
+            lfac[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb] = blk
+            ofac[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb] = oblk
+    res = rel_fro(lfac @ lfac.T, a_dense)
+    res_o = rel_fro(ofac @ ofac.T, a_dense)
+    assert res < 1e-6 and res <= 2 * max(res_o, acc), (res, res_o)
+    assert rel_fro(lfac, ofac) < 1e-5

@@ -122,3 +122,29 @@ def test_compress_from_dense_rank_rule():
     assert t.rank == 6 and t.max_rank == 10
     t = O.CompressedTile.from_dense(a, O.CompressionParameters(1e-14, truncated_svd=True))
     assert t.rank == 10  # clamped at 30 / 3
+
+
+def test_potrf_kat():
+    # TestKernels.cpp:1070-1124: lower Cholesky of [[25,15,5],[15,13,11],[5,11,21]] (the reference
+    # prints but does not compare; the lower triangle is the known factor).
+    a = rowmajor("potrf", "matrix_A", 3, 3)
+    c, info = O.potrf_lower(a)
+    assert info == 0
+    np.testing.assert_allclose(np.tril(c), rowmajor("potrf", "matrix_Output", 3, 3), rtol=1e-12)
+
+
+def test_trsm_kat():
+    # TestKernels.cpp:1126-1184: Left, Upper, NoTrans, NonUnit, alpha 1
+    a = rowmajor("trsm", "matrix_A", 3, 3)
+    b = rowmajor("trsm", "matrix_B", 3, 1)
+    x = O.trsm(True, False, False, False, 1.0, a, b)
+    np.testing.assert_allclose(x, rowmajor("trsm", "matrix_output", 3, 1), rtol=1e-2)
+
+
+def test_syrk_kat():
+    # TestKernels.cpp:1185-1250: C = A A^T on the lower triangle, beta 0; the upper triangle keeps C.
+    a = rowmajor("syrk_cross_product", "matrix_A", 4, 4)
+    c0 = rowmajor("syrk_cross_product", "matrix_B", 4, 4)
+    expected = rowmajor("syrk_cross_product", "matrix_output", 4, 4)
+    got = np.where(np.tril(np.ones((4, 4))) > 0, a @ a.T, c0)
+    np.testing.assert_allclose(got, expected, rtol=1e-2)
