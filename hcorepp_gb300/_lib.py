@@ -17,7 +17,7 @@ HCGB_OK, HCGB_CUDA_ERROR, HCGB_BAD_ARG, HCGB_POOL_TOO_SMALL = 0, 1, 2, 3
 HCGB_RANK_OVERFLOW, HCGB_NOT_CONVERGED, HCGB_UNSUPPORTED = 4, 5, 6
 STATUS_NAMES = {0: "OK", 1: "CUDA_ERROR", 2: "BAD_ARG", 3: "POOL_TOO_SMALL", 4: "RANK_OVERFLOW",
                 5: "NOT_CONVERGED", 6: "UNSUPPORTED"}
-DENSE, COMPRESSED = 0, 1
+DENSE, COMPRESSED, COMPRESSED_VT = 0, 1, 2  # COMPRESSED_VT: V region holds W = V^T (cols x rank)
 LOWER, UPPER = 0, 1
 LEFT, RIGHT = 0, 1
 NONUNIT, UNIT = 0, 1
@@ -93,7 +93,8 @@ def lib():
         L.hcgb_potrf.argtypes = [vp, ip, ip, vp, ip, C.POINTER(C.c_int)]
         L.hcgb_trsm.argtypes = [vp, ip, ip, ip, ip, ip, ip, C.c_double, vp, ip, vp, ip]
         L.hcgb_syrk.argtypes = [vp, ip, ip, ip, ip, C.c_double, vp, ip, C.c_double, vp, ip]
-        for nm in ("hcgb_potrf", "hcgb_trsm", "hcgb_syrk"):
+        L.hcgb_fill_triangle.argtypes = [vp, ip, ip, vp, ip, C.c_double]
+        for nm in ("hcgb_potrf", "hcgb_trsm", "hcgb_syrk", "hcgb_fill_triangle"):
             getattr(L, nm).restype = C.c_int
         L.hcgb_set_k_order.restype = C.c_int
         L.hcgb_compress_tile.argtypes = [vp, vp, ip, ip, C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int)]

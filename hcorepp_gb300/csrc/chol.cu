@@ -111,7 +111,21 @@ __global__ void syrk_kernel(int uplo, int trans, int n, int k, double alpha, con
     *c = alpha * s + (beta != 0.0 ? beta * *c : 0.0);
 }
 
+// Sets the strict uplo triangle of A (n x n, ld lda) to value (HCoreKernels::FillMatrixTriangle,
+// src/kernels/omp/kernels.cpp:246-264).
+__global__ void fill_triangle_kernel(int uplo, int n, double *A, int lda, double value) {
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || j >= n) return;
+    if (uplo == 0 ? (i > j) : (i < j)) A[i + (size_t) j * lda] = value;
+}
+
 }  // namespace
+
+void launch_fill_triangle(int uplo, int n, double *A, int lda, double value, cudaStream_t st) {
+    dim3 blk(32, 8), grid((n + 31) / 32, (n + 7) / 8);
+    fill_triangle_kernel<<<grid, blk, 0, st>>>(uplo, n, A, lda, value);
+}
 
 void launch_potrf(double *A, int n, int lda, int uplo, int *info_dev, cudaStream_t st) {
     potrf_kernel<<<1, CT, 0, st>>>(A, n, lda, uplo, info_dev);

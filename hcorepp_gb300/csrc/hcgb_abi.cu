@@ -75,23 +75,25 @@ int ensure_stage(hcgb_context *ctx, size_t want) {
     return HCGB_OK;
 }
 
+bool compressed(int kind) { return kind == HCGB_COMPRESSED || kind == HCGB_COMPRESSED_VT; }
+
 DevTile to_dev(const hcgb_tile &t) {
     DevTile d;
     d.data = t.data;
     d.rank = t.rank;
     d.rows = t.rows;
     d.cols = t.cols;
-    d.max_rank = t.kind == HCGB_COMPRESSED ? t.max_rank : 0;
-    d.kind = t.kind == HCGB_COMPRESSED ? 1 : 0;
+    d.max_rank = compressed(t.kind) ? t.max_rank : 0;
+    d.kind = compressed(t.kind) ? t.kind : 0;
     return d;
 }
 
 int check_tile(hcgb_context *ctx, const hcgb_tile &t, const char *name) {
     if (!t.data || t.rows <= 0 || t.cols <= 0)
         return fail(ctx, HCGB_BAD_ARG, std::string(name) + ": null buffer or empty shape");
-    if (t.kind == HCGB_COMPRESSED && (!t.rank || t.max_rank <= 0))
+    if (compressed(t.kind) && (!t.rank || t.max_rank <= 0))
         return fail(ctx, HCGB_BAD_ARG, std::string(name) + ": compressed tile without rank or capacity");
-    if (t.kind != HCGB_DENSE && t.kind != HCGB_COMPRESSED)
+    if (t.kind != HCGB_DENSE && !compressed(t.kind))
         return fail(ctx, HCGB_BAD_ARG, std::string(name) + ": unknown tile kind");
     return HCGB_OK;
 }
@@ -108,8 +110,8 @@ BatchShape shape_of(const hcgb_update *ups, int n) {
     BatchShape s;
     for (int i = 0; i < n; i++) {
         const hcgb_update &u = ups[i];
-        const bool ak = u.a.kind == HCGB_COMPRESSED, bk = u.b.kind == HCGB_COMPRESSED,
-                   ck = u.c.kind == HCGB_COMPRESSED;
+        const bool ak = compressed(u.a.kind), bk = compressed(u.b.kind),
+                   ck = compressed(u.c.kind);
         const int m = u.c.rows, nn = u.c.cols;
         const int ra = ak ? u.a.max_rank : 0, rb = bk ? u.b.max_rank : 0, rc = ck ? u.c.max_rank : 0;
         s.ld = std::max({s.ld, m, nn, u.a.cols});
@@ -327,7 +329,7 @@ int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const h
             (rc = check_tile(ctx, updates[i].c, "C")))
             return rc;
         if (updates[i].a.kind == HCGB_DENSE && updates[i].b.kind == HCGB_DENSE &&
-            updates[i].c.kind == HCGB_COMPRESSED)
+            compressed(updates[i].c.kind))
             return fail(ctx, HCGB_UNSUPPORTED, "hcgb_gemm_batch: DDC updates go through hcgb_tile_gemm");
         dv[i] = DevUpdate{to_dev(updates[i].a), to_dev(updates[i].b), to_dev(updates[i].c), i};
     }
@@ -368,7 +370,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         for (int kk = 0; kk < kt; kk++) korder[(size_t) idx * kt + kk] = kk;
     if (ctx->k_order == 1) {
         auto rank_of = [&](const hcgb_tile &t, int *out) -> int {
-            *out = t.kind == HCGB_COMPRESSED ? -1 : t.rows;
+            *out = compressed(t.kind) ? -1 : t.rows;
             return HCGB_OK;
         };
         // gather device ranks of every compressed tile with one synchronisation
@@ -383,7 +385,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         int *hst = static_cast<int *>(ctx->stage);
         auto fetch = [&](const hcgb_tile *grid, std::vector<int> &dst, size_t off) -> int {
             for (size_t q = 0; q < dst.size(); q++)
-                if (grid[q].kind == HCGB_COMPRESSED)
+                if (compressed(grid[q].kind))
                     HCGB_CUDA(ctx, cudaMemcpyAsync(hst + off + q, grid[q].rank, sizeof(int), cudaMemcpyDeviceToHost,
                                                    ctx->stream));
             return HCGB_OK;
@@ -397,7 +399,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         for (size_t q = 0; q < rcv.size(); q++) if (rcv[q] < 0) rcv[q] = hst[ra.size() + rb.size() + q];
         for (int idx = 0; idx < n; idx++) {
             const int i = idx % mt, j = idx / mt;
-            if (c_grid[idx].kind != HCGB_COMPRESSED) continue;
+            if (!compressed(c_grid[idx].kind)) continue;
             std::vector<std::pair<double, int>> est(kt);
             for (int kk = 0; kk < kt; kk++) {
                 const hcgb_tile &ta = a_grid[i + (size_t) kk * mt], &tb = b_grid[kk + (size_t) j * kt];
@@ -430,7 +432,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
                 if ((rc = check_tile(ctx, u.a, "A")) || (rc = check_tile(ctx, u.b, "B")) ||
                     (rc = check_tile(ctx, u.c, "C")))
                     return rc;
-                if (u.a.kind == HCGB_DENSE && u.b.kind == HCGB_DENSE && u.c.kind == HCGB_COMPRESSED)
+                if (u.a.kind == HCGB_DENSE && u.b.kind == HCGB_DENSE && compressed(u.c.kind))
                     return fail(ctx, HCGB_UNSUPPORTED, "hcgb_tlr_gemm: DDC updates are not batched");
                 all[w] = u;
                 dv[w] = DevUpdate{to_dev(u.a), to_dev(u.b), to_dev(u.c), kx * n + idx};
@@ -549,10 +551,21 @@ int transposed_tile(hcgb_context *ctx, const hcgb_tile &t, int rank, hcgb_tile *
     }
     const size_t cap = (size_t) t.cols * t.max_rank + (size_t) t.max_rank * t.rows;
     HCGB_CUDA(ctx, cudaMalloc(&tmp->buf, sizeof(double) * cap));
-    // new U (cols x rank, ld cols) = V^T, new V (rank x rows, ld rank) = U^T
     const double *U = t.data, *V = t.data + (size_t) t.rows * t.max_rank;
-    launch_transpose(V, rank, rank, t.cols, tmp->buf, t.cols, ctx->stream);
-    launch_transpose(U, t.rows, t.rows, rank, tmp->buf + (size_t) t.cols * t.max_rank, rank, ctx->stream);
+    if (t.kind == HCGB_COMPRESSED_VT) {
+        // (U W^T)^T = W U^T: the factors swap places, both already in their layouts.
+        if (rank > 0) {
+            HCGB_CUDA(ctx, cudaMemcpyAsync(tmp->buf, V, sizeof(double) * (size_t) t.cols * rank,
+                                           cudaMemcpyDeviceToDevice, ctx->stream));
+            HCGB_CUDA(ctx, cudaMemcpyAsync(tmp->buf + (size_t) t.cols * t.max_rank, U,
+                                           sizeof(double) * (size_t) t.rows * rank, cudaMemcpyDeviceToDevice,
+                                           ctx->stream));
+        }
+    } else {
+        // new U (cols x rank, ld cols) = V^T, new V (rank x rows, ld rank) = U^T
+        launch_transpose(V, rank, rank, t.cols, tmp->buf, t.cols, ctx->stream);
+        launch_transpose(U, t.rows, t.rows, rank, tmp->buf + (size_t) t.cols * t.max_rank, rank, ctx->stream);
+    }
     out->data = tmp->buf;
     out->rank = t.rank;  // the rank itself is unchanged
     return HCGB_OK;
@@ -560,7 +573,7 @@ int transposed_tile(hcgb_context *ctx, const hcgb_tile &t, int rank, hcgb_tile *
 
 int read_rank(hcgb_context *ctx, const hcgb_tile &t, int *r) {
     *r = 0;
-    if (t.kind != HCGB_COMPRESSED) return HCGB_OK;
+    if (!compressed(t.kind)) return HCGB_OK;
     HCGB_CUDA(ctx, cudaMemcpyAsync(r, t.rank, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HCGB_OK;
@@ -596,7 +609,7 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
         return fail(ctx, HCGB_BAD_ARG, "hcgb_tile_gemm: shapes of op(A), op(B) and C do not match");
     }
     const size_t m = c->rows, n = c->cols, kd = A.cols;
-    const bool ak = A.kind == HCGB_COMPRESSED, bk = B.kind == HCGB_COMPRESSED, ck = c->kind == HCGB_COMPRESSED;
+    const bool ak = compressed(A.kind), bk = compressed(B.kind), ck = compressed(c->kind);
     unsigned long long fl = 0;
     int out_rank = 0;
     if (!ak && !bk && ck) {
@@ -624,7 +637,9 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
         std::memset(j, 0, sizeof(j));
         double *W = ws.base + ws.off_tmp2;
         const double *Cu = c->data, *Cv = c->data + m * (size_t) c->max_rank;
-        j[0] = GemmJob{Cu, Cv, W, (int) m, (int) n, rcank, (int) m, std::max(1, rcank), ws.ld, 0, 0, beta, 0.0};
+        const bool cvt = c->kind == HCGB_COMPRESSED_VT;  // Cv read as W^T (W: n x rank, ld n)
+        j[0] = GemmJob{Cu, Cv, W, (int) m, (int) n, rcank, (int) m, cvt ? (int) n : std::max(1, rcank), ws.ld,
+                       0, cvt ? 1 : 0, beta, 0.0};
         j[1] = GemmJob{A.data, B.data, W, (int) m, (int) n, (int) kd, (int) m, (int) kd, ws.ld, 0, 0, alpha, 1.0};
         if ((rc = ensure_stage(ctx, sizeof(j)))) {
             cleanup();
@@ -734,7 +749,7 @@ __global__ void identity_kernel(double *a, int n, int ld) {
 extern "C" int hcgb_compress_tile(hcgb_context *ctx, const double *dense, int rows, int cols, hcgb_tile *out,
                                   const hcgb_params *params, int *rank) {
     if (!ctx) return HCGB_BAD_ARG;
-    if (!dense || !out || rows <= 0 || cols <= 0 || out->kind != HCGB_COMPRESSED || out->rows != rows ||
+    if (!dense || !out || rows <= 0 || cols <= 0 || !compressed(out->kind) || out->rows != rows ||
         out->cols != cols || !out->rank || out->max_rank <= 0)
         return fail(ctx, HCGB_BAD_ARG, "hcgb_compress_tile: bad arguments");
     HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -807,6 +822,17 @@ extern "C" int hcgb_syrk(hcgb_context *ctx, int uplo, int trans, int n, int k, d
     HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
     if (n == 0) return HCGB_OK;
     launch_syrk(uplo, trans, n, k, alpha, A, lda, beta, C, ldc, ctx->stream);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_fill_triangle(hcgb_context *ctx, int uplo, int n, double *A, int lda, double value) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (!A || n < 0 || lda < (n > 1 ? n : 1) || (uplo != HCGB_LOWER && uplo != HCGB_UPPER))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_fill_triangle: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (n == 0) return HCGB_OK;
+    launch_fill_triangle(uplo, n, A, lda, value, ctx->stream);
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
 }

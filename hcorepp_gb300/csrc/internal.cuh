@@ -134,6 +134,7 @@ void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t
 void launch_transpose(const double *src, int lds, int rows, int cols, double *dst, int ldd, cudaStream_t st);
 
 // Dense tile building blocks of a tile Cholesky (chol.cu).
+void launch_fill_triangle(int uplo, int n, double *A, int lda, double value, cudaStream_t st);
 void launch_potrf(double *A, int n, int lda, int uplo, int *info_dev, cudaStream_t st);
 void launch_trsm(int side, int uplo, int trans, int diag, int m, int n, double alpha, const double *A, int lda,
                  double *B, int ldb, cudaStream_t st);

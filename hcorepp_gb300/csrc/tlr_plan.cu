@@ -75,15 +75,19 @@ __global__ void plan_kernel(const DevUpdate *ups, int n, double alpha, double be
     const double *Au = u.a.data, *Av = u.a.data + (size_t) u.a.rows * u.a.max_rank;
     const double *Bu = u.b.data, *Bv = u.b.data + (size_t) u.b.rows * u.b.max_rank;
     const double *Ad = u.a.data, *Bd = u.b.data;
+    // V factors as GEMM operands: V (rank x cols, ld rank), or for a compressed_vt tile the stored
+    // W = V^T (cols x rank, ld cols) read with the opposite op.
+    const int avt = ak == HCGB_COMPRESSED_VT, bvt = bk == HCGB_COMPRESSED_VT;
+    const int lav = avt ? u.a.cols : rA, lbv = bvt ? u.b.cols : rB;
 
     if (ck) {
         int side = 0, k = 0;
         if (ak && bk) {
             side = (p.side_mode && rB < rA) ? 1 : 0;
-            jobs[s] = make_job(Av, rA, 0, Bu, kd, 0, T1, lr, rA, rB, kd, 1.0, 0.0);  // T1 = Av Bu
+            jobs[s] = make_job(Av, lav, avt, Bu, kd, 0, T1, lr, rA, rB, kd, 1.0, 0.0);  // T1 = Av Bu
             if (side == 0) {
                 // V[:, rC:rC+rA] = (T1 Bv)^T = Bv^T T1^T   (ProcessVpointer's B part)
-                jobs[n + s] = make_job(Bv, rB, 1, T1, lr, 1, Vs + (size_t) rC * ld, ld, nn, rA, rB, 1.0, 0.0);
+                jobs[n + s] = make_job(Bv, lbv, !bvt, T1, lr, 1, Vs + (size_t) rC * ld, ld, nn, rA, rB, 1.0, 0.0);
                 k = rC + rA;
             } else {
                 // U[:, rC:rC+rB] = alpha Au T1
@@ -96,7 +100,7 @@ __global__ void plan_kernel(const DevUpdate *ups, int n, double alpha, double be
             k = rC + rB;
         } else {
             side = 0;  // CDC: U[:, rC:] = alpha Au, V[:, rC:] = (Av B)^T = B^T Av^T (HCore.cpp:246-257)
-            jobs[s] = make_job(Bd, kd, 1, Av, rA, 1, Vs + (size_t) rC * ld, ld, nn, rA, kd, 1.0, 0.0);
+            jobs[s] = make_job(Bd, kd, 1, Av, lav, !avt, Vs + (size_t) rC * ld, ld, nn, rA, kd, 1.0, 0.0);
             k = rC + rA;
         }
         if (k > ws.kmax) status = HCGB_POOL_TOO_SMALL;
@@ -113,20 +117,20 @@ __global__ void plan_kernel(const DevUpdate *ups, int n, double alpha, double be
     // Dense C: plain GEMM chains, C <- alpha * left * right + beta * C.
     double *C = u.c.data;
     if (ak && bk) {
-        jobs[s] = make_job(Av, rA, 0, Bu, kd, 0, T1, lr, rA, rB, kd, 1.0, 0.0);
+        jobs[s] = make_job(Av, lav, avt, Bu, kd, 0, T1, lr, rA, rB, kd, 1.0, 0.0);
         if (!p.side_mode || rA <= rB) {
             // HCore.cpp:178-264: T2 = T1 Bv, C = alpha Au T2 + beta C
-            jobs[n + s] = make_job(T1, lr, 0, Bv, rB, 0, T2, lr, rA, nn, rB, 1.0, 0.0);
+            jobs[n + s] = make_job(T1, lr, 0, Bv, lbv, bvt, T2, lr, rA, nn, rB, 1.0, 0.0);
             jobs[2 * n + s] = make_job(Au, m, 0, T2, lr, 0, C, m, m, nn, rA, alpha, beta);
         } else {
             jobs[n + s] = make_job(Au, m, 0, T1, lr, 0, T2, ld, m, rB, rA, 1.0, 0.0);
-            jobs[2 * n + s] = make_job(T2, ld, 0, Bv, rB, 0, C, m, m, nn, rB, alpha, beta);
+            jobs[2 * n + s] = make_job(T2, ld, 0, Bv, lbv, bvt, C, m, m, nn, rB, alpha, beta);
         }
     } else if (!ak && bk) {
         jobs[s] = make_job(Ad, m, 0, Bu, kd, 0, T2, ld, m, rB, kd, 1.0, 0.0);  // DCD
-        jobs[2 * n + s] = make_job(T2, ld, 0, Bv, rB, 0, C, m, m, nn, rB, alpha, beta);
+        jobs[2 * n + s] = make_job(T2, ld, 0, Bv, lbv, bvt, C, m, m, nn, rB, alpha, beta);
     } else if (ak && !bk) {
-        jobs[s] = make_job(Av, rA, 0, Bd, kd, 0, T2, lr, rA, nn, kd, 1.0, 0.0);  // CDD
+        jobs[s] = make_job(Av, lav, avt, Bd, kd, 0, T2, lr, rA, nn, kd, 1.0, 0.0);  // CDD
         jobs[2 * n + s] = make_job(Au, m, 0, T2, lr, 0, C, m, m, nn, rA, alpha, beta);
     } else {
         jobs[2 * n + s] = make_job(Ad, m, 0, Bd, kd, 0, C, m, m, nn, kd, alpha, beta);  // DDD
@@ -176,10 +180,13 @@ __global__ void __launch_bounds__(256) stack_kernel(const DevUpdate *ups, double
     const double *Cu = u.c.data, *Cv = u.c.data + (size_t) u.c.rows * u.c.max_rank;
     copy_scaled(Cu, m, m, rC, Us, ld, 1.0);                                      // U[:, :rC] = Cu
     if (side == 0 && u.a.kind) copy_scaled(u.a.data, m, m, rA, Us + (size_t) rC * ld, ld, alpha);  // alpha Au
-    transpose_scaled(Cv, rC, rC, nn, Vs, ld, beta, tile);                        // V[:, :rC] = beta Cv^T
+    // V[:, :rC] = beta Cv^T; a compressed_vt C stores Cv^T itself (ProcessVpointer's Cholesky copy)
+    if (u.c.kind == HCGB_COMPRESSED_VT) copy_scaled(Cv, nn, nn, rC, Vs, ld, beta);
+    else transpose_scaled(Cv, rC, rC, nn, Vs, ld, beta, tile);
     if (side == 1 && u.b.kind) {
         const double *Bv = u.b.data + (size_t) u.b.rows * u.b.max_rank;
-        transpose_scaled(Bv, rB, rB, nn, Vs + (size_t) rC * ld, ld, 1.0, tile);  // V[:, rC:] = Bv^T
+        if (u.b.kind == HCGB_COMPRESSED_VT) copy_scaled(Bv, nn, nn, rB, Vs + (size_t) rC * ld, ld, 1.0);
+        else transpose_scaled(Bv, rB, rB, nn, Vs + (size_t) rC * ld, ld, 1.0, tile);  // V[:, rC:] = Bv^T
     }
 }
 
@@ -295,7 +302,8 @@ __global__ void __launch_bounds__(256) finalize_kernel(const DevUpdate *ups, Wor
     const int r = meta[META_NEWRANK], nn = meta[META_N];
     const double *XV = ws.slot(s) + ws.off_xv;
     double *Cv = u.c.data + (size_t) u.c.rows * u.c.max_rank;
-    transpose_scaled(XV, ws.ld, nn, r, Cv, r, 1.0, tile);
+    if (u.c.kind == HCGB_COMPRESSED_VT) copy_scaled(XV, ws.ld, nn, r, Cv, nn, 1.0);  // W = XV (n x r, ld n)
+    else transpose_scaled(XV, ws.ld, nn, r, Cv, r, 1.0, tile);
     if (threadIdx.x == 0) *u.c.rank = r;
 }
 
@@ -310,8 +318,10 @@ __global__ void __launch_bounds__(256) ddc_finalize_kernel(const DevUpdate *ups,
     double *V = u.c.data + (size_t) m * u.c.max_rank;
     for (int j = 0; j < r; j++)
         for (int i = threadIdx.x; i < m; i += blockDim.x) U[i + (size_t) j * m] = W[i + (size_t) j * ws.ld];
-    for (int j = 0; j < nn; j++)
-        for (int i = threadIdx.x; i < r; i += blockDim.x) V[i + (size_t) j * r] = (i == j) ? 1.0 : 0.0;
+    // V = I (r x n, ld r); a compressed_vt C stores W = V^T (n x r, ld n), the same identity pattern.
+    const int vr = u.c.kind == HCGB_COMPRESSED_VT ? nn : r, vc = u.c.kind == HCGB_COMPRESSED_VT ? r : nn;
+    for (int j = 0; j < vc; j++)
+        for (int i = threadIdx.x; i < vr; i += blockDim.x) V[i + (size_t) j * vr] = (i == j) ? 1.0 : 0.0;
     if (threadIdx.x == 0) *u.c.rank = r;
 }
 

@@ -86,12 +86,18 @@ class CompressedTile:
     CompressedTile(rows, cols, u, v, rank) mirrors the (pointer, rank) constructor
     (Compressed.cpp:50-73): the capacity max_rank defaults to the rank, so the rank can
     never grow.  Pass max_rank to reserve room (the dense constructor uses min(m, n)/3).
+
+    ``vt=True`` marks a tile of a Cholesky flow, whose V region holds W = V^T (cols x rank, ld
+    cols) as HCore++'s Trsm, Syrk and Gemm(aCholesky = true) read it; the host accessors
+    (``v``, ``w``, ``to_dense``, ``set_factors``) follow the mark, and those calls pass it on.
     """
     kind = L.COMPRESSED
 
     def __init__(self, rows: int, cols: int, u=None, v=None, rank: int | None = None, max_rank: int | None = None,
-                 buffer: torch.Tensor | None = None, rank_buf: torch.Tensor | None = None, device="cuda"):
+                 buffer: torch.Tensor | None = None, rank_buf: torch.Tensor | None = None, device="cuda",
+                 vt: bool = False):
         self.rows, self.cols = rows, cols
+        self.vt = vt
         if rank is None:
             rank = np.asarray(u).shape[1]
         self.max_rank = max_rank if max_rank is not None else rank
@@ -122,6 +128,7 @@ class CompressedTile:
         return t
 
     def set_factors(self, u, v):
+        """Tile = u v (v: rank x cols); stored as W = v^T on a ``vt`` tile."""
         u = np.asarray(u, dtype=np.float64)
         v = np.asarray(v, dtype=np.float64)
         r = u.shape[1]
@@ -129,12 +136,13 @@ class CompressedTile:
             raise ValueError("rank exceeds the tile capacity")
         self.buffer[:self.rows * r].copy_(_fortran_flat(u))
         o = self.rows * self.max_rank
-        self.buffer[o:o + r * self.cols].copy_(_fortran_flat(v))
+        self.buffer[o:o + r * self.cols].copy_(_fortran_flat(v.T if self.vt else v))
         self.rank_buf.fill_(r)
 
-    def c_tile(self) -> L.Tile:
+    def c_tile(self, vt: bool | None = None) -> L.Tile:
+        vt = self.vt if vt is None else vt
         return L.Tile(self.buffer.data_ptr(), self.rank_buf.data_ptr(), self.rows, self.cols, self.max_rank,
-                      L.COMPRESSED)
+                      L.COMPRESSED_VT if vt else L.COMPRESSED)
 
     def GetTileRank(self) -> int:
         return int(self.rank_buf.item())
@@ -146,9 +154,16 @@ class CompressedTile:
         return self.buffer[:self.rows * r].cpu().numpy().reshape((self.rows, r), order="F")
 
     def v(self) -> np.ndarray:
-        r = self.rank
+        """V (rank x cols) of tile = U V."""
+        return self.w().T.copy() if self.vt else self._region(self.rank, self.cols)
+
+    def w(self) -> np.ndarray:
+        """W = V^T (cols x rank), the Cholesky-flow reading."""
+        return self._region(self.cols, self.rank) if self.vt else self.v().T.copy()
+
+    def _region(self, r, c) -> np.ndarray:
         o = self.rows * self.max_rank
-        return self.buffer[o:o + r * self.cols].cpu().numpy().reshape((r, self.cols), order="F")
+        return self.buffer[o:o + r * c].cpu().numpy().reshape((r, c), order="F")
 
     def to_dense(self) -> np.ndarray:
         return self.u() @ self.v()
@@ -161,10 +176,21 @@ class HCore:
     """HCore<double> (include/hcorepp/api/HCore.hpp:41-63)."""
 
     @staticmethod
-    def Gemm(alpha, a, a_op, b, b_op, beta, c, params: CompressionParameters = CompressionParameters(1e-9)):
-        """C = alpha op(A) op(B) + beta C; returns the reference's flop count for the update."""
+    def Gemm(alpha, a, a_op, b, b_op, beta, c, params: CompressionParameters = CompressionParameters(1e-9),
+             cholesky: bool = False):
+        """C = alpha op(A) op(B) + beta C; returns the reference's flop count for the update.
+
+        ``cholesky=True`` is the aCholesky branch (HCore.cpp:160-174, Compressed.cpp:273-276,
+        :529-595, :669-673): A, B and C compressed with their V regions read and written as W = V^T,
+        op(A) = NoTrans, op(B) = Trans.  The reference's branch produces no meaningful result for
+        any other combination, so the mirror rejects them."""
         ctx = run_context()
-        ta, tb, tc = a.c_tile(), b.c_tile(), c.c_tile()
+        if cholesky:
+            if not (a.kind == b.kind == c.kind == L.COMPRESSED) or a_op != L.NOTRANS or b_op != L.TRANS:
+                raise ValueError("Gemm(aCholesky): compressed A, B, C with opA = NoTrans, opB = Trans only")
+            ta, tb, tc = a.c_tile(vt=True), b.c_tile(vt=True), c.c_tile(vt=True)
+        else:
+            ta, tb, tc = a.c_tile(), b.c_tile(), c.c_tile()
         p = params.c()
         nr = C.c_int(0)
         fl = C.c_ulonglong(0)
@@ -224,25 +250,38 @@ def Trsm(side, uplo, trans, diag, alpha, a: DenseTile, b: CompressedTile):
 
 def Syrk(alpha, a, a_op, uplo, beta, c: DenseTile, params=None):
     """HCore<T>::Syrk (src/api/HCore.cpp:482-583) for a dense C.  Dense A: dsyrk on the uplo
-    triangle.  Compressed A = U V: C <- beta C - U (V V^T) U^T (the reference hard-codes -1 there),
-    then the other triangle is set to zero (FillMatrixTriangle, HCore.cpp:555-563)."""
+    triangle.  Compressed A, its V region read as W (cols x rank, ld cols) so that A = U W^T:
+    C <- beta C - U (W^T W) U^T (the reference hard-codes -1 there), then the other strict triangle
+    is set to zero (FillMatrixTriangle, HCore.cpp:555-563)."""
     if c.kind != L.DENSE:
         raise NotImplementedError("Syrk into a compressed C is not provided")
     n = c.rows
     if a.kind == L.DENSE:
         Blas.syrk(uplo, a_op, n, c.cols, alpha, a.buffer, a.rows, beta, c.buffer, n)
         return
-    HCore.Gemm(-1.0, a, L.NOTRANS, a, L.TRANS, beta, c, params or CompressionParameters(1e-9))
-    m = c.buffer.view(n, n).t()  # column-major view: m[i, j] = C(i, j)
-    mask = torch.triu(torch.ones(n, n, dtype=torch.bool, device=m.device), 1)
-    m.masked_fill_(mask if uplo == L.LOWER else mask.t(), 0.0)
+    # A = U W^T (Cholesky-flow reading, HCore.cpp:512-545): C <- beta C - A A^T
+    ctx = run_context()
+    ta, tc = a.c_tile(vt=True), c.c_tile()
+    p = (params or CompressionParameters(1e-9)).c()
+    ctx.check(L.lib().hcgb_tile_gemm(ctx.handle, -1.0, C.byref(ta), L.NOTRANS, C.byref(ta), L.TRANS, float(beta),
+                                     C.byref(tc), C.byref(p), None, None), allow=(L.HCGB_OK, L.HCGB_NOT_CONVERGED))
+    other = L.UPPER if uplo == L.LOWER else L.LOWER
+    ctx.check(L.lib().hcgb_fill_triangle(ctx.handle, other, n, _dptr(c.buffer), n, 0.0))
 
 
 def tile_cholesky(a: "TileMatrix", params: CompressionParameters) -> int:
-    """Right-looking tile Cholesky A = L L^T of a symmetric positive definite tile matrix with dense
-    diagonal tiles and compressed tiles below the diagonal (tiles above are not referenced).
-    The reference provides the per-tile operations (Potrf, Trsm, Syrk, Gemm) but no driver.
-    Returns 0, or the potrf info of the first failing diagonal tile (as k*nb + info)."""
+    """Right-looking tile Cholesky A = L L^T of a symmetric positive definite tile matrix: dense
+    diagonal tiles, compressed tiles below the diagonal in the Cholesky-flow layout (TileMatrix with
+    ``vt=True``: tile = U W^T), tiles above the diagonal not referenced.  The reference provides the
+    per-tile operations but no driver; this loop composes them:
+      Potrf(A_kk, Lower)                                                  HCore.cpp:585-621
+      Trsm(Left, Lower, NoTrans, NonUnit, 1, A_kk, A_ik): W_ik <- L_kk^-1 W_ik   HCore.cpp:623-647
+      Syrk(-1, A_ik, NoTrans, Lower, 1, A_ii)                             HCore.cpp:482-583
+      Gemm(-1, A_ik, NoTrans, A_jk, Trans, 1, A_ij, aCholesky = true)     HCore.cpp:23-344
+    One call per tile operation, each a GPU kernel sequence on the context stream.
+    Returns 0, or k * nb + info of the first failing diagonal tile."""
+    if not a.vt:
+        raise ValueError("tile_cholesky needs a TileMatrix in the Cholesky-flow layout (vt=True)")
     nt, nb = a.mt, a.nb
     for k in range(nt):
         akk = a.tile(k, k)
@@ -250,16 +289,12 @@ def tile_cholesky(a: "TileMatrix", params: CompressionParameters) -> int:
         if info:
             return k * nb + info
         for i in range(k + 1, nt):
-            # A_ik <- A_ik L_kk^-T on the V factor: V <- V L_kk^-T (rank x nb, ld rank)
-            aik = a.tile(i, k)
-            r = aik.rank
-            v = aik.buffer[nb * aik.max_rank:]
-            Blas.trsm(L.RIGHT, L.LOWER, L.TRANS, L.NONUNIT, r, nb, 1.0, akk.buffer, nb, v, max(r, 1))
+            Trsm(L.LEFT, L.LOWER, L.NOTRANS, L.NONUNIT, 1.0, akk, a.tile(i, k))
         for i in range(k + 1, nt):
             aik = a.tile(i, k)
-            HCore.Gemm(-1.0, aik, L.NOTRANS, aik, L.TRANS, 1.0, a.tile(i, i), params)
+            Syrk(-1.0, aik, L.NOTRANS, L.LOWER, 1.0, a.tile(i, i), params)
             for j in range(k + 1, i):
-                HCore.Gemm(-1.0, aik, L.NOTRANS, a.tile(j, k), L.TRANS, 1.0, a.tile(i, j), params)
+                HCore.Gemm(-1.0, aik, L.NOTRANS, a.tile(j, k), L.TRANS, 1.0, a.tile(i, j), params, cholesky=True)
     return 0
 
 
@@ -268,10 +303,12 @@ class TileMatrix:
 
     ``kinds[i][j]`` is DENSE or COMPRESSED; compressed tiles get capacity ``max_rank``.
     Ranks live in one device int array (``ranks``), so a whole multiply runs without the host.
+    ``vt=True`` lays the compressed tiles out for a Cholesky flow (V region = W = V^T).
     """
 
-    def __init__(self, mt: int, nt: int, nb: int, kinds, max_rank: int, device="cuda"):
+    def __init__(self, mt: int, nt: int, nb: int, kinds, max_rank: int, device="cuda", vt: bool = False):
         self.mt, self.nt, self.nb, self.max_rank = mt, nt, nb, max_rank
+        self.vt = vt
         self.kinds = [[kinds[i][j] for j in range(nt)] for i in range(mt)]
         sizes = []
         for j in range(nt):
@@ -294,7 +331,7 @@ class TileMatrix:
         if self.kinds[i][j] == L.DENSE:
             return DenseTile(nb, nb, buffer=self._view(i, j))
         return CompressedTile(nb, nb, rank=0, max_rank=self.max_rank, buffer=self._view(i, j),
-                              rank_buf=self.ranks[idx:idx + 1])
+                              rank_buf=self.ranks[idx:idx + 1], vt=self.vt)
 
     def c_grid(self):
         nb = self.nb
@@ -308,7 +345,8 @@ class TileMatrix:
                 if self.kinds[i][j] == L.DENSE:
                     arr[idx] = L.Tile(ptr, None, nb, nb, 0, L.DENSE)
                 else:
-                    arr[idx] = L.Tile(ptr, rbase + 4 * idx, nb, nb, self.max_rank, L.COMPRESSED)
+                    arr[idx] = L.Tile(ptr, rbase + 4 * idx, nb, nb, self.max_rank,
+                                      L.COMPRESSED_VT if self.vt else L.COMPRESSED)
         return arr
 
     def set_tile(self, i, j, dense=None, u=None, v=None):
@@ -332,7 +370,8 @@ class TileMatrix:
                 else:
                     r = int(ranks[idx])
                     u = seg[:nb * r].reshape((nb, r), order="F")
-                    v = seg[nb * self.max_rank:nb * self.max_rank + r * nb].reshape((r, nb), order="F")
+                    vreg = seg[nb * self.max_rank:nb * self.max_rank + r * nb]
+                    v = vreg.reshape((nb, r), order="F").T if self.vt else vreg.reshape((r, nb), order="F")
                     blk = u @ v
                 out[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb] = blk
         return out

@@ -12,6 +12,12 @@
  *                (DenseTile, include/hcorepp/operators/concrete/Dense.hpp:90-91)
  *   compressed : [U: rows x max_rank (ld rows) | V: max_rank x cols (ld = rank)]
  *                (CompressedTile, src/operators/concrete/Compressed.cpp:50-73, :176-185)
+ *   compressed_vt (HCore++'s Cholesky-flow reading of the same buffer):
+ *                [U: rows x max_rank (ld rows) | W: cols x rank (ld cols)], tile = U W^T.
+ *                HCore<T>::Trsm solves on W (src/api/HCore.cpp:636-640), HCore<T>::Syrk forms
+ *                U (W^T W) U^T (:512-545), and Gemm's aCholesky branch reads and writes W
+ *                (src/api/HCore.cpp:160-174, src/operators/concrete/Compressed.cpp:273-276,
+ *                :529-595, :669-673, ProcessVpointer's Cholesky copies omp/kernels.cpp:35-56).
  * A compressed tile's rank lives in a device int so that batched calls never need the host.
  */
 #ifndef HCGB_H
@@ -34,7 +40,7 @@ typedef enum {
     HCGB_UNSUPPORTED = 6      /* combination not available on this entry point */
 } hcgb_status;
 
-typedef enum { HCGB_DENSE = 0, HCGB_COMPRESSED = 1 } hcgb_tile_kind;
+typedef enum { HCGB_DENSE = 0, HCGB_COMPRESSED = 1, HCGB_COMPRESSED_VT = 2 } hcgb_tile_kind;
 typedef enum { HCGB_NOTRANS = 0, HCGB_TRANS = 1 } hcgb_op;
 typedef enum { HCGB_GESVD = 0, HCGB_GESDD = 1 } hcgb_svd_type;
 
@@ -119,7 +125,8 @@ size_t hcgb_workspace_bytes(int n, int max_rows, int max_cols, int max_rank_c, i
  * Replaces n calls of HCore<T>::Gemm (src/api/HCore.cpp:23-344) with NoTrans operands.
  * Ranks are read and written on the device; nothing is synchronised with the host.
  * info_dev (optional, device, n records) receives a per-update hcgb_update_info.
- * Supported combinations: CCC, DCC, CDC, CCD, DCD, CDD, DDD (DDC: hcgb_tile_gemm). */
+ * Supported combinations: CCC, DCC, CDC, CCD, DCD, CDD, DDD (DDC: hcgb_tile_gemm).  Any compressed
+ * operand may be HCGB_COMPRESSED_VT; a compressed_vt C is written back in that layout. */
 int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const hcgb_update *updates,
                     const hcgb_params *params, hcgb_update_info *info_dev);
 
@@ -149,6 +156,8 @@ int hcgb_set_k_order(hcgb_context *ctx, int policy);
  * updated; *new_rank (if not NULL) receives it on the host, like CompressedTile::Gemm updating
  * mRank (src/operators/concrete/Compressed.cpp:656-662).  The DDC combination rewrites C at full
  * rank with an identity V (HCore.cpp:272-299) and needs max_rank >= min(rows, cols).
+ * HCore<T>::Gemm(..., aCholesky = true) is this call with A, B and C given as HCGB_COMPRESSED_VT
+ * and op_b = HCGB_TRANS (the one combination the reference's Cholesky branch handles).
  * flops (if not NULL) is incremented by the reference's count for the update. */
 int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *a, int op_a, const hcgb_tile *b, int op_b,
                    double beta, hcgb_tile *c, const hcgb_params *params, int *new_rank,
@@ -181,6 +190,10 @@ int hcgb_trsm(hcgb_context *ctx, int side, int uplo, int trans, int diag, int m,
  * semantics; replaces HCoreKernels::syrk (src/kernels/cuda/kernels.cpp:299-306).  Asynchronous. */
 int hcgb_syrk(hcgb_context *ctx, int uplo, int trans, int n, int k, double alpha, const double *A, int lda,
               double beta, double *C, int ldc);
+/* Sets the strict uplo triangle of A (n x n, ld lda) to value; replaces
+ * HCoreKernels::FillMatrixTriangle (src/kernels/omp/kernels.cpp:246-264), which HCore<T>::Syrk
+ * applies after a compressed-A update (src/api/HCore.cpp:555-563).  Asynchronous. */
+int hcgb_fill_triangle(hcgb_context *ctx, int uplo, int n, double *A, int lda, double value);
 
 /* Stage timing with CUDA events on the context stream (the GB300 replacement of the reference's
  * DebuggingTimer snapshots, src/helpers/debugging-timer/ActiveTimer.cpp:47-60).  While enabled,

@@ -9,6 +9,7 @@
 //   hcorepp::kernels::RunContext               include/hcorepp/kernels/cuda/RunContext.hpp:15-53
 //   hcorepp::dataunits::MemoryUnit             include/hcorepp/data-units/memory-handlers/pool/MemoryHandler.hpp:22-157
 //   hcorepp::api::HCore<T>::Gemm               include/hcorepp/api/HCore.hpp:41-63
+//   hcorepp::api::HCore<T>::Syrk/Potrf/Trsm    include/hcorepp/api/HCore.hpp:65-112 (src/api/HCore.cpp:482-647)
 // Tile buffers live on the device (as in the reference's CUDA build); constructors accept host or
 // device pointers (cudaMemcpyDefault).  Errors throw std::runtime_error / std::invalid_argument as
 // the reference does.  The GPU path computes in double precision: T = double.
@@ -30,6 +31,9 @@
 namespace blas {
 enum class Layout : char { ColMajor = 'C', RowMajor = 'R' };
 enum class Op : char { NoTrans = 'N', Trans = 'T', ConjTrans = 'C' };
+enum class Uplo : char { Upper = 'U', Lower = 'L', General = 'G' };
+enum class Side : char { Left = 'L', Right = 'R' };
+enum class Diag : char { NonUnit = 'N', Unit = 'U' };
 }  // namespace blas
 #endif
 
@@ -249,6 +253,12 @@ public:
     hcgb_tile c_tile() const override {
         return hcgb_tile{mData, mRank, (int) this->mRows, (int) this->mCols, (int) mMaxRank, HCGB_COMPRESSED};
     }
+    // The Cholesky-flow reading of the same buffer: V region = W = V^T (cols x rank, ld cols).
+    hcgb_tile c_tile_vt() const {
+        hcgb_tile t = c_tile();
+        t.kind = HCGB_COMPRESSED_VT;
+        return t;
+    }
     // Room for the full-rank form a DDC update produces (HCore.cpp:294-298 re-sizes the tile the
     // same way): grow the buffer to rank min(rows, cols), keeping U and V in place.
     void EnsureFullRankCapacity() {
@@ -300,11 +310,22 @@ public:
                      const blas::Op &aBOp, T aBeta, operators::Tile<T> &aC, const kernels::RunContext &aContext,
                      size_t &aFlops, dataunits::MemoryUnit<T> &aMemoryUnit,
                      const operators::CompressionParameters &aParameters = {1e-9}, bool aCholesky = false) {
-        if (aCholesky) throw std::invalid_argument("HCore::Gemm: the Cholesky variant is not provided on this path");
-        // The DDC combination re-sets C at full rank: make room first.
-        const bool ddc = aA.isDense() && aB.isDense() && aC.isCompressed();
-        if (ddc) static_cast<operators::CompressedTile<T> &>(aC).EnsureFullRankCapacity();
         hcgb_tile a = aA.c_tile(), b = aB.c_tile(), c = aC.c_tile();
+        if (aCholesky) {
+            // The aCholesky branch (HCore.cpp:160-174, Compressed.cpp:273-276, :529-595, :669-673):
+            // compressed A, B, C whose V regions hold W = V^T, op(A) = NoTrans, op(B) = Trans.  The
+            // reference's branch gives no meaningful result for other combinations; they are rejected.
+            if (!aA.isCompressed() || !aB.isCompressed() || !aC.isCompressed() || aAOp != blas::Op::NoTrans ||
+                aBOp == blas::Op::NoTrans)
+                throw std::invalid_argument("HCore::Gemm(aCholesky): compressed A, B, C with NoTrans, Trans only");
+            a = static_cast<const operators::CompressedTile<T> &>(aA).c_tile_vt();
+            b = static_cast<const operators::CompressedTile<T> &>(aB).c_tile_vt();
+            c = static_cast<operators::CompressedTile<T> &>(aC).c_tile_vt();
+        } else if (aA.isDense() && aB.isDense() && aC.isCompressed()) {
+            // The DDC combination re-sets C at full rank: make room first.
+            static_cast<operators::CompressedTile<T> &>(aC).EnsureFullRankCapacity();
+            c = aC.c_tile();
+        }
         hcgb_params p = aParameters.c_params();
         int r = 0;
         unsigned long long fl = 0;
@@ -315,14 +336,70 @@ public:
         aFlops += (size_t) fl;
     }
 
+    // Syrk (HCore.cpp:482-583) into a dense C.  Dense A: dsyrk(uplo, op, n, k = C.cols) on the uplo
+    // triangle.  Compressed A read as U W^T: C <- beta C - A A^T (the reference uses -1, not alpha),
+    // then the opposite strict triangle is set to zero (FillMatrixTriangle).
+    static void Syrk(T aAlpha, const operators::Tile<T> &aA, const blas::Op &aAOp, blas::Uplo aUplo, T aBeta,
+                     operators::Tile<T> &aC, const kernels::RunContext &aContext, size_t &aFlops,
+                     dataunits::MemoryUnit<T> &aMemoryUnit) {
+        if (!aC.isDense()) throw std::invalid_argument("HCore::Syrk: C must be dense");
+        hcgb_tile c = aC.c_tile();
+        const int lo = aUplo == blas::Uplo::Upper ? HCGB_UPPER : HCGB_LOWER;
+        if (aA.isDense()) {
+            hcgb_tile a = aA.c_tile();
+            const int op = aAOp == blas::Op::NoTrans ? HCGB_NOTRANS : HCGB_TRANS;
+            detail::check(hcgb_syrk(aContext.handle(), lo, op, c.rows, c.cols, aAlpha, a.data, a.rows, aBeta, c.data,
+                                    c.rows),
+                          aContext.handle(), "HCore::Syrk");
+            return;
+        }
+        hcgb_tile a = static_cast<const operators::CompressedTile<T> &>(aA).c_tile_vt();
+        hcgb_params p = operators::CompressionParameters(1e-9).c_params();
+        unsigned long long fl = 0;
+        detail::check(hcgb_tile_gemm(aContext.handle(), -1.0, &a, HCGB_NOTRANS, &a, HCGB_TRANS, aBeta, &c, &p,
+                                     nullptr, &fl),
+                      aContext.handle(), "HCore::Syrk");
+        detail::check(hcgb_fill_triangle(aContext.handle(), lo == HCGB_LOWER ? HCGB_UPPER : HCGB_LOWER, c.rows,
+                                         c.data, c.rows, 0.0),
+                      aContext.handle(), "HCore::Syrk");
+        aFlops += (size_t) fl;
+    }
+
+    // Potrf (HCore.cpp:585-621): dense tiles only; dpotrf semantics on the uplo triangle.
+    static void Potrf(operators::Tile<T> &aA, blas::Uplo aUplo, const kernels::RunContext &aContext,
+                      size_t &aFlops, dataunits::MemoryUnit<T> &aMemoryUnit) {
+        if (aA.GetNumOfSubMatrices() != 1) throw std::runtime_error(" Potrf works only with dense tiles");
+        hcgb_tile a = aA.c_tile();
+        int info = 0;
+        detail::check(hcgb_potrf(aContext.handle(), aUplo == blas::Uplo::Upper ? HCGB_UPPER : HCGB_LOWER, a.rows,
+                                 a.data, a.rows, &info),
+                      aContext.handle(), "HCore::Potrf");
+    }
+
+    // Trsm (HCore.cpp:623-647): B compressed; the solve runs on its V region read as rows x rank
+    // (ld rows), i.e. on W of the Cholesky-flow layout.
+    static void Trsm(blas::Side aSide, blas::Uplo aUplo, blas::Op aTrans, blas::Diag aDiag, T aAlpha,
+                     operators::Tile<T> &aA, operators::Tile<T> &aB, const kernels::RunContext &aContext,
+                     size_t &aFlops, dataunits::MemoryUnit<T> &aMemoryHandler) {
+        if (aB.GetNumOfSubMatrices() != 2) throw std::runtime_error(" TRSM: Tile B must be compressed ");
+        auto &b = static_cast<operators::CompressedTile<T> &>(aB);
+        hcgb_tile a = aA.c_tile();
+        detail::check(hcgb_trsm(aContext.handle(), aSide == blas::Side::Right ? HCGB_RIGHT : HCGB_LEFT,
+                                aUplo == blas::Uplo::Upper ? HCGB_UPPER : HCGB_LOWER,
+                                aTrans == blas::Op::NoTrans ? HCGB_NOTRANS : HCGB_TRANS,
+                                aDiag == blas::Diag::Unit ? HCGB_UNIT : HCGB_NONUNIT, (int) b.GetNumOfRows(),
+                                (int) b.GetTileRank(), aAlpha, a.data, a.rows, b.GetVMatrix(), (int) b.GetNumOfRows()),
+                      aContext.handle(), "HCore::Trsm");
+    }
+
     // Scratch the library needs for one update of these tiles (HCore.cpp:417-480), in elements of T.
     static size_t CalculateMemoryPoolSize(const operators::Tile<T> &aA, const operators::Tile<T> &aB,
                                           const operators::Tile<T> &aC, operators::CompressionParameters,
                                           const kernels::RunContext &) {
         hcgb_tile a = aA.c_tile(), b = aB.c_tile(), c = aC.c_tile();
-        const int rab = std::max(a.kind == HCGB_COMPRESSED ? a.max_rank : 0, b.kind == HCGB_COMPRESSED ? b.max_rank : 0);
+        const int rab = std::max(a.kind != HCGB_DENSE ? a.max_rank : 0, b.kind != HCGB_DENSE ? b.max_rank : 0);
         return hcgb_workspace_bytes(1, (int) std::max(c.rows, a.cols), c.cols,
-                                    c.kind == HCGB_COMPRESSED ? c.max_rank : 0, rab) / sizeof(T);
+                                    c.kind != HCGB_DENSE ? c.max_rank : 0, rab) / sizeof(T);
     }
 };
 

@@ -319,8 +319,11 @@ def potrf_lower(a: np.ndarray):
 
 
 def trsm(side_left: bool, lower: bool, trans: bool, unit: bool, alpha: float, a: np.ndarray, b: np.ndarray):
-    """BLAS dtrsm: op(A) X = alpha B (left) or X op(A) = alpha B (right)."""
+    """BLAS dtrsm: op(A) X = alpha B (left) or X op(A) = alpha B (right).  Like dtrsm, only the
+    leading order-m (left) or order-n (right) block of A is referenced."""
     import scipy.linalg as sl
+    k = b.shape[0] if side_left else b.shape[1]
+    a = np.asarray(a)[:k, :k]
     t = np.tril(a) if lower else np.triu(a)
     if unit:
         t = t - np.diag(np.diag(t)) + np.eye(t.shape[0])
@@ -330,32 +333,96 @@ def trsm(side_left: bool, lower: bool, trans: bool, unit: bool, alpha: float, a:
     return sl.solve_triangular(opt.T, alpha * b.T, lower=not (lower != trans)).T
 
 
-def hcore_trsm_compressed(side_left, lower, trans, unit, alpha, a: np.ndarray, b: "CompressedTile") -> None:
-    """HCore<T>::Trsm (HCore.cpp:623-647): trsm on the V buffer viewed as rows x rank (ld rows)."""
+def hcore_trsm_compressed(side_left, lower, trans, unit, alpha, a: np.ndarray, b) -> None:
+    """HCore<T>::Trsm (HCore.cpp:623-647): trsm on the V buffer viewed as rows x rank (ld rows).
+    Works on the flat buffer, so it serves a CompressedTile (b.v = V, rank x cols) and a
+    CholeskyTile (b.w = W, cols x rank) alike; the buffer keeps its shape."""
+    attr = "w" if isinstance(b, CholeskyTile) else "v"
+    cur = getattr(b, attr)
     rows, r = b.rows, b.rank
-    flat = b.v.ravel(order="F").copy()
-    x = flat.reshape((rows, r), order="F")
+    x = cur.ravel(order="F").copy().reshape((rows, r), order="F")
     x = trsm(side_left, lower, trans, unit, alpha, a, x)
-    b.v = np.asfortranarray(x.ravel(order="F").reshape((r, b.cols), order="F"))
+    setattr(b, attr, np.asfortranarray(x.ravel(order="F").reshape(cur.shape, order="F")))
+
+
+class CholeskyTile:
+    """A compressed tile as HCore++'s Cholesky routines read its buffer: U (rows x rank) and
+    W (cols x rank, ld cols), tile = U W^T (HCore.cpp:512-545 Syrk, :636-640 Trsm, and the
+    aCholesky branch of Gemm, HCore.cpp:160-174, Compressed.cpp:529-595, :669-673)."""
+    kind = "compressed"
+
+    def __init__(self, u: np.ndarray, w: np.ndarray, max_rank: int | None = None):
+        self.u = np.array(u, dtype=np.float64, order="F")
+        self.w = np.array(w, dtype=np.float64, order="F")
+        self.max_rank = self.rank if max_rank is None else max_rank
+
+    @property
+    def rows(self):
+        return self.u.shape[0]
+
+    @property
+    def cols(self):
+        return self.w.shape[0]
+
+    @property
+    def rank(self):
+        return self.u.shape[1]
+
+    def to_dense(self) -> np.ndarray:
+        return self.u @ self.w.T
+
+
+def hcore_syrk(alpha: float, a, uplo_lower: bool, beta: float, c: DenseTile) -> None:
+    """HCore<T>::Syrk (HCore.cpp:482-583) into a dense C.
+    Compressed A = U W^T: C <- beta C - U (W^T W) U^T over the whole tile (the reference uses -1,
+    not alpha), then the opposite strict triangle is set to zero (FillMatrixTriangle,
+    omp/kernels.cpp:246-264).  Dense A: dsyrk(uplo, NoTrans, n, k = C.cols) on the uplo triangle."""
+    if isinstance(a, CholeskyTile):
+        prod = (a.u @ (a.w.T @ a.w)) @ a.u.T
+        out = beta * c.data - prod
+        mask = np.triu(np.ones_like(out, dtype=bool), 1)
+        out[mask if uplo_lower else mask.T] = 0.0
+        c.data = np.asfortranarray(out)
+        return
+    tri = np.tril if uplo_lower else np.triu
+    full = alpha * (a.data @ a.data.T) + beta * c.data
+    c.data = np.asfortranarray(np.where(tri(np.ones_like(full)) > 0, full, c.data))
+
+
+def hcore_gemm_cholesky(alpha: float, a: CholeskyTile, b: CholeskyTile, beta: float, c: CholeskyTile,
+                        params: CompressionParameters) -> dict:
+    """HCore<T>::Gemm(alpha, A, NoTrans, B, Trans, beta, C, ..., aCholesky = true) for compressed A, B
+    and C (HCore.cpp:160-174; Compressed.cpp:273-276, :468-476, :529-595, :669-673).
+    The branch forms T2 = (U_B W_B^T) W_A and recompresses U = [U_C | alpha U_A], W = [beta W_C | T2],
+    i.e. alpha A B^T + beta C, with Sigma kept on the W side and every V factor read and written as
+    W = V^T.  Restated through the plain recompression on the transposed views
+    A = (U_A, W_A^T), B^T = (W_B, U_B^T), C = (U_C, W_C^T)."""
+    ca = CompressedTile(a.u, a.w.T, a.max_rank)
+    cb = CompressedTile(b.w, b.u.T, b.max_rank)
+    cc = CompressedTile(c.u, c.w.T, c.max_rank)
+    info = hcore_gemm(alpha, ca, cb, beta, cc, params)
+    c.u, c.w = np.asfortranarray(cc.u), np.asfortranarray(cc.v.T)
+    return info
 
 
 def tile_cholesky(a_tiles, nt, params) -> int:
-    """Right-looking tile Cholesky on a grid of oracle tiles (dense diagonal, compressed below)."""
+    """Right-looking tile Cholesky A = L L^T composed of the reference's per-tile operations (the
+    reference itself has no driver): dense diagonal tiles, CholeskyTile tiles below the diagonal.
+      Potrf(A_kk, Lower)                                       HCore.cpp:585-621
+      Trsm(Left, Lower, NoTrans, NonUnit, 1, A_kk, A_ik):  W_ik <- L_kk^-1 W_ik   HCore.cpp:623-647
+      Syrk(-1, A_ik, NoTrans, Lower, 1, A_ii)                  HCore.cpp:482-583
+      Gemm(-1, A_ik, NoTrans, A_jk, Trans, 1, A_ij, aCholesky = true)   HCore.cpp:23-344
+    Returns 0, or k * nb + info of the first failing diagonal tile."""
     for k in range(nt):
         c, info = potrf_lower(a_tiles[k][k].data)
         if info:
             return k * a_tiles[k][k].rows + info
-        lkk = np.tril(c)
         a_tiles[k][k].data = np.asfortranarray(np.where(np.tril(np.ones_like(c)) > 0, c, a_tiles[k][k].data))
+        lkk = np.tril(c)
         for i in range(k + 1, nt):
-            t = a_tiles[i][k]
-            t.v = np.asfortranarray(trsm(False, True, True, False, 1.0, lkk, t.v))
+            hcore_trsm_compressed(True, True, False, False, 1.0, lkk, a_tiles[i][k])
         for i in range(k + 1, nt):
-            aik = a_tiles[i][k]
-            d = a_tiles[i][i]
-            d.data = np.asfortranarray(d.data - aik.to_dense() @ aik.to_dense().T)
+            hcore_syrk(-1.0, a_tiles[i][k], True, 1.0, a_tiles[i][i])
             for j in range(k + 1, i):
-                ajk = a_tiles[j][k]
-                hcore_gemm(-1.0, CompressedTile(aik.u, aik.v), CompressedTile(ajk.v.T, ajk.u.T), 1.0, a_tiles[i][j],
-                           params)
+                hcore_gemm_cholesky(-1.0, a_tiles[i][k], a_tiles[j][k], 1.0, a_tiles[i][j], params)
     return 0

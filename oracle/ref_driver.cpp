@@ -93,6 +93,77 @@ int hcref_tile_gemm(double alpha, int a_kind, int am, int an, int a_rank, int a_
     }
 }
 
+// HCore<double>::Gemm with explicit operand ops and the aCholesky flag (HCore.cpp:23-344).
+int hcref_tile_gemm_ops(double alpha, int a_kind, int am, int an, int a_rank, int a_max_rank, double *a_data,
+                        int op_a, int b_kind, int bm, int bn, int b_rank, int b_max_rank, double *b_data, int op_b,
+                        double beta, int c_kind, int cm, int cn, int *c_rank, int c_max_rank, double *c_data,
+                        double acc, int truncated, int fixed_rank, int op_type, int cholesky) {
+    try {
+        auto &ctx = kernels::ContextManager::GetInstance().GetContext();
+        auto a = wrap_tile(a_kind, am, an, a_rank, a_max_rank, a_data, ctx);
+        auto b = wrap_tile(b_kind, bm, bn, b_rank, b_max_rank, b_data, ctx);
+        auto c = wrap_tile(c_kind, cm, cn, *c_rank, c_max_rank, c_data, ctx);
+        auto &mh = dataunits::MemoryHandler<double>::GetInstance();
+        size_t fl = 0;
+        api::HCore<double>::Gemm(alpha, *a, op_a ? blas::Op::Trans : blas::Op::NoTrans, *b,
+                                 op_b ? blas::Op::Trans : blas::Op::NoTrans, beta, *c, ctx, fl, mh.GetMemoryUnit(),
+                                 make_params(acc, truncated, fixed_rank, op_type), cholesky != 0);
+        if (c_kind != 0) *c_rank = (int) c->GetTileRank();
+        return 0;
+    } catch (const std::exception &) {
+        return -1;
+    }
+}
+
+// HCore<double>::Potrf on a dense n x n tile (HCore.cpp:585-621).
+int hcref_potrf(int uplo, int n, double *a_data) {
+    try {
+        auto &ctx = kernels::ContextManager::GetInstance().GetContext();
+        auto a = wrap_tile(0, n, n, 0, 0, a_data, ctx);
+        auto &mh = dataunits::MemoryHandler<double>::GetInstance();
+        size_t fl = 0;
+        api::HCore<double>::Potrf(*a, uplo ? blas::Uplo::Upper : blas::Uplo::Lower, ctx, fl, mh.GetMemoryUnit());
+        return 0;
+    } catch (const std::exception &) {
+        return -1;
+    }
+}
+
+// HCore<double>::Trsm with a dense n x n A and a compressed B (HCore.cpp:623-647).
+int hcref_trsm(int side, int uplo, int trans, int diag, double alpha, int n, double *a_data, int bm, int bn,
+               int b_rank, int b_max_rank, double *b_data) {
+    try {
+        auto &ctx = kernels::ContextManager::GetInstance().GetContext();
+        auto a = wrap_tile(0, n, n, 0, 0, a_data, ctx);
+        auto b = wrap_tile(1, bm, bn, b_rank, b_max_rank, b_data, ctx);
+        auto &mh = dataunits::MemoryHandler<double>::GetInstance();
+        size_t fl = 0;
+        api::HCore<double>::Trsm(side ? blas::Side::Right : blas::Side::Left, uplo ? blas::Uplo::Upper : blas::Uplo::Lower,
+                                 trans ? blas::Op::Trans : blas::Op::NoTrans, diag ? blas::Diag::Unit : blas::Diag::NonUnit,
+                                 alpha, *a, *b, ctx, fl, mh.GetMemoryUnit());
+        return 0;
+    } catch (const std::exception &) {
+        return -1;
+    }
+}
+
+// HCore<double>::Syrk into a dense C (HCore.cpp:482-583); A dense (a_kind 0) or compressed (1).
+int hcref_syrk(double alpha, int a_kind, int am, int an, int a_rank, int a_max_rank, double *a_data, int op_a,
+               int uplo, double beta, int cm, int cn, double *c_data) {
+    try {
+        auto &ctx = kernels::ContextManager::GetInstance().GetContext();
+        auto a = wrap_tile(a_kind, am, an, a_rank, a_max_rank, a_data, ctx);
+        auto c = wrap_tile(0, cm, cn, 0, 0, c_data, ctx);
+        auto &mh = dataunits::MemoryHandler<double>::GetInstance();
+        size_t fl = 0;
+        api::HCore<double>::Syrk(alpha, *a, op_a ? blas::Op::Trans : blas::Op::NoTrans,
+                                 uplo ? blas::Uplo::Upper : blas::Uplo::Lower, beta, *c, ctx, fl, mh.GetMemoryUnit());
+        return 0;
+    } catch (const std::exception &) {
+        return -1;
+    }
+}
+
 // Tile-matrix multiply C += A*B in the style of examples/matrix_multiplication/omp_main.cpp:112-124:
 // OpenMP over the listed C tiles, k ascending per C tile, one memory unit per thread.
 // Tile (i, j) of an nt x nt grid is entry i + j*nt of the kind/rank/maxrank/pointer arrays.

@@ -37,6 +37,17 @@ def lib():
                                      + [ip, ip, ip, C.POINTER(dp)] * 2
                                      + [ip, ip, ip, C.POINTER(dp), ip, C.c_int, C.c_double, C.c_int, C.c_int,
                                         C.c_int, C.c_int, ip])
+        L.hcref_tile_gemm_ops.restype = C.c_int
+        L.hcref_tile_gemm_ops.argtypes = ([C.c_double] + [C.c_int] * 5 + [dp, C.c_int] + [C.c_int] * 5
+                                          + [dp, C.c_int, C.c_double] + [C.c_int] * 3
+                                          + [ip, C.c_int, dp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int])
+        L.hcref_potrf.restype = C.c_int
+        L.hcref_potrf.argtypes = [C.c_int, C.c_int, dp]
+        L.hcref_trsm.restype = C.c_int
+        L.hcref_trsm.argtypes = [C.c_int] * 4 + [C.c_double, C.c_int, dp] + [C.c_int] * 4 + [dp]
+        L.hcref_syrk.restype = C.c_int
+        L.hcref_syrk.argtypes = ([C.c_double] + [C.c_int] * 5 + [dp] + [C.c_int] * 2
+                                 + [C.c_double, C.c_int, C.c_int, dp])
         L.hcref_set_blas_threads.argtypes = [C.c_int]
         _LIB = L
     return _LIB
@@ -79,6 +90,21 @@ class RefTile:
     def v(self):
         o = self.rows * self.max_rank
         return self.buf[o:o + self.rank * self.cols].reshape((self.rank, self.cols), order="F")
+
+    def w(self):
+        """The V region read as HCore++'s Cholesky routines read it: cols x rank, ld cols."""
+        o = self.rows * self.max_rank
+        return self.buf[o:o + self.rank * self.cols].reshape((self.cols, self.rank), order="F")
+
+    @classmethod
+    def cholesky(cls, u, w, max_rank):
+        """A compressed tile holding U and W (tile = U W^T) in the buffer."""
+        m, r = u.shape
+        n = w.shape[0]
+        buf = np.zeros(m * max_rank + max_rank * n)
+        buf[:m * r] = np.asarray(u).ravel(order="F")
+        buf[m * max_rank:m * max_rank + r * n] = np.asarray(w).ravel(order="F")
+        return cls(1, m, n, r, max_rank, buf)
 
     def to_dense(self):
         if self.kind == 0:
@@ -141,3 +167,33 @@ def tlr_gemm(nt, nb, alpha, beta, a_tiles, b_tiles, c_tiles, params, c_list=None
     for idx in range(nt * nt):
         cf[idx].rank = int(cr[idx])
     return secs, err.value
+
+
+def tile_gemm_ops(alpha, a: RefTile, op_a, b: RefTile, op_b, beta, c: RefTile, params: O.CompressionParameters,
+                  cholesky=False) -> None:
+    rk = C.c_int(c.rank)
+    rc = lib().hcref_tile_gemm_ops(alpha, a.kind, a.rows, a.cols, a.rank, a.max_rank, _ptr(a.buf), int(op_a),
+                                   b.kind, b.rows, b.cols, b.rank, b.max_rank, _ptr(b.buf), int(op_b), beta,
+                                   c.kind, c.rows, c.cols, C.byref(rk), c.max_rank, _ptr(c.buf),
+                                   params.accuracy, int(params.truncated_svd), params.fixed_rank, params.op_type,
+                                   int(cholesky))
+    if rc != 0:
+        raise RuntimeError("hcref_tile_gemm_ops failed")
+    c.rank = rk.value
+
+
+def potrf(uplo, a: RefTile) -> None:
+    if lib().hcref_potrf(int(uplo), a.rows, _ptr(a.buf)) != 0:
+        raise RuntimeError("hcref_potrf failed")
+
+
+def trsm(side, uplo, trans, diag, alpha, a: RefTile, b: RefTile) -> None:
+    if lib().hcref_trsm(int(side), int(uplo), int(trans), int(diag), alpha, a.rows, _ptr(a.buf), b.rows, b.cols,
+                        b.rank, b.max_rank, _ptr(b.buf)) != 0:
+        raise RuntimeError("hcref_trsm failed")
+
+
+def syrk(alpha, a: RefTile, op_a, uplo, beta, c: RefTile) -> None:
+    if lib().hcref_syrk(alpha, a.kind, a.rows, a.cols, a.rank, a.max_rank, _ptr(a.buf), int(op_a), int(uplo), beta,
+                        c.rows, c.cols, _ptr(c.buf)) != 0:
+        raise RuntimeError("hcref_syrk failed")

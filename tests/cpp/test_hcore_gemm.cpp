@@ -5,7 +5,8 @@
 //   ||C_ref - C||_inf / (sqrt(k + 2) |alpha| ||A||_inf ||B||_inf + 2 |beta| ||C||_inf) < 3 * accuracy.
 // Inputs: Q1 diag(10^-i) Q2^T with seeded random orthogonal Q1, Q2 -- the singular values the
 // reference's generate_dense_matrix asks dlatms for (src/helpers/MatrixHelpers.cpp:22-31); the
-// LAPACK generator itself is not linked here.  Exit status 0 = every case passed.
+// LAPACK generator itself is not linked here.  Then the Cholesky-flow operations (Potrf, Trsm, Syrk,
+// Gemm with aCholesky = true) against host loops.  Exit status 0 = every case passed.
 #include <hcorepp_gb300/hcore.hpp>
 
 #include <cmath>
@@ -81,6 +82,124 @@ static M to_host_dense(const operators::Tile<double> &t) {
     return out;
 }
 
+// A compressed tile as the Cholesky routines read it: U (m x r) times W^T, W = V region (n x r, ld n).
+static M vt_dense(const operators::CompressedTile<double> &c) {
+    const int m = (int) c.GetNumOfRows(), n = (int) c.GetNumOfCols(), r = (int) c.GetTileRank();
+    M u((size_t) m * r), w((size_t) n * r), out((size_t) m * n, 0.0);
+    cudaMemcpy(u.data(), c.GetUMatrix(), sizeof(double) * u.size(), cudaMemcpyDeviceToHost);
+    cudaMemcpy(w.data(), c.GetVMatrix(), sizeof(double) * w.size(), cudaMemcpyDeviceToHost);
+    for (int j = 0; j < n; j++)
+        for (int l = 0; l < r; l++) {
+            const double wl = w[j + (size_t) l * n];
+            for (int i = 0; i < m; i++) out[i + (size_t) j * m] += u[i + (size_t) l * m] * wl;
+        }
+    return out;
+}
+
+static M host_of(const double *dev, size_t count) {
+    M h(count);
+    cudaMemcpy(h.data(), dev, sizeof(double) * count, cudaMemcpyDeviceToHost);
+    return h;
+}
+
+static bool report(const char *name, int n, double err, double tol) {
+    const bool pass = err < tol;
+    std::printf("|%-5s|%-5d|%-14.3e|%-5s|%-6s|\n", name, n, err, "-", pass ? "Pass" : "Fail");
+    return pass;
+}
+
+// Potrf, Trsm, Syrk and Gemm(aCholesky = true) of the Cholesky flow (HCore.cpp:23-344, :482-647).
+static int cholesky_ops(kernels::RunContext &ctx, dataunits::MemoryUnit<double> &mem) {
+    const int n = 96;
+    int failures = 0;
+    size_t flops = 0;
+    std::mt19937_64 g(5);
+    M q = random_orthogonal(n, g), spd((size_t) n * n, 0.0);
+    for (int l = 0; l < n; l++)
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < n; i++) spd[i + (size_t) j * n] += q[i + (size_t) l * n] * (1.0 + l) * q[j + (size_t) l * n];
+    operators::DenseTile<double> L(n, n, spd.data(), n, ctx);
+    api::HCore<double>::Potrf(L, blas::Uplo::Lower, ctx, flops, mem);
+    ctx.Sync();
+    M lh = host_of(L.GetTileSubMatrix(0), (size_t) n * n);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < j; i++) lh[i + (size_t) j * n] = 0.0;
+    double e = 0, s = 0;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+            double t = 0;
+            for (int l = 0; l < n; l++) t += lh[i + (size_t) l * n] * lh[j + (size_t) l * n];
+            e = std::max(e, std::fabs(t - spd[i + (size_t) j * n]));
+            s = std::max(s, std::fabs(spd[i + (size_t) j * n]));
+        }
+    failures += !report("POTRF", n, e / s, 1e-13);
+
+    operators::CompressionParameters params(1e-10);
+    M bd = graded_matrix(n, 71), ad = graded_matrix(n, 72), cd = graded_matrix(n, 73);
+    operators::CompressedTile<double> B(n, n, bd.data(), n, params, blas::Layout::ColMajor, ctx);
+    const int rb = (int) B.GetTileRank();
+    M w0 = host_of(B.GetVMatrix(), (size_t) n * rb);
+    api::HCore<double>::Trsm(blas::Side::Left, blas::Uplo::Lower, blas::Op::NoTrans, blas::Diag::NonUnit, 1.0, L, B,
+                             ctx, flops, mem);
+    ctx.Sync();
+    M w1 = host_of(B.GetVMatrix(), (size_t) n * rb);
+    e = 0, s = 0;
+    for (int c = 0; c < rb; c++)
+        for (int i = 0; i < n; i++) {
+            double t = 0;
+            for (int l = 0; l <= i; l++) t += lh[i + (size_t) l * n] * w1[l + (size_t) c * n];
+            e = std::max(e, std::fabs(t - w0[i + (size_t) c * n]));
+            s = std::max(s, std::fabs(w0[i + (size_t) c * n]));
+        }
+    failures += !report("TRSM", n, e / s, 1e-12);
+
+    operators::CompressedTile<double> A(n, n, ad.data(), n, params, blas::Layout::ColMajor, ctx);
+    M a_vt = vt_dense(A);
+    operators::DenseTile<double> Cd(n, n, cd.data(), n, ctx);
+    api::HCore<double>::Syrk(-1.0, A, blas::Op::NoTrans, blas::Uplo::Lower, 0.5, Cd, ctx, flops, mem);
+    ctx.Sync();
+    M ch = host_of(Cd.GetTileSubMatrix(0), (size_t) n * n);
+    e = 0, s = 0;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+            double t = 0;
+            if (i >= j) {
+                t = 0.5 * cd[i + (size_t) j * n];
+                for (int l = 0; l < n; l++) t -= a_vt[i + (size_t) l * n] * a_vt[j + (size_t) l * n];
+            }
+            e = std::max(e, std::fabs(t - ch[i + (size_t) j * n]));
+            s = std::max(s, std::fabs(t));
+        }
+    failures += !report("SYRK", n, e / s, 1e-12);
+
+    operators::CompressedTile<double> Bc(n, n, bd.data(), n, params, blas::Layout::ColMajor, ctx);
+    operators::CompressedTile<double> Cc(n, n, cd.data(), n, params, blas::Layout::ColMajor, ctx);
+    M b_vt = vt_dense(Bc), c_vt = vt_dense(Cc), ref((size_t) n * n);
+    const double alpha = -1.0, beta = 1.0;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+            double t = beta * c_vt[i + (size_t) j * n];
+            for (int l = 0; l < n; l++) t += alpha * a_vt[i + (size_t) l * n] * b_vt[j + (size_t) l * n];
+            ref[i + (size_t) j * n] = t;
+        }
+    api::HCore<double>::Gemm(alpha, A, blas::Op::NoTrans, Bc, blas::Op::Trans, beta, Cc, ctx, flops, mem, params, true);
+    ctx.Sync();
+    M out = vt_dense(Cc);
+    for (size_t q2 = 0; q2 < out.size(); q2++) out[q2] = ref[q2] - out[q2];
+    const double denom = std::sqrt((double) n + 2) * norm_inf(a_vt, n, n) * norm_inf(b_vt, n, n) +
+                         2 * norm_inf(c_vt, n, n);
+    failures += !report("CHOLG", n, norm_inf(out, n, n) / denom, 3 * 1e-10);
+    bool threw = false;
+    try {
+        api::HCore<double>::Gemm(alpha, A, blas::Op::NoTrans, Bc, blas::Op::NoTrans, beta, Cc, ctx, flops, mem, params,
+                                 true);
+    } catch (const std::invalid_argument &) {
+        threw = true;
+    }
+    failures += !report("CHOLX", n, threw ? 0.0 : 1.0, 0.5);
+    return failures;
+}
+
 int main() {
     kernels::RunContext ctx(0);
     dataunits::MemoryUnit<double> mem(ctx);
@@ -124,5 +243,6 @@ int main() {
             std::printf("|%-5s|%-5d|%-14.3e|%-5zu|%-6s|\n", combo, n, err, C->GetTileRank(), pass ? "Pass" : "Fail");
         }
     }
+    failures += cholesky_ops(ctx, mem);
     return failures == 0 ? 0 : 1;
 }

@@ -99,28 +99,115 @@ def test_hcore_trsm_compressed_matches_oracle(T):
     np.testing.assert_allclose(gb.v(), ob.v, rtol=1e-10, atol=1e-12)
 
 
-def test_tile_cholesky_residual(T):
-    """Tile Cholesky of an SPD exponential-kernel matrix (3-D points, dense diagonal tiles, 1e-8
-    compressed off-diagonal tiles): residual ||L L^T - A||_F / ||A||_F and agreement with the
-    oracle's driver."""
+def _chol_pair(T, nb, rank, rng, max_rank):
+    """The same U W^T tile for the oracle (CholeskyTile) and the GPU (a vt CompressedTile)."""
+    u = rng.standard_normal((nb, rank)) * 0.5 ** np.arange(rank)
+    w = rng.standard_normal((nb, rank))
+    g = T.CompressedTile(nb, nb, rank=0, max_rank=max_rank, vt=True)
+    if rank:
+        g.set_factors(u, w.T)
+    return O.CholeskyTile(u, w, max_rank), g
+
+
+@pytest.mark.parametrize("nb,ra,rb,rc", [(60, 7, 9, 5), (96, 20, 12, 0), (128, 30, 30, 30)])
+def test_gemm_cholesky_branch_vs_oracle(T, nb, ra, rb, rc):
+    """Gemm(-1, A, NoTrans, B, Trans, 0.5, C, aCholesky = true): compressed_vt operands through
+    hcgb_tile_gemm against the oracle's restatement (pinned to HCore++'s own branch)."""
+    rng = np.random.default_rng(nb + ra)
+    mr = nb // 3
+    oa, ga = _chol_pair(T, nb, ra, rng, mr)
+    ob, gb = _chol_pair(T, nb, rb, rng, mr)
+    oc, gc = _chol_pair(T, nb, rc, rng, mr)
+    want = -oa.to_dense() @ ob.to_dense().T + 0.5 * oc.to_dense()
+    params = O.CompressionParameters(1e-8, truncated_svd=True)
+    O.hcore_gemm_cholesky(-1.0, oa, ob, 0.5, oc, params)
+    from hcorepp_gb300 import _lib as L
+    T.HCore.Gemm(-1.0, ga, L.NOTRANS, gb, L.TRANS, 0.5, gc, T.CompressionParameters(1e-8, truncated_svd=True),
+                 cholesky=True)
+    assert abs(gc.rank - oc.rank) <= 1
+    got = gc.u() @ gc.w().T
+    assert rel_fro(got, want) <= 2 * max(rel_fro(oc.to_dense(), want), 1e-8)
+    with pytest.raises(ValueError):
+        T.HCore.Gemm(-1.0, ga, L.NOTRANS, gb, L.NOTRANS, 0.5, gc, cholesky=True)
+
+
+@pytest.mark.parametrize("uplo", [0, 1])
+def test_syrk_compressed_vs_oracle(T, uplo):
+    """HCore<T>::Syrk with a compressed A (A = U W^T) into a dense C: C <- beta C - A A^T, the other
+    strict triangle zeroed (HCore.cpp:482-583)."""
+    rng = np.random.default_rng(20 + uplo)
+    nb = 112
+    oa, ga = _chol_pair(T, nb, 13, rng, nb // 3)
+    c0 = rng.standard_normal((nb, nb))
+    oc = O.DenseTile(c0.copy())
+    gc = T.DenseTile(nb, nb, c0)
+    O.hcore_syrk(-1.0, oa, uplo == 0, 0.75, oc)
+    T.Syrk(-1.0, ga, 0, uplo, 0.75, gc)
+    np.testing.assert_allclose(gc.to_dense(), oc.data, rtol=1e-11, atol=1e-11)
+
+
+def test_vt_layout_is_bitwise_equal_to_plain(T):
+    """A 3x3-tile multiply with dense diagonals (all seven batched combinations occur) run once in
+    the plain layout and once with every compressed tile in the compressed_vt layout: the same
+    ranks, U factors and (transposed) V factors, bit for bit."""
+    import torch
     from hcorepp_gb300 import _lib as L
     from hcorepp_gb300.problems import KernelMatrix
-    nt, nb, acc = 4, 128, 1e-8
-    km = KernelMatrix(nt * nb, nb, 3, 0.2, 5, diag_shift=1e-2)
-    a_dense = km.dense()
+    nt, nb, acc = 3, 96, 1e-8
     kinds = [[L.DENSE if i == j else L.COMPRESSED for j in range(nt)] for i in range(nt)]
-    tm = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
-    og = [[None] * nt for _ in range(nt)]
+    mats = {}
+    for vt in (False, True):
+        ms = []
+        for seed in (1, 2):
+            km = KernelMatrix(nt * nb, nb, 2, 0.1, seed)
+            tm = T.TileMatrix(nt, nt, nb, kinds, nb // 3, vt=vt)
+            for i in range(nt):
+                for j in range(nt):
+                    if i == j:
+                        tm.set_tile(i, j, dense=km.tile(i, j))
+                    else:
+                        t = compressed_from_dense(km.tile(i, j), acc)
+                        tm.set_tile(i, j, u=t.u, v=t.v)
+            ms.append(tm)
+        a, c = ms
+        T.tlr_gemm(1.0, a, a, 1.0, c, T.CompressionParameters(acc, truncated_svd=True))
+        torch.cuda.synchronize()
+        mats[vt] = c
+    np.testing.assert_array_equal(mats[True].rank_grid(), mats[False].rank_grid())
     for i in range(nt):
         for j in range(nt):
+            p, q = mats[False].tile(i, j), mats[True].tile(i, j)
+            if i == j:
+                np.testing.assert_array_equal(q.to_dense(), p.to_dense())
+            else:
+                np.testing.assert_array_equal(q.u(), p.u())
+                np.testing.assert_array_equal(q.v(), p.v())
+
+
+def test_tile_cholesky_residual(T):
+    """Tile Cholesky of an SPD exponential-kernel matrix (2-D points, length scale 0.1, 4 x 4 tiles
+    of 256, dense diagonal tiles, off-diagonal tiles compressed at 1e-8 with the reference's
+    capacity nb/3, Cholesky-flow layout): residual ||L L^T - A||_F / ||A||_F and agreement with the
+    oracle's driver.  Tiles whose 1e-8 rank would exceed nb/3 are clamped there, which bounds the
+    residual near 1e-8 rather than at it."""
+    from hcorepp_gb300 import _lib as L
+    from hcorepp_gb300.problems import KernelMatrix
+    nt, nb, acc = 4, 256, 1e-8
+    km = KernelMatrix(nt * nb, nb, 2, 0.1, 5, diag_shift=1e-2)
+    a_dense = km.dense()
+    kinds = [[L.DENSE if i == j else L.COMPRESSED for j in range(nt)] for i in range(nt)]
+    tm = T.TileMatrix(nt, nt, nb, kinds, nb // 3, vt=True)
+    og = [[None] * nt for _ in range(nt)]
+    for i in range(nt):
+        for j in range(i + 1):
             blk = km.tile(i, j)
             if i == j:
                 tm.set_tile(i, j, dense=blk)
                 og[i][j] = O.DenseTile(blk)
-            elif i > j:
+            else:
                 t = compressed_from_dense(blk, acc)
                 tm.set_tile(i, j, u=t.u, v=t.v)
-                og[i][j] = t
+                og[i][j] = O.CholeskyTile(t.u, t.v.T, t.max_rank)
     params = T.CompressionParameters(acc, truncated_svd=True)
     assert T.tile_cholesky(tm, params) == 0
     assert O.tile_cholesky(og, nt, O.CompressionParameters(acc, truncated_svd=True)) == 0
@@ -137,5 +224,5 @@ def test_tile_cholesky_residual(T):
             ofac[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb] = oblk
     res = rel_fro(lfac @ lfac.T, a_dense)
     res_o = rel_fro(ofac @ ofac.T, a_dense)
-    assert res < 1e-6 and res <= 2 * max(res_o, acc), (res, res_o)
+    assert res < 1e-7 and res <= 2 * max(res_o, acc), (res, res_o)
     assert rel_fro(lfac, ofac) < 1e-5
