@@ -172,6 +172,50 @@ class CompressedTile:
     GetNumOfCols = lambda self: self.cols
 
 
+@dataclass(frozen=True)
+class TileMetadata:
+    """TileMetadata (include/hcorepp/operators/interface/Tile.hpp:30-52): everything a task runtime
+    needs to move a tile but its buffer, which stays in device memory."""
+    rows: int
+    cols: int
+    rank: int
+    max_rank: int
+    leading_dim: int
+    layout: str  # "C" = column-major, the only layout of this path
+    type: int    # L.DENSE or L.COMPRESSED
+
+
+class TilePacker:
+    """TilePacker<T> (include/hcorepp/operators/interface/TilePacker.hpp:17-60,
+    src/operators/TilePacker.cpp:5-26)."""
+
+    @staticmethod
+    def UnPackTile(tile):
+        """(metadata, buffer) of a tile; the buffer is the tile's own device memory (no copy)."""
+        if tile.kind == L.DENSE:
+            return TileMetadata(tile.rows, tile.cols, 0, 0, tile.rows, "C", L.DENSE), tile.buffer
+        return (TileMetadata(tile.rows, tile.cols, tile.rank, tile.max_rank, tile.rows, "C", L.COMPRESSED),
+                tile.buffer)
+
+    @staticmethod
+    def PackTile(meta: TileMetadata, buffer: torch.Tensor):
+        """A tile over ``buffer`` described by ``meta`` (no copy)."""
+        if meta.layout != "C" or meta.leading_dim != meta.rows:
+            raise ValueError("PackTile: column-major metadata with leading dimension = rows expected")
+        if meta.type == L.DENSE:
+            if buffer.numel() < meta.rows * meta.cols:
+                raise ValueError("PackTile: buffer smaller than the dense tile")
+            return DenseTile(meta.rows, meta.cols, buffer=buffer)
+        if meta.rank > meta.max_rank or buffer.numel() < meta.max_rank * (meta.rows + meta.cols):
+            raise ValueError("PackTile: rank above capacity or buffer smaller than the compressed tile")
+        t = CompressedTile(meta.rows, meta.cols, rank=0, max_rank=meta.max_rank, buffer=buffer, device=buffer.device)
+        t.rank_buf.fill_(meta.rank)
+        return t
+
+    unpack = UnPackTile
+    pack = PackTile
+
+
 class HCore:
     """HCore<double> (include/hcorepp/api/HCore.hpp:41-63)."""
 

@@ -10,6 +10,8 @@
 //   hcorepp::dataunits::MemoryUnit             include/hcorepp/data-units/memory-handlers/pool/MemoryHandler.hpp:22-157
 //   hcorepp::api::HCore<T>::Gemm               include/hcorepp/api/HCore.hpp:41-63
 //   hcorepp::api::HCore<T>::Syrk/Potrf/Trsm    include/hcorepp/api/HCore.hpp:65-112 (src/api/HCore.cpp:482-647)
+//   hcorepp::operators::TileMetadata / TilePacker  include/hcorepp/operators/interface/Tile.hpp:20-52,
+//                                              include/hcorepp/operators/interface/TilePacker.hpp:17-60
 // Tile buffers live on the device (as in the reference's CUDA build); constructors accept host or
 // device pointers (cudaMemcpyDefault).  Errors throw std::runtime_error / std::invalid_argument as
 // the reference does.  The GPU path computes in double precision: T = double.
@@ -22,6 +24,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 
 #include "hcgb.h"
 
@@ -125,11 +128,35 @@ private:
     int mMode = HCGB_PLAIN_FP64;
 };
 
+// Tile metadata for task runtimes moving tiles between workers (Tile.hpp:20-52): everything but
+// the data buffer, which stays where it is (device memory) and travels as one pointer.
+enum TileType { DENSE, COMPRESSED };
+
+struct TileMetadata {
+    size_t mNumOfRows;
+    size_t mNumOfCols;
+    size_t mMatrixRank;
+    size_t mMaxRank;
+    size_t mLeadingDimension;
+    blas::Layout mLayout;
+    TileType mType;
+    TileMetadata(size_t aRows, size_t aCols, size_t aMatrixRank, size_t aMaxRank, size_t aLeadingDim,
+                 blas::Layout aLayout, TileType aType)
+        : mNumOfRows(aRows), mNumOfCols(aCols), mMatrixRank(aMatrixRank), mMaxRank(aMaxRank),
+          mLeadingDimension(aLeadingDim), mLayout(aLayout), mType(aType) {}
+};
+
 template <typename T>
 class Tile {
 public:
     static_assert(sizeof(T) == 8, "the GB300 TLR path computes in double precision");
     virtual ~Tile() = default;
+    // (metadata, data buffer) of this tile; the metadata is heap-allocated and owned by the caller,
+    // the buffer stays owned by the tile (Dense.cpp:127-134, Compressed.cpp:769-778).
+    virtual std::pair<TileMetadata *, T *> UnPackTile(const kernels::RunContext &aContext) = 0;
+    // Re-point this tile at a buffer described by aMetadata, without copying; the tile does not own
+    // the buffer afterwards (Dense.cpp:136-142, Compressed.cpp:780-788).
+    virtual void PackTile(TileMetadata aMetadata, T *aDataArray, const kernels::RunContext &aContext) = 0;
     size_t GetNumOfRows() const { return mRows; }
     size_t GetNumOfCols() const { return mCols; }
     blas::Layout GetLayout() const { return blas::Layout::ColMajor; }
@@ -168,6 +195,20 @@ public:
     }
     DenseTile(size_t aRows, size_t aCols, T *aData, size_t aLd, const kernels::RunContext &aContext)
         : DenseTile(aRows, aCols, aData, aLd, blas::Layout::ColMajor, aContext) {}
+    DenseTile() = default;
+    std::pair<TileMetadata *, T *> UnPackTile(const kernels::RunContext &) override {
+        return {new TileMetadata(this->mRows, this->mCols, 0, 0, this->mRows, blas::Layout::ColMajor, DENSE), mData};
+    }
+    void PackTile(TileMetadata aMetadata, T *aDataArray, const kernels::RunContext &) override {
+        if (aMetadata.mType != DENSE || aMetadata.mLayout != blas::Layout::ColMajor ||
+            aMetadata.mLeadingDimension != aMetadata.mNumOfRows)
+            throw std::invalid_argument("DenseTile::PackTile: column-major dense metadata with ld = rows expected");
+        if (mOwn) cudaFree(mData);
+        mOwn = false;
+        mData = aDataArray;
+        this->mRows = aMetadata.mNumOfRows;
+        this->mCols = aMetadata.mNumOfCols;
+    }
     ~DenseTile() override {
         if (mOwn) cudaFree(mData);
     }
@@ -228,9 +269,28 @@ public:
             detail::check(rc, aContext.handle(), "hcgb_compress_tile");
         }
     }
+    CompressedTile() = default;
     ~CompressedTile() override {
-        cudaFree(mData);
+        if (mOwnData) cudaFree(mData);
         cudaFree(mRank);
+    }
+    std::pair<TileMetadata *, T *> UnPackTile(const kernels::RunContext &) override {
+        return {new TileMetadata(this->mRows, this->mCols, GetTileRank(), mMaxRank, this->mRows,
+                                 blas::Layout::ColMajor, COMPRESSED),
+                mData};
+    }
+    void PackTile(TileMetadata aMetadata, T *aDataArray, const kernels::RunContext &) override {
+        if (aMetadata.mType != COMPRESSED || aMetadata.mLayout != blas::Layout::ColMajor ||
+            aMetadata.mMatrixRank > aMetadata.mMaxRank)
+            throw std::invalid_argument("CompressedTile::PackTile: column-major compressed metadata expected");
+        if (mOwnData) cudaFree(mData);
+        mOwnData = false;
+        mData = aDataArray;
+        this->mRows = aMetadata.mNumOfRows;
+        this->mCols = aMetadata.mNumOfCols;
+        mMaxRank = aMetadata.mMaxRank;
+        if (!mRank) detail::cuda(cudaMalloc(&mRank, sizeof(int)), "cudaMalloc");
+        set_rank(aMetadata.mMatrixRank);
     }
     CompressedTile(const CompressedTile &) = delete;
     CompressedTile &operator=(const CompressedTile &) = delete;
@@ -273,8 +333,9 @@ public:
         detail::cuda(cudaMemcpy(nd + this->mRows * r, GetVMatrix(), sizeof(T) * rank * this->mCols,
                                 cudaMemcpyDeviceToDevice),
                      "cudaMemcpy");
-        cudaFree(mData);
+        if (mOwnData) cudaFree(mData);
         mData = nd;
+        mOwnData = true;
         mMaxRank = r;
     }
 
@@ -296,6 +357,25 @@ private:
     T *mData = nullptr;
     int *mRank = nullptr;
     size_t mMaxRank = 0;
+    bool mOwnData = true;
+};
+
+// TilePacker (TilePacker.hpp:17-60, src/operators/TilePacker.cpp:5-26).
+template <typename T>
+class TilePacker {
+public:
+    virtual ~TilePacker() = default;
+    static std::pair<TileMetadata *, T *> UnPackTile(Tile<T> &aTile, const kernels::RunContext &aContext) {
+        return aTile.UnPackTile(aContext);
+    }
+    // A new heap tile (owned by the caller) over the given buffer.
+    static Tile<T> *PackTile(TileMetadata aMetadata, T *aDataArray, const kernels::RunContext &aContext) {
+        Tile<T> *tile;
+        if (aMetadata.mType == DENSE) tile = new DenseTile<T>();
+        else tile = new CompressedTile<T>();
+        tile->PackTile(aMetadata, aDataArray, aContext);
+        return tile;
+    }
 };
 
 }  // namespace operators

@@ -6,7 +6,8 @@
 // Inputs: Q1 diag(10^-i) Q2^T with seeded random orthogonal Q1, Q2 -- the singular values the
 // reference's generate_dense_matrix asks dlatms for (src/helpers/MatrixHelpers.cpp:22-31); the
 // LAPACK generator itself is not linked here.  Then the Cholesky-flow operations (Potrf, Trsm, Syrk,
-// Gemm with aCholesky = true) against host loops.  Exit status 0 = every case passed.
+// Gemm with aCholesky = true) against host loops, and a TilePacker round trip.  Exit status 0 =
+// every case passed.
 #include <hcorepp_gb300/hcore.hpp>
 
 #include <cmath>
@@ -200,6 +201,38 @@ static int cholesky_ops(kernels::RunContext &ctx, dataunits::MemoryUnit<double> 
     return failures;
 }
 
+// TilePacker round trip (TestTilePacker.cpp): unpack -> metadata + buffer, pack -> a tile over the
+// same buffer; a product through packed tiles equals the product through the originals bitwise.
+static int tile_packer(kernels::RunContext &ctx, dataunits::MemoryUnit<double> &mem) {
+    const int n = 128;
+    int failures = 0;
+    operators::CompressionParameters params(1e-8);
+    M ad = graded_matrix(n, 81), bd = graded_matrix(n, 82), cd = graded_matrix(n, 83);
+    operators::CompressedTile<double> A(n, n, ad.data(), n, params, blas::Layout::ColMajor, ctx);
+    operators::DenseTile<double> B(n, n, bd.data(), n, ctx);
+    auto ma = operators::TilePacker<double>::UnPackTile(A, ctx);
+    auto mb = operators::TilePacker<double>::UnPackTile(B, ctx);
+    const bool meta_ok = ma.first->mType == operators::COMPRESSED && ma.first->mNumOfRows == (size_t) n &&
+                         ma.first->mMatrixRank == A.GetTileRank() && ma.first->mMaxRank == A.GetMaxRank() &&
+                         ma.second == A.GetUMatrix() && mb.first->mType == operators::DENSE &&
+                         mb.second == B.GetTileSubMatrix(0);
+    std::unique_ptr<operators::Tile<double>> pa(operators::TilePacker<double>::PackTile(*ma.first, ma.second, ctx));
+    std::unique_ptr<operators::Tile<double>> pb(operators::TilePacker<double>::PackTile(*mb.first, mb.second, ctx));
+    delete ma.first;
+    delete mb.first;
+    operators::CompressedTile<double> C1(n, n, cd.data(), n, params, blas::Layout::ColMajor, ctx);
+    operators::CompressedTile<double> C2(n, n, cd.data(), n, params, blas::Layout::ColMajor, ctx);
+    size_t flops = 0;
+    api::HCore<double>::Gemm(1.0, A, blas::Op::NoTrans, B, blas::Op::NoTrans, 1.0, C1, ctx, flops, mem, params);
+    api::HCore<double>::Gemm(1.0, *pa, blas::Op::NoTrans, *pb, blas::Op::NoTrans, 1.0, C2, ctx, flops, mem, params);
+    ctx.Sync();
+    M o1 = to_host_dense(C1), o2 = to_host_dense(C2), a1 = to_host_dense(A), a2 = to_host_dense(*pa);
+    double diff = 0;
+    for (size_t e = 0; e < o1.size(); e++) diff = std::max(diff, std::fabs(o1[e] - o2[e]) + std::fabs(a1[e] - a2[e]));
+    failures += !report("PACK", n, meta_ok ? diff : 1.0, 1e-300);
+    return failures;
+}
+
 int main() {
     kernels::RunContext ctx(0);
     dataunits::MemoryUnit<double> mem(ctx);
@@ -244,5 +277,6 @@ int main() {
         }
     }
     failures += cholesky_ops(ctx, mem);
+    failures += tile_packer(ctx, mem);
     return failures == 0 ? 0 : 1;
 }

@@ -1,6 +1,10 @@
 """CPU-side checks of the C ABI: the library builds for sm_103a, loads, and exports every
-entry point include/hcgb.h declares (no compute call: there is no GPU here)."""
+entry point include/hcgb.h declares (no compute call: there is no GPU here); and host-side logic
+of the Python mirror that needs no kernel (TilePacker)."""
 import ctypes
+
+import numpy as np
+import pytest
 
 from hcorepp_gb300 import _lib as L
 from hcorepp_gb300.build import build
@@ -30,3 +34,29 @@ def test_bad_arguments_without_a_device():
     lib = L.lib()
     assert lib.hcgb_sync(None) == L.HCGB_BAD_ARG
     assert lib.hcgb_gemm_batch(None, 1.0, 1.0, 0, None, None, None) == L.HCGB_BAD_ARG
+
+
+def test_tile_packer_round_trip_on_host():
+    """TilePacker.UnPackTile / PackTile (TilePacker.cpp:5-26) on host tensors: metadata fields and a
+    tile over the same buffer, no copy."""
+    import torch
+    from hcorepp_gb300 import _lib as L
+    from hcorepp_gb300 import tiles as T
+    rng = np.random.default_rng(0)
+    u, v = rng.standard_normal((40, 5)), rng.standard_normal((5, 30))
+    c = T.CompressedTile(40, 30, u, v, max_rank=13, device="cpu")
+    meta, buf = T.TilePacker.UnPackTile(c)
+    assert (meta.rows, meta.cols, meta.rank, meta.max_rank, meta.leading_dim, meta.type) == (40, 30, 5, 13, 40,
+                                                                                              L.COMPRESSED)
+    assert buf.data_ptr() == c.buffer.data_ptr()
+    p = T.TilePacker.PackTile(meta, buf)
+    assert p.buffer.data_ptr() == buf.data_ptr() and p.rank == 5
+    np.testing.assert_array_equal(p.to_dense(), u @ v)
+    d = T.DenseTile(7, 9, rng.standard_normal((7, 9)), device="cpu")
+    md, bd = T.TilePacker.UnPackTile(d)
+    assert md.type == L.DENSE and (md.rows, md.cols, md.leading_dim) == (7, 9, 7)
+    np.testing.assert_array_equal(T.TilePacker.PackTile(md, bd).to_dense(), d.to_dense())
+    with pytest.raises(ValueError):
+        T.TilePacker.PackTile(T.TileMetadata(40, 30, 14, 13, 40, "C", L.COMPRESSED), buf)
+    with pytest.raises(ValueError):
+        T.TilePacker.PackTile(T.TileMetadata(7, 9, 0, 0, 8, "C", L.DENSE), bd)

@@ -1,6 +1,6 @@
 """Builds and runs the C++ check of the HCore++-shaped adapter (tests/cpp/test_hcore_gemm.cpp):
 every tile combination through hcorepp::api::HCore<double>::Gemm against the reference's pass
-rule, then Potrf, Trsm, Syrk and Gemm(aCholesky) against host loops.  The compile step runs without a GPU; the run needs one."""
+rule, then Potrf, Trsm, Syrk and Gemm(aCholesky) against host loops, and a TilePacker round trip.  The compile step runs without a GPU; the run needs one."""
 import os
 import subprocess
 
@@ -31,4 +31,4 @@ def test_adapter_all_combinations_pass_reference_rule():
     r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count("Pass") == 29
+    assert r.stdout.count("Pass") == 30

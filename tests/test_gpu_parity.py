@@ -282,3 +282,25 @@ def test_compress_tile_vs_oracle(T, truncated, acc):
         assert abs(g.rank - o.rank) <= 1, (i, j, g.rank, o.rank)
         e_o = rel_fro(o.to_dense(), d)
         assert rel_fro(g.to_dense(), d) <= 2 * max(e_o, 1e-14), (i, j)
+
+
+def test_tile_packer_gemm_through_packed_tiles(T):
+    """A tile moved as (TileMetadata, device buffer) and re-packed gives a bitwise identical product."""
+    rng = np.random.default_rng(9)
+    nb = 128
+    a = compressed_from_dense(random_lowrank(nb, nb, 20, rng), 1e-10)
+    c = compressed_from_dense(random_lowrank(nb, nb, 15, rng), 1e-10)
+    bd = rng.standard_normal((nb, nb))
+    ga, gb = _gpu_tile(T, a), T.DenseTile(nb, nb, bd)
+    outs = []
+    for packed in (False, True):
+        gc = _gpu_tile(T, c)
+        ta, tb = ga, gb
+        if packed:
+            ta = T.TilePacker.PackTile(*T.TilePacker.UnPackTile(ga))
+            tb = T.TilePacker.PackTile(*T.TilePacker.UnPackTile(gb))
+        T.HCore.Gemm(1.0, ta, 0, tb, 0, 1.0, gc, T.CompressionParameters(1e-8, truncated_svd=True))
+        outs.append((gc.rank, gc.u().copy(), gc.v().copy()))
+    assert outs[0][0] == outs[1][0]
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+    np.testing.assert_array_equal(outs[0][2], outs[1][2])
