@@ -94,7 +94,8 @@ def lib():
         L.hcgb_trsm.argtypes = [vp, ip, ip, ip, ip, ip, ip, C.c_double, vp, ip, vp, ip]
         L.hcgb_syrk.argtypes = [vp, ip, ip, ip, ip, C.c_double, vp, ip, C.c_double, vp, ip]
         L.hcgb_fill_triangle.argtypes = [vp, ip, ip, vp, ip, C.c_double]
-        for nm in ("hcgb_potrf", "hcgb_trsm", "hcgb_syrk", "hcgb_fill_triangle"):
+        L.hcgb_tile_cholesky.argtypes = [vp, ip, C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int), vp]
+        for nm in ("hcgb_potrf", "hcgb_trsm", "hcgb_syrk", "hcgb_fill_triangle", "hcgb_tile_cholesky"):
             getattr(L, nm).restype = C.c_int
         L.hcgb_set_k_order.restype = C.c_int
         L.hcgb_compress_tile.argtypes = [vp, vp, ip, ip, C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int)]

@@ -120,7 +120,35 @@ __global__ void fill_triangle_kernel(int uplo, int n, double *A, int lda, double
     if (uplo == 0 ? (i > j) : (i < j)) A[i + (size_t) j * lda] = value;
 }
 
+// Panel solve of a tile Cholesky step: for every compressed_vt tile of the panel, W <- L^-1 W
+// (Left, Lower, NoTrans, NonUnit, alpha 1 on the W region, rows x rank, ld rows): HCore<T>::Trsm
+// as the tile Cholesky applies it (src/api/HCore.cpp:623-647), one CTA per tile, the rank read on
+// the device.  Same operations in the same order as trsm_kernel, so the results are identical.
+__global__ void __launch_bounds__(256) trsm_panel_kernel(const double *L, int nb, int ldl, const DevTile *tiles) {
+    const DevTile t = tiles[blockIdx.x];
+    const int r = *t.rank;
+    if (r <= 0 || r > t.max_rank || t.rows != nb) return;
+    double *W = t.v;
+    const int ld = t.rows;
+    for (int i = 0; i < nb; i++) {
+        const double lii = L[i + (size_t) i * ldl];
+        for (int c = threadIdx.x; c < r; c += blockDim.x) W[i + (size_t) c * ld] /= lii;
+        __syncthreads();
+        const int rest = nb - 1 - i;
+        for (int e = threadIdx.x; e < rest * r; e += blockDim.x) {
+            const int q = e % rest, c = e / rest;
+            const int k = i + 1 + q;
+            W[k + (size_t) c * ld] = fma(-L[k + (size_t) i * ldl], W[i + (size_t) c * ld], W[k + (size_t) c * ld]);
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+void launch_trsm_panel(const double *L, int nb, int ldl, const DevTile *tiles, int count, cudaStream_t st) {
+    if (count > 0) trsm_panel_kernel<<<count, 256, 0, st>>>(L, nb, ldl, tiles);
+}
 
 void launch_fill_triangle(int uplo, int n, double *A, int lda, double value, cudaStream_t st) {
     dim3 blk(32, 8), grid((n + 31) / 32, (n + 7) / 8);

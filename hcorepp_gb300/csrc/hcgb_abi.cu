@@ -85,6 +85,7 @@ DevTile to_dev(const hcgb_tile &t) {
     d.cols = t.cols;
     d.max_rank = compressed(t.kind) ? t.max_rank : 0;
     d.kind = compressed(t.kind) ? t.kind : 0;
+    d.v = compressed(t.kind) ? t.data + (size_t) t.rows * t.max_rank : nullptr;
     return d;
 }
 
@@ -835,4 +836,92 @@ extern "C" int hcgb_fill_triangle(hcgb_context *ctx, int uplo, int n, double *A,
     launch_fill_triangle(uplo, n, A, lda, value, ctx->stream);
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
+}
+
+extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *grid, const hcgb_params *params,
+                                  int *info, hcgb_update_info *info_dev) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (nt <= 0 || !grid) return fail(ctx, HCGB_BAD_ARG, "hcgb_tile_cholesky: bad grid");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int nb = grid[0].rows;
+    for (int j = 0; j < nt; j++)
+        for (int i = j; i < nt; i++) {
+            const hcgb_tile &t = grid[i + (size_t) j * nt];
+            int rc;
+            if ((rc = check_tile(ctx, t, "A"))) return rc;
+            const bool want = i == j ? t.kind == HCGB_DENSE : t.kind == HCGB_COMPRESSED_VT;
+            if (!want || t.rows != nb || t.cols != nb)
+                return fail(ctx, HCGB_BAD_ARG,
+                            "hcgb_tile_cholesky: nb x nb tiles, dense on the diagonal, compressed_vt below");
+        }
+    if (info) *info = 0;
+    int *dinfo = nullptr;
+    DevTile *dpanel = nullptr;
+    HCGB_CUDA(ctx, cudaMalloc(&dinfo, sizeof(int) * (size_t) nt));
+    if (cudaMalloc(&dpanel, sizeof(DevTile) * (size_t) nt) != cudaSuccess) {
+        cudaFree(dinfo);
+        return fail(ctx, HCGB_CUDA_ERROR, "hcgb_tile_cholesky: cudaMalloc failed");
+    }
+    auto done = [&](int rc) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(dinfo);
+        cudaFree(dpanel);
+        return rc;
+    };
+    const Params p = to_params(params);
+    const int chunk = 1024;  // updates per pipeline launch (bounds the workspace)
+    int uid = 0;
+    auto tile = [&](int i, int j) -> const hcgb_tile & { return grid[i + (size_t) j * nt]; };
+    for (int k = 0; k < nt; k++) {
+        // Syrk leaves the strict upper triangle of a diagonal tile zero (HCore.cpp:555-563).
+        if (k > 0) launch_fill_triangle(HCGB_UPPER, nb, tile(k, k).data, nb, 0.0, ctx->stream);
+        launch_potrf(tile(k, k).data, nb, nb, HCGB_LOWER, dinfo + k, ctx->stream);
+        int h = 0;
+        cudaError_t e = cudaMemcpyAsync(&h, dinfo + k, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return done(fail(ctx, HCGB_CUDA_ERROR, std::string("hcgb_tile_cholesky: ") +
+                                                                     cudaGetErrorString(e)));
+        if (h) {
+            if (info) *info = k * nb + h;
+            return done(HCGB_OK);
+        }
+        if (k == nt - 1) break;
+        // Panel: W_ik <- L_kk^-1 W_ik for every i > k.
+        std::vector<DevTile> panel;
+        for (int i = k + 1; i < nt; i++) panel.push_back(to_dev(tile(i, k)));
+        HCGB_CUDA(ctx, cudaMemcpyAsync(dpanel, panel.data(), sizeof(DevTile) * panel.size(), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+        launch_trsm_panel(tile(k, k).data, nb, nb, dpanel, (int) panel.size(), ctx->stream);
+        HCGB_CUDA(ctx, cudaGetLastError());
+        // Trailing updates A_ij -= A_ik A_jk^T (j <= i): Syrk on the diagonal, Gemm(aCholesky) below.
+        // B = A_jk^T is the stored compressed_vt tile with its factors swapped (U' = W, W' = U).
+        std::vector<hcgb_update> hu;
+        std::vector<DevUpdate> dv;
+        for (int i = k + 1; i < nt; i++)
+            for (int j = k + 1; j <= i; j++) {
+                const hcgb_tile &ta = tile(i, k), &tb = tile(j, k), &tc = tile(i, j);
+                hcgb_tile tbt = tb;
+                tbt.rows = tb.cols;
+                tbt.cols = tb.rows;
+                hu.push_back(hcgb_update{ta, tbt, tc});
+                DevTile db = to_dev(tb);
+                std::swap(db.data, db.v);
+                std::swap(db.rows, db.cols);
+                dv.push_back(DevUpdate{to_dev(ta), db, to_dev(tc), uid++});
+            }
+        for (size_t off = 0; off < dv.size(); off += chunk) {
+            const int n = (int) std::min<size_t>(chunk, dv.size() - off);
+            std::vector<DevUpdate> part(dv.begin() + off, dv.begin() + off + n);
+            BatchShape sh = shape_of(hu.data() + off, n);
+            Workspace ws;
+            int rc = prepare_workspace(ctx, sh, n, false, &ws);
+            if (rc) return done(rc);
+            DevUpdate *dups;
+            GemmJob *djobs;
+            if ((rc = upload_updates(ctx, part, &dups, &djobs))) return done(rc);
+            launch_pipeline(ctx, ctx->stream, dups, djobs, n, -1.0, 1.0, ws, sh, p, info_dev);
+            HCGB_CUDA(ctx, cudaGetLastError());
+        }
+    }
+    return done(HCGB_OK);
 }

@@ -54,7 +54,9 @@ struct GemmJob {
 };
 
 struct DevTile {
-    double *data;
+    double *data;  // U (rows x rank, ld rows), or the dense tile
+    double *v;     // V region: data + rows * max_rank for a stored tile; the U buffer of the stored tile
+                   // when this descriptor is the transpose of a compressed_vt tile (factors swapped)
     int *rank;
     int rows, cols, max_rank, kind;
 };
@@ -134,6 +136,7 @@ void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t
 void launch_transpose(const double *src, int lds, int rows, int cols, double *dst, int ldd, cudaStream_t st);
 
 // Dense tile building blocks of a tile Cholesky (chol.cu).
+void launch_trsm_panel(const double *L, int nb, int ldl, const DevTile *tiles, int count, cudaStream_t st);
 void launch_fill_triangle(int uplo, int n, double *A, int lda, double value, cudaStream_t st);
 void launch_potrf(double *A, int n, int lda, int uplo, int *info_dev, cudaStream_t st);
 void launch_trsm(int side, int uplo, int trans, int diag, int m, int n, double alpha, const double *A, int lda,

@@ -115,6 +115,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
         d.cols = t->cols;
         d.max_rank = t->kind == HCGB_COMPRESSED ? t->max_rank : 0;
         d.kind = t->kind == HCGB_COMPRESSED ? 1 : 0;
+        d.v = t->kind == HCGB_COMPRESSED ? t->data + (size_t) t->rows * t->max_rank : nullptr;
         return d;
     };
     DevUpdate u{dev_tile(a), dev_tile(b), dev_tile(c), 0};

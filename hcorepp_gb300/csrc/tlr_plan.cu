@@ -71,9 +71,9 @@ __global__ void plan_kernel(const DevUpdate *ups, int n, double alpha, double be
     double *T1 = slot + ws.off_tmp1;  // rmax x rmax, ld rmax
     double *T2 = slot + ws.off_tmp2;  // ld x rmax (ld ld) or rmax x ld (ld rmax)
     const int ld = ws.ld, lr = ws.rmax;
-    // Compressed views: U at data (ld rows), V at data + rows*max_rank (ld rank).
-    const double *Au = u.a.data, *Av = u.a.data + (size_t) u.a.rows * u.a.max_rank;
-    const double *Bu = u.b.data, *Bv = u.b.data + (size_t) u.b.rows * u.b.max_rank;
+    // Compressed views: U at data (ld rows), V region at v (ld rank, or ld cols when compressed_vt).
+    const double *Au = u.a.data, *Av = u.a.v;
+    const double *Bu = u.b.data, *Bv = u.b.v;
     const double *Ad = u.a.data, *Bd = u.b.data;
     // V factors as GEMM operands: V (rank x cols, ld rank), or for a compressed_vt tile the stored
     // W = V^T (cols x rank, ld cols) read with the opposite op.
@@ -177,14 +177,14 @@ __global__ void __launch_bounds__(256) stack_kernel(const DevUpdate *ups, double
     double *Us = slot + ws.off_ustack;
     double *Vs = slot + ws.off_vstack;
     const int ld = ws.ld;
-    const double *Cu = u.c.data, *Cv = u.c.data + (size_t) u.c.rows * u.c.max_rank;
+    const double *Cu = u.c.data, *Cv = u.c.v;
     copy_scaled(Cu, m, m, rC, Us, ld, 1.0);                                      // U[:, :rC] = Cu
     if (side == 0 && u.a.kind) copy_scaled(u.a.data, m, m, rA, Us + (size_t) rC * ld, ld, alpha);  // alpha Au
     // V[:, :rC] = beta Cv^T; a compressed_vt C stores Cv^T itself (ProcessVpointer's Cholesky copy)
     if (u.c.kind == HCGB_COMPRESSED_VT) copy_scaled(Cv, nn, nn, rC, Vs, ld, beta);
     else transpose_scaled(Cv, rC, rC, nn, Vs, ld, beta, tile);
     if (side == 1 && u.b.kind) {
-        const double *Bv = u.b.data + (size_t) u.b.rows * u.b.max_rank;
+        const double *Bv = u.b.v;
         if (u.b.kind == HCGB_COMPRESSED_VT) copy_scaled(Bv, nn, nn, rB, Vs + (size_t) rC * ld, ld, 1.0);
         else transpose_scaled(Bv, rB, rB, nn, Vs + (size_t) rC * ld, ld, 1.0, tile);  // V[:, rC:] = Bv^T
     }
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(const DevUpdate *ups, Wor
     const DevUpdate u = ups[s];
     const int r = meta[META_NEWRANK], nn = meta[META_N];
     const double *XV = ws.slot(s) + ws.off_xv;
-    double *Cv = u.c.data + (size_t) u.c.rows * u.c.max_rank;
+    double *Cv = u.c.v;
     if (u.c.kind == HCGB_COMPRESSED_VT) copy_scaled(XV, ws.ld, nn, r, Cv, nn, 1.0);  // W = XV (n x r, ld n)
     else transpose_scaled(XV, ws.ld, nn, r, Cv, r, 1.0, tile);
     if (threadIdx.x == 0) *u.c.rank = r;
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256) ddc_finalize_kernel(const DevUpdate *ups,
     const int r = m < nn ? m : nn;
     const double *W = ws.slot(s) + ws.off_tmp2;
     double *U = u.c.data;
-    double *V = u.c.data + (size_t) m * u.c.max_rank;
+    double *V = u.c.v;
     for (int j = 0; j < r; j++)
         for (int i = threadIdx.x; i < m; i += blockDim.x) U[i + (size_t) j * m] = W[i + (size_t) j * ws.ld];
     // V = I (r x n, ld r); a compressed_vt C stores W = V^T (n x r, ld n), the same identity pattern.

@@ -313,11 +313,16 @@ def Syrk(alpha, a, a_op, uplo, beta, c: DenseTile, params=None):
     ctx.check(L.lib().hcgb_fill_triangle(ctx.handle, other, n, _dptr(c.buffer), n, 0.0))
 
 
-def tile_cholesky(a: "TileMatrix", params: CompressionParameters) -> int:
+def tile_cholesky(a: "TileMatrix", params: CompressionParameters, batched: bool = True,
+                  info: torch.Tensor | None = None) -> int:
     """Right-looking tile Cholesky A = L L^T of a symmetric positive definite tile matrix: dense
     diagonal tiles, compressed tiles below the diagonal in the Cholesky-flow layout (TileMatrix with
-    ``vt=True``: tile = U W^T), tiles above the diagonal not referenced.  The reference provides the
-    per-tile operations but no driver; this loop composes them:
+    ``vt=True``: tile = U W^T), tiles above the diagonal not referenced.
+
+    ``batched=True``: hcgb_tile_cholesky, one panel-solve launch and batched trailing updates per
+    step (``info``, optional, from ``info_buffer(nt*(nt*nt-1)//6)``, gets the update records).
+    ``batched=False``: the reference's per-tile operations called one by one; the reference provides
+    them but no driver, and this loop composes them:
       Potrf(A_kk, Lower)                                                  HCore.cpp:585-621
       Trsm(Left, Lower, NoTrans, NonUnit, 1, A_kk, A_ik): W_ik <- L_kk^-1 W_ik   HCore.cpp:623-647
       Syrk(-1, A_ik, NoTrans, Lower, 1, A_ii)                             HCore.cpp:482-583
@@ -327,6 +332,14 @@ def tile_cholesky(a: "TileMatrix", params: CompressionParameters) -> int:
     if not a.vt:
         raise ValueError("tile_cholesky needs a TileMatrix in the Cholesky-flow layout (vt=True)")
     nt, nb = a.mt, a.nb
+    if batched:
+        ctx = run_context()
+        grid = a.c_grid()
+        p = params.c()
+        res = C.c_int(0)
+        sp = C.c_void_p(info.data_ptr()) if info is not None else None
+        ctx.check(L.lib().hcgb_tile_cholesky(ctx.handle, nt, grid, C.byref(p), C.byref(res), sp))
+        return res.value
     for k in range(nt):
         akk = a.tile(k, k)
         info = Potrf(akk, L.LOWER)

@@ -190,6 +190,19 @@ int hcgb_trsm(hcgb_context *ctx, int side, int uplo, int trans, int diag, int m,
  * semantics; replaces HCoreKernels::syrk (src/kernels/cuda/kernels.cpp:299-306).  Asynchronous. */
 int hcgb_syrk(hcgb_context *ctx, int uplo, int trans, int n, int k, double alpha, const double *A, int lda,
               double beta, double *C, int ldc);
+/* Tile Cholesky A = L L^T of an nt x nt tile matrix (grid: nt*nt descriptors, column-major; only
+ * i >= j is read): nb x nb tiles, dense on the diagonal, HCGB_COMPRESSED_VT below it (tile = U W^T).
+ * The reference provides the per-tile operations but no driver; this composes them right-looking:
+ * for each k, Potrf(A_kk) (src/api/HCore.cpp:585-621), the panel Trsm W_ik <- L_kk^-1 W_ik
+ * (:623-647) in one launch, and every trailing update A_ij -= A_ik A_jk^T, j <= i -- Syrk on the
+ * diagonal (:482-583), Gemm(aCholesky) below (:23-344) -- batched into pipeline launches of up to
+ * 1024 updates.  Synchronous (one host wait per step, on the potrf info).  *info (if not NULL)
+ * receives 0 or k * nb + the potrf info of the first failing diagonal tile.  info_dev (optional)
+ * receives one hcgb_update_info per trailing update, in step order (k ascending; within a step
+ * i ascending, then j = k+1 .. i). */
+int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *grid, const hcgb_params *params, int *info,
+                       hcgb_update_info *info_dev);
+
 /* Sets the strict uplo triangle of A (n x n, ld lda) to value; replaces
  * HCoreKernels::FillMatrixTriangle (src/kernels/omp/kernels.cpp:246-264), which HCore<T>::Syrk
  * applies after a compressed-A update (src/api/HCore.cpp:555-563).  Asynchronous. */

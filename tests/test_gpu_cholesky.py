@@ -188,8 +188,9 @@ def test_tile_cholesky_residual(T):
     """Tile Cholesky of an SPD exponential-kernel matrix (2-D points, length scale 0.1, 4 x 4 tiles
     of 256, dense diagonal tiles, off-diagonal tiles compressed at 1e-8 with the reference's
     capacity nb/3, Cholesky-flow layout): residual ||L L^T - A||_F / ||A||_F and agreement with the
-    oracle's driver.  Tiles whose 1e-8 rank would exceed nb/3 are clamped there, which bounds the
-    residual near 1e-8 rather than at it."""
+    oracle's driver; the batched driver (hcgb_tile_cholesky) and the per-tile loop give identical
+    factors.  Tiles whose 1e-8 rank would exceed nb/3 are clamped there, which bounds the residual
+    near 1e-8 rather than at it."""
     from hcorepp_gb300 import _lib as L
     from hcorepp_gb300.problems import KernelMatrix
     nt, nb, acc = 4, 256, 1e-8
@@ -209,7 +210,16 @@ def test_tile_cholesky_residual(T):
                 tm.set_tile(i, j, u=t.u, v=t.v)
                 og[i][j] = O.CholeskyTile(t.u, t.v.T, t.max_rank)
     params = T.CompressionParameters(acc, truncated_svd=True)
-    assert T.tile_cholesky(tm, params) == 0
+    tm2 = T.TileMatrix(nt, nt, nb, kinds, nb // 3, vt=True)
+    tm2.arena.copy_(tm.arena)
+    tm2.ranks.copy_(tm.ranks)
+    info = T.info_buffer(nt * (nt * nt - 1) // 6)
+    assert T.tile_cholesky(tm, params, batched=True, info=info) == 0
+    assert int(info[:, 0].max()) == 0
+    assert T.tile_cholesky(tm2, params, batched=False) == 0
+    # the batched driver runs the per-tile operations' arithmetic: bit-identical factors
+    np.testing.assert_array_equal(tm.ranks.cpu().numpy(), tm2.ranks.cpu().numpy())
+    np.testing.assert_array_equal(tm.arena.cpu().numpy(), tm2.arena.cpu().numpy())
     assert O.tile_cholesky(og, nt, O.CompressionParameters(acc, truncated_svd=True)) == 0
     full = tm.to_dense()
     lfac = np.zeros_like(full)
@@ -226,3 +236,20 @@ def test_tile_cholesky_residual(T):
     res_o = rel_fro(ofac @ ofac.T, a_dense)
     assert res < 1e-7 and res <= 2 * max(res_o, acc), (res, res_o)
     assert rel_fro(lfac, ofac) < 1e-5
+
+
+def test_tile_cholesky_not_positive_definite(T):
+    """A failing diagonal block stops the factorisation with k * nb + the potrf info."""
+    from hcorepp_gb300 import _lib as L
+    nt, nb = 3, 64
+    rng = np.random.default_rng(4)
+    kinds = [[L.DENSE if i == j else L.COMPRESSED for j in range(nt)] for i in range(nt)]
+    tm = T.TileMatrix(nt, nt, nb, kinds, nb // 3, vt=True)
+    for i in range(nt):
+        d = np.eye(nb) * 4.0
+        if i == 1:
+            d[10, 10] = -1.0
+        tm.set_tile(i, i, dense=d)
+        for j in range(i):
+            tm.set_tile(i, j, u=rng.standard_normal((nb, 2)) * 1e-3, v=rng.standard_normal((2, nb)))
+    assert T.tile_cholesky(tm, T.CompressionParameters(1e-8, truncated_svd=True)) == nb + 11
