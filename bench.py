@@ -409,6 +409,8 @@ def gpu_arm(args, rank, world, local):
         "stages_ms_serial_step": {s: stages[s][0] for s in stages},
         "serial_step_ms": serial_ms,
         "stage_share": {s: stages[s][0] / total_stage_ms for s in stages},
+        "stage_algorithmic_tflops": {s: st_flops[s] / (stages[s][0] * 1e-3) / 1e12 for s in st_flops
+                                     if s in stages and stages[s][0] > 0},
         "gpu_launches": launches,
         "ranks": {"mean_final": float(rk[comp_mask].mean()), "max_final": int(rk[comp_mask].max()),
                   "updates_at_capacity": clamped, "bad_status": bad,

@@ -212,6 +212,10 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
     for (int i = 0; i < 4; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) acc[i][j][0] = acc[i][j][1] = 0.0;
+    // 8x8 blocks of this warp's 32x32 sub-tile that intersect the job
+    const int rem_m = jb.M - (m0 + wm * 32), rem_n = jb.N - (n0 + wn * 32);
+    const int mblk = rem_m <= 0 ? 0 : (rem_m >= 32 ? 4 : (rem_m + 7) >> 3);
+    const int nblk = rem_n <= 0 ? 0 : (rem_n >= 32 ? 4 : (rem_n + 7) >> 3);
 
     for (int k0 = 0; k0 < jb.K; k0 += GK) {
         for (int e = threadIdx.x; e < GT * GK; e += blockDim.x) {
@@ -245,8 +249,13 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
             Bs[kk][j] = v;
         }
         __syncthreads();
+        // The FP64 pipe is the limit: no MMA is issued for 8x8 blocks or k-steps that lie wholly
+        // outside the job (small factor products fill a fraction of the 64x64 tile).  All
+        // conditions are warp-uniform.
+        const int kend = jb.K - k0 < GK ? jb.K - k0 : GK;
 #pragma unroll
         for (int kk = 0; kk < GK; kk += 4) {
+            if (kk >= kend) break;
             double af[4], bf[4];
 #pragma unroll
             for (int i = 0; i < 4; i++) af[i] = As[wm * 32 + i * 8 + lr][kk + lc];
@@ -255,7 +264,8 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
-                for (int j = 0; j < 4; j++) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
+                for (int j = 0; j < 4; j++)
+                    if (i < mblk && j < nblk) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
         }
         __syncthreads();
     }

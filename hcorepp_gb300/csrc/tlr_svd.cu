@@ -185,9 +185,13 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
 template <typename T, bool ACC, int MAXRPL>
 __device__ void jacobi_dispatch(T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax,
                                 int *sweeps, bool *conv, double tol, int max_sweeps, T *J = nullptr, int ldj = 0) {
-    if (rows <= 32) jacobi<T, 8, 4, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
+    // Fewer lanes per pair put more pairs in one warp instruction, so the per-pair scalar work
+    // (tangent, tests, norm updates) is shared by 2-4 pairs; RPL rows per lane stay in registers.
+    if (rows <= 32) jacobi<T, 4, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
     else if (rows <= 64) jacobi<T, 8, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
+    else if (rows <= 128 && MAXRPL >= 16) jacobi<T, 8, 16, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
     else if (rows <= 128) jacobi<T, 16, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
+    else if (rows <= 256 && MAXRPL >= 16) jacobi<T, 16, 16, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
     else if (rows <= 256 || MAXRPL <= 8) jacobi<T, 32, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
     else jacobi<T, 32, MAXRPL, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
 }
@@ -402,15 +406,19 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     __syncthreads();
 
     // 2. Rank-revealing QR with column pivoting, M P = Q R, stopped once every remaining column
-    //    is below 1e-4 of the truncation threshold: the dropped block R22 changes no singular
-    //    value by more than sqrt(kV) * 1e-4 * threshold.  (Fixed-rank mode keeps every row.)
+    //    is below QRCP_STOP (1e-2) of the truncation threshold.  The dropped block R22 lies far
+    //    below the threshold: it cannot carry a kept singular value, it moves the kept ones by at
+    //    most ||R22||_2 <= sqrt(kV) * 1e-2 * threshold (in practice ~1e-6 relative), and it only
+    //    holds directions the truncation discards anyway.  The Jacobi stage then works on the
+    //    rk rows above it.  (Fixed-rank mode keeps every row.)
+    constexpr double QRCP_STOP = 1e-2;
     double stop2 = -1.0, rel = 0.0;
     if (p.fixed_rank <= 0) {
         if (p.truncated) {
             stop2 = 0.0;
-            rel = 1e-4 * p.accuracy;  // |r_00| <= sigma_0, so this threshold is conservative
+            rel = QRCP_STOP * p.accuracy;  // |r_00| <= sigma_0, so this threshold is conservative
         } else {
-            stop2 = (1e-4 * p.accuracy) * (1e-4 * p.accuracy);
+            stop2 = (QRCP_STOP * p.accuracy) * (QRCP_STOP * p.accuracy);
         }
     }
     const long long t1 = clock64();
