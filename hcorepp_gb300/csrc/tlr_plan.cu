@@ -205,17 +205,19 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
     __shared__ double As[GT][AS_LD];
     __shared__ double Bs[GK][BS_LD];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wm = warp & 1, wn = warp >> 1;
     const int lr = lane >> 2, lc = lane & 3;
-    double acc[4][4][2];
+    // Warp w owns 8-row blocks w and w + 4 of the tile and all eight 8-column blocks, so a small
+    // job (say 30 x 30) still spreads over the four warps -- one per SM sub-partition and FP64
+    // pipe -- instead of landing on one warp.
+    const int rb0 = warp, rb1 = warp + 4;
+    const int rem_m = jb.M - m0, rem_n = jb.N - n0;
+    const bool r0ok = rb0 * 8 < rem_m, r1ok = rb1 * 8 < rem_m;
+    const int nblk = rem_n <= 0 ? 0 : (rem_n >= 64 ? 8 : (rem_n + 7) >> 3);
+    double acc[2][8][2];
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < 2; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j][0] = acc[i][j][1] = 0.0;
-    // 8x8 blocks of this warp's 32x32 sub-tile that intersect the job
-    const int rem_m = jb.M - (m0 + wm * 32), rem_n = jb.N - (n0 + wn * 32);
-    const int mblk = rem_m <= 0 ? 0 : (rem_m >= 32 ? 4 : (rem_m + 7) >> 3);
-    const int nblk = rem_n <= 0 ? 0 : (rem_n >= 32 ? 4 : (rem_n + 7) >> 3);
+        for (int j = 0; j < 8; j++) acc[i][j][0] = acc[i][j][1] = 0.0;
 
     for (int k0 = 0; k0 < jb.K; k0 += GK) {
         for (int e = threadIdx.x; e < GT * GK; e += blockDim.x) {
@@ -256,31 +258,32 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
 #pragma unroll
         for (int kk = 0; kk < GK; kk += 4) {
             if (kk >= kend) break;
-            double af[4], bf[4];
+            const double af0 = As[rb0 * 8 + lr][kk + lc], af1 = As[rb1 * 8 + lr][kk + lc];
+            double bf[8];
 #pragma unroll
-            for (int i = 0; i < 4; i++) af[i] = As[wm * 32 + i * 8 + lr][kk + lc];
+            for (int j = 0; j < 8; j++) bf[j] = Bs[kk + lc][j * 8 + lr];
 #pragma unroll
-            for (int j = 0; j < 4; j++) bf[j] = Bs[kk + lc][wn * 32 + j * 8 + lr];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++)
-                    if (i < mblk && j < nblk) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
+            for (int j = 0; j < 8; j++)
+                if (j < nblk) {
+                    if (r0ok) dmma(acc[0][j][0], acc[0][j][1], af0, bf[j]);
+                    if (r1ok) dmma(acc[1][j][0], acc[1][j][1], af1, bf[j]);
+                }
         }
         __syncthreads();
     }
+    const bool scale = jb.alpha != 1.0, accum = jb.beta != 0.0;
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < 2; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++)
+        for (int j = 0; j < 8; j++)
 #pragma unroll
             for (int e = 0; e < 2; e++) {
-                const int row = m0 + wm * 32 + i * 8 + lr;
-                const int col = n0 + wn * 32 + j * 8 + 2 * lc + e;
+                const int row = m0 + (i ? rb1 : rb0) * 8 + lr;
+                const int col = n0 + j * 8 + 2 * lc + e;
                 if (row < jb.M && col < jb.N) {
                     double *c = jb.C + row + (size_t) col * jb.ldc;
-                    double v = jb.alpha * acc[i][j][e];
-                    if (jb.beta != 0.0) v += jb.beta * *c;
+                    double v = scale ? jb.alpha * acc[i][j][e] : acc[i][j][e];
+                    if (accum) v = fma(jb.beta, *c, v);
                     *c = v;
                 }
             }

@@ -63,9 +63,16 @@ __device__ __forceinline__ float jacobi_tangent(double a, double b, double c) {
 // inner product.  A pair is rotated when c^2 > tol2 a b and both columns are above the noise
 // floor `tiny`; columns below it hold only rounding errors of the larger ones.
 // With ACC the same rotations are accumulated into the columns of J (ncols x ncols, ld ldj).
+//
+// Without ACC the rotations are applied in scaled form (the idea of fast Givens rotations): column
+// i is stored as x_i with the true column d_i x_i, so the rotation
+//   X_i' = cos (X_i - t X_j),  X_j' = cos (X_j + t X_i)
+// becomes x_i' = x_i - t (d_j / d_i) x_j, x_j' = x_j + t (d_i / d_j) x_i, d' = cos d: one FMA per
+// element instead of a multiply and an FMA.  d and 1/d live in dsc[0..) and dsc[dstride..);
+// the caller folds them back into the columns at the start of every sweep.
 template <typename T, int G, int RPL, bool ACC>
 __device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, double tol2, double tiny, int n2,
-                            T *J, int ldj) {
+                            T *J, int ldj, double *dsc, int dstride) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     constexpr int PPW = 32 / G;
     const int gl = lane % G, grp = lane / G;
@@ -99,9 +106,39 @@ __device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, dou
             }
             c = group_sum(c, G);
             const double a = act ? nrm[i] : 0.0, b = act ? nrm[j] : 0.0;
-            const double cd = (double) c;
+            double di = 1.0, dj = 1.0;
+            if (!ACC && act) {
+                di = dsc[i];
+                dj = dsc[j];
+            }
+            const double cd = ACC ? (double) c : (double) c * di * dj;  // true inner product
             const bool rot = act && a > tiny && b > tiny && cd * cd > tol2 * a * b;
-            if (rot) {
+            if (!ACC && rot) {
+                const double tt = (double) jacobi_tangent(a, b, cd);
+                const double q = fma(tt, tt, 1.0);
+                const double cs = rsqrt(q);
+                const double dvi = dsc[dstride + i], dvj = dsc[dstride + j];
+                const T t1 = (T) (tt * dj * dvi), t2 = (T) (tt * di * dvj);
+#pragma unroll
+                for (int q2 = 0; q2 < RPL; q2++) {
+                    if (G * q2 < rows) {
+                        const int r = gl + G * q2;
+                        if (r < rows) {
+                            x[r] = fma(-t1, yr[q2], xr[q2]);
+                            y[r] = fma(t2, xr[q2], yr[q2]);
+                        }
+                    }
+                }
+                if (gl == 0) {
+                    nrm[i] = a - tt * cd;
+                    nrm[j] = b + tt * cd;
+                    dsc[i] = di * cs;
+                    dsc[j] = dj * cs;
+                    dsc[dstride + i] = dvi * q * cs;
+                    dsc[dstride + j] = dvj * q * cs;
+                    rotations++;
+                }
+            } else if (ACC && rot) {
                 const float tf = jacobi_tangent(a, b, cd);
                 const T tt = (T) tf;
                 const T cs = rsqrt_t(fma(tt, tt, T(1)));
@@ -140,7 +177,7 @@ __device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, dou
 // until no pair rotates (or max_sweeps).
 template <typename T, int G, int RPL, bool ACC>
 __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax, int *sweeps_out,
-                       bool *converged_out, double tol, int max_sweeps, T *J = nullptr, int ldj = 0) {
+                       bool *converged_out, double tol, int max_sweeps, T *J, int ldj, double *dsc, int dstride) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const double tol2 = tol * tol;
     // Noise floor from double precision also for single-precision sweeps: X is graded (each column
@@ -149,6 +186,32 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
     const int n2 = ncols + (ncols & 1);
     int sweeps = 0;
     bool converged = ncols < 2;
+    if (!ACC) {
+        for (int j = threadIdx.x; j < ncols; j += blockDim.x) dsc[j] = dsc[dstride + j] = 1.0;
+        __syncthreads();
+    }
+    // Exact squared norms; the scales d of the previous sweep are folded into the columns.
+    auto fold_and_norms = [&](double &amax) {
+        for (int j = warp; j < ncols; j += nw) {
+            T *col = X + (size_t) j * ldx;
+            const double dj = ACC ? 1.0 : dsc[j];
+            double sq = 0.0;
+            for (int r = lane; r < rows; r += 32) {
+                double v = (double) col[r];
+                if (!ACC && dj != 1.0) {
+                    v *= dj;
+                    col[r] = (T) v;
+                }
+                sq = fma(v, v, sq);
+            }
+            sq = warp_sum(sq);
+            if (lane == 0) {
+                nrm[j] = sq;
+                if (!ACC) dsc[j] = dsc[dstride + j] = 1.0;
+            }
+            amax = fmax(amax, sq);
+        }
+    };
     while (!converged && sweeps < max_sweeps) {
         if (threadIdx.x == 0) {
             *s_rot = 0;
@@ -156,25 +219,20 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
         }
         __syncthreads();
         double amax = 0.0;
-        for (int j = warp; j < ncols; j += nw) {
-            const T *col = X + (size_t) j * ldx;
-            double sq = 0.0;
-            for (int r = lane; r < rows; r += 32) {
-                const double v = (double) col[r];
-                sq = fma(v, v, sq);
-            }
-            sq = warp_sum(sq);
-            if (lane == 0) nrm[j] = sq;
-            amax = fmax(amax, sq);
-        }
+        fold_and_norms(amax);
         if (lane == 0) atomicMax(reinterpret_cast<unsigned long long *>(s_amax), __double_as_longlong(amax));
         __syncthreads();
         const double tiny = *s_amax * noise * noise;
-        const int rot = jacobi_sweep<T, G, RPL, ACC>(X, ldx, rows, ncols, nrm, tol2, tiny, n2, J, ldj);
+        const int rot = jacobi_sweep<T, G, RPL, ACC>(X, ldx, rows, ncols, nrm, tol2, tiny, n2, J, ldj, dsc, dstride);
         if (rot) atomicAdd(s_rot, rot);
         __syncthreads();
         sweeps++;
         converged = (*s_rot == 0);
+        __syncthreads();
+    }
+    if (!ACC) {  // a sweep limit can leave scales unfolded
+        double amax = 0.0;
+        fold_and_norms(amax);
         __syncthreads();
     }
     *sweeps_out = sweeps;
@@ -184,16 +242,17 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
 // Lane-group / register-tile choice for a column length: G lanes per pair, RPL rows per lane.
 template <typename T, bool ACC, int MAXRPL>
 __device__ void jacobi_dispatch(T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax,
-                                int *sweeps, bool *conv, double tol, int max_sweeps, T *J = nullptr, int ldj = 0) {
+                                int *sweeps, bool *conv, double tol, int max_sweeps, T *J, int ldj, double *dsc,
+                                int dstride) {
     // Fewer lanes per pair put more pairs in one warp instruction, so the per-pair scalar work
     // (tangent, tests, norm updates) is shared by 2-4 pairs; RPL rows per lane stay in registers.
-    if (rows <= 32) jacobi<T, 4, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
-    else if (rows <= 64) jacobi<T, 8, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
-    else if (rows <= 128 && MAXRPL >= 16) jacobi<T, 8, 16, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
-    else if (rows <= 128) jacobi<T, 16, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
-    else if (rows <= 256 && MAXRPL >= 16) jacobi<T, 16, 16, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
-    else if (rows <= 256 || MAXRPL <= 8) jacobi<T, 32, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
-    else jacobi<T, 32, MAXRPL, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj);
+    if (rows <= 32) jacobi<T, 4, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 64) jacobi<T, 8, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 128 && MAXRPL >= 16) jacobi<T, 8, 16, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 128) jacobi<T, 16, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 256 && MAXRPL >= 16) jacobi<T, 16, 16, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 256 || MAXRPL <= 8) jacobi<T, 32, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else jacobi<T, 32, MAXRPL, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
 }
 
 // Householder QR with column pivoting of A (mrows x ncols, ld lda) in place, stopped early once
@@ -362,7 +421,8 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     double *nrm = inv + ws.kmax;
     int *perm = reinterpret_cast<int *>(nrm + ws.kmax);
     int *pvt = perm + ws.kmax;
-    double *red = nrm + ws.kmax + ws.kmax + 1;
+    double *dsc = nrm + ws.kmax + ws.kmax + 1;  // Jacobi column scales d and 1/d (2 kmax)
+    double *red = dsc + 2 * ws.kmax;
     int *redi = reinterpret_cast<int *>(red + 48);
     double *pool = red + 48 + 24;
     const int pool_doubles = smem_doubles - (int) (pool - sm);
@@ -454,7 +514,8 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         int sw32 = 0;
         bool conv32 = true;
         jacobi_dispatch<float, true, RPL>(X32, kV, kV, rk, nrm, &s_rot, &s_amax, &sw32, &conv32,
-                                          4.0 * FLT_EPSILON * sqrt((double) kV), MAX_JACOBI_SWEEPS, J32, rk);
+                                          4.0 * FLT_EPSILON * sqrt((double) kV), MAX_JACOBI_SWEEPS, J32, rk, dsc,
+                                          ws.kmax);
         // W = X J32 (kV x rk) on DMMA into XV, then back into X.
         {
             const int ntr = (kV + 7) >> 3, ntc = (rk + 7) >> 3;
@@ -478,11 +539,11 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
             __syncthreads();
         }
         jacobi_dispatch<double, false, RPL>(X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
-                                            MAX_JACOBI_SWEEPS);
+                                            MAX_JACOBI_SWEEPS, (double *) nullptr, 0, dsc, ws.kmax);
         sweeps += 100 * sw32;  // record: single-precision sweeps in the hundreds
     } else {
         jacobi_dispatch<double, false, RPL>(X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
-                                            MAX_JACOBI_SWEEPS);
+                                            MAX_JACOBI_SWEEPS, (double *) nullptr, 0, dsc, ws.kmax);
     }
 
     const long long t3 = clock64();
@@ -578,7 +639,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
 }  // namespace
 
 size_t svd_smem_bytes(int kmax) {
-    size_t aux = (size_t) 4 * kmax + 1 + 48 + 24;
+    size_t aux = (size_t) 6 * kmax + 1 + 48 + 24;
     size_t want = aux + (size_t) kmax * kmax;
     const size_t cap = 110 * 1024 / sizeof(double);  // two CTAs per SM
     if (want > cap) want = cap;
