@@ -229,6 +229,10 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
 }
 
 int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, Workspace *out) {
+    // The QR panels and the core's bookkeeping live in shared memory: refuse shapes beyond it.
+    const size_t smem_limit = 227 * 1024;
+    if (sh.any_compressed_c && (qr_smem_bytes(sh.ld, sh.kmax) > smem_limit || svd_smem_bytes(sh.kmax) > smem_limit))
+        return fail(ctx, HCGB_POOL_TOO_SMALL, "tile too large: the QR panel or core bookkeeping exceeds shared memory");
     Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, ddc);
     size_t need = workspace_bytes_for(w, n);
     int rc = ensure_device(ctx, &ctx->ws, &ctx->ws_bytes, need);

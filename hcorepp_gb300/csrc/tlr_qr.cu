@@ -20,6 +20,12 @@ constexpr int QR_THREADS = 256;
 
 __host__ __device__ __forceinline__ int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
+// Width of the W = V^T X buffer: the trailing columns are updated in chunks of at most this many.
+__host__ __device__ __forceinline__ int qr_w_cols(int kmax) {
+    const int w = round_up(kmax, 8);
+    return w < 512 ? w : 512;
+}
+
 // Block-wide sum; `red` holds >= 33 doubles.  Must be called by all threads.
 __device__ double block_sum(double v, double *red) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -125,8 +131,19 @@ __device__ void build_t(const double *Ps, int ldp, int mr, int nbp, const double
 
 // X (mr x nt, ld ldx) <- (I - V op(T) V^T) X with V = Ps (explicit, NB columns, ldp), T = Ts.
 // trans_t: op(T) = T^T (applying Q^T, the QR trailing update); else op(T) = T (applying Q).
+__device__ void apply_block_reflector_cols(const double *Ps, int ldp, const double *Ts, bool trans_t, double *X,
+                                           int ldx, int mr, int nt, double *Ws, int ldw);
+
+// Columns are processed in chunks of at most ldw (the width of the W buffer in shared memory).
 __device__ void apply_block_reflector(const double *Ps, int ldp, const double *Ts, bool trans_t, double *X, int ldx,
                                       int mr, int nt, double *Ws, int ldw) {
+    for (int c0 = 0; c0 < nt; c0 += ldw)
+        apply_block_reflector_cols(Ps, ldp, Ts, trans_t, X + (size_t) c0 * ldx, ldx, mr,
+                                   nt - c0 < ldw ? nt - c0 : ldw, Ws, ldw);
+}
+
+__device__ void apply_block_reflector_cols(const double *Ps, int ldp, const double *Ts, bool trans_t, double *X,
+                                           int ldx, int mr, int nt, double *Ws, int ldw) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int lr = lane >> 2, lc = lane & 3;
     if (nt <= 0 || mr <= 0) return;
@@ -211,7 +228,7 @@ struct QrShared {
 __device__ QrShared carve(double *sm, int ld, int kmax) {
     QrShared s;
     s.ldp = round_up(ld, 8);
-    s.ldw = round_up(kmax, 8);
+    s.ldw = qr_w_cols(kmax);
     s.Ps = sm;
     s.Ws = s.Ps + (size_t) NB * s.ldp;
     s.Ts = s.Ws + (size_t) NB * s.ldw;
@@ -305,7 +322,7 @@ __global__ void __launch_bounds__(QR_THREADS) apply_q_kernel(const DevUpdate *up
 }  // namespace
 
 size_t qr_smem_bytes(int ld, int kmax) {
-    const int ldp = round_up(ld, 8), ldw = round_up(kmax, 8);
+    const int ldp = round_up(ld, 8), ldw = qr_w_cols(kmax);
     return sizeof(double) * ((size_t) NB * ldp + (size_t) NB * ldw + 2 * NB * NB + 64 + NB);
 }
 

@@ -641,7 +641,8 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
 size_t svd_smem_bytes(int kmax) {
     size_t aux = (size_t) 6 * kmax + 1 + 48 + 24;
     size_t want = aux + (size_t) kmax * kmax;
-    const size_t cap = 110 * 1024 / sizeof(double);  // two CTAs per SM
+    size_t cap = 110 * 1024 / sizeof(double);  // two CTAs per SM
+    if (cap < aux) cap = aux;                   // the aux arrays always fit (checked against the device limit)
     if (want > cap) want = cap;
     return want * sizeof(double);
 }
