@@ -90,6 +90,8 @@ def lib():
         L.hcgb_fp64_peak.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.hcgb_set_concurrency.argtypes = [vp, ip]
         L.hcgb_set_k_order.argtypes = [vp, ip]
+        L.hcgb_set_tensor_products.argtypes = [vp, ip]
+        L.hcgb_set_tensor_products.restype = C.c_int
         L.hcgb_potrf.argtypes = [vp, ip, ip, vp, ip, C.POINTER(C.c_int)]
         L.hcgb_trsm.argtypes = [vp, ip, ip, ip, ip, ip, ip, C.c_double, vp, ip, vp, ip]
         L.hcgb_syrk.argtypes = [vp, ip, ip, ip, ip, C.c_double, vp, ip, C.c_double, vp, ip]
@@ -151,6 +153,10 @@ class Context:
 
     def set_k_order(self, policy: int):
         self.check(lib().hcgb_set_k_order(self._h, int(policy)))
+
+    def set_tensor_products(self, enable: bool):
+        """Large factor products on the 16-bit tensor cores (FP64-accurate splitting) or on DMMA."""
+        self.check(lib().hcgb_set_tensor_products(self._h, int(bool(enable))))
 
     def set_concurrency(self, groups: int):
         self.check(lib().hcgb_set_concurrency(self._h, int(groups)))

@@ -19,7 +19,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhcgb.so")
 
-CU_SOURCES = ["hcgb_abi.cu", "tlr_plan.cu", "tlr_qr.cu", "tlr_svd.cu", "probe.cu", "noalloc.cu", "chol.cu"]
+CU_SOURCES = ["hcgb_abi.cu", "tlr_plan.cu", "tlr_qr.cu", "tlr_svd.cu", "probe.cu", "noalloc.cu", "chol.cu",
+              "oz_gemm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -31,6 +31,7 @@ struct hcgb_context {
     // independent C-tile groups of hcgb_tlr_gemm, one stream each
     int groups = 8;
     int k_order = 0;  // 0: ascending k per C tile (reference order); 1: estimated cost, largest first
+    int oz = 1;       // large factor products on the 16-bit tensor cores (FP64-accurate splitting)
     std::vector<cudaStream_t> group_streams;
     std::vector<cudaEvent_t> group_events;  // [0] fork, [1..] joins
 };
@@ -154,8 +155,9 @@ size_t workspace_bytes_for(const Workspace &w, int n) {
     return sizeof(double) * w.slot_doubles * (size_t) n + sizeof(int) * (META_INTS + 1) * (size_t) n + 256;
 }
 
-Params to_params(const hcgb_params *p) {
+Params to_params(const hcgb_params *p, const hcgb_context *ctx) {
     Params q;
+    q.oz = ctx ? ctx->oz : 1;
     q.accuracy = p ? p->accuracy : 1e-9;
     q.truncated = p ? p->truncated_svd : 0;
     q.fixed_rank = p ? p->fixed_rank : 0;
@@ -345,7 +347,7 @@ int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const h
     DevUpdate *dups;
     GemmJob *djobs;
     if ((rc = upload_updates(ctx, dv, &dups, &djobs))) return rc;
-    launch_pipeline(ctx, ctx->stream, dups, djobs, n, alpha, beta, ws, sh, to_params(params), info_dev);
+    launch_pipeline(ctx, ctx->stream, dups, djobs, n, alpha, beta, ws, sh, to_params(params, ctx), info_dev);
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
 }
@@ -456,7 +458,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
     auto *dups = static_cast<DevUpdate *>(ctx->desc);
     auto *djobs = reinterpret_cast<GemmJob *>(static_cast<char *>(ctx->desc) + ub_al);
-    const Params p = to_params(params);
+    const Params p = to_params(params, ctx);
     // Streams and fork/join events for the groups.
     while ((int) ctx->group_streams.size() < G) {
         cudaStream_t s;
@@ -585,6 +587,13 @@ int read_rank(hcgb_context *ctx, const hcgb_tile &t, int *r) {
 }
 
 }  // namespace
+
+extern "C" int hcgb_set_tensor_products(hcgb_context *ctx, int enable) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (enable != 0 && enable != 1) return fail(ctx, HCGB_BAD_ARG, "hcgb_set_tensor_products: 0 or 1");
+    ctx->oz = enable;
+    return HCGB_OK;
+}
 
 extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *a, int op_a, const hcgb_tile *b,
                               int op_b, double beta, hcgb_tile *c, const hcgb_params *params, int *new_rank,
@@ -872,7 +881,7 @@ extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *gr
         cudaFree(dpanel);
         return rc;
     };
-    const Params p = to_params(params);
+    const Params p = to_params(params, ctx);
     const int chunk = 1024;  // updates per pipeline launch (bounds the workspace)
     int uid = 0;
     auto tile = [&](int i, int j) -> const hcgb_tile & { return grid[i + (size_t) j * nt]; };

@@ -51,7 +51,13 @@ struct GemmJob {
     int lda, ldb, ldc;
     int opA, opB;
     double alpha, beta;
+    int oz;  // 1: computed on the 16-bit tensor cores by error-free splitting (oz_gemm.cu)
 };
+
+// Products worth the split (enough k for the FP64 flushes to amortise, enough outputs for a tile).
+__host__ __device__ inline bool oz_shape(int M, int N, int K) {
+    return K >= 48 && M >= 16 && N >= 8 && (long long) M * N >= 2048;
+}
 
 struct DevTile {
     double *data;  // U (rows x rank, ld rows), or the dense tile
@@ -115,6 +121,7 @@ struct Params {
     int fixed_rank;
     int side_mode;   // 0: always the reference's [Cu | alpha Au]; 1: pick the smaller stack
     int mode;        // 0: plain FP64; 1: mixed (single-precision Jacobi preconditioning of the core)
+    int oz;          // 1: large factor products on the 16-bit tensor cores (FP64-accurate splitting)
 };
 
 // ---- launchers (stream-ordered, asynchronous) ----
@@ -124,6 +131,7 @@ void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Worksp
 // ws.order <- updates sorted by decreasing stack width k (ties by index); needs ws.order != nullptr.
 void launch_order(int n, Workspace ws, cudaStream_t st);
 void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st);
+void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st);
 void launch_qr(Workspace ws, int n, cudaStream_t st);
 void launch_core_svd(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st);
 void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st);

@@ -125,6 +125,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     prm.fixed_rank = params ? params->fixed_rank : 0;
     prm.side_mode = 1;
     prm.mode = params ? params->mode : 0;
+    prm.oz = 1;
 
     // GEMM grid bounds from the tile kinds and capacities (ranks are read on the device).
     int pm[3] = {0, 0, 0}, pn[3] = {0, 0, 0};

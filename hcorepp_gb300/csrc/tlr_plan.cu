@@ -23,15 +23,29 @@ __device__ __forceinline__ GemmJob make_job(const double *A, int lda, int opA, c
     j.opB = opB;
     j.alpha = alpha;
     j.beta = beta;
+    j.oz = 0;
     return j;
 }
 
 // One thread per update: read ranks on the device, validate, choose the stacking side and
 // emit up to three dependent GEMM jobs (phase 1, 2, 3).
+__device__ void plan_update(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p,
+                            GemmJob *jobs, int s);
+
 __global__ void plan_kernel(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p,
                             GemmJob *jobs) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
+    plan_update(ups, n, alpha, beta, ws, p, jobs, s);
+    // Large products go to the tensor-core path.
+    for (int ph = 0; ph < 3; ph++) {
+        GemmJob &j = jobs[(size_t) ph * n + s];
+        j.oz = (p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K)) ? 1 : 0;
+    }
+}
+
+__device__ void plan_update(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p,
+                            GemmJob *jobs, int s) {
     const DevUpdate u = ups[s];
     int *meta = ws.meta + (size_t) s * META_INTS;
     GemmJob none;
@@ -198,7 +212,7 @@ constexpr int GT = 64, GK = 16, AS_LD = GK + 4, BS_LD = GT + 4;
 
 __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
     const GemmJob jb = jobs[blockIdx.y];
-    if (jb.M <= 0 || jb.N <= 0) return;
+    if (jb.M <= 0 || jb.N <= 0 || jb.oz) return;
     const int ntm = (jb.M + GT - 1) / GT, ntn = (jb.N + GT - 1) / GT;
     if ((int) blockIdx.x >= ntm * ntn) return;
     const int m0 = (blockIdx.x % ntm) * GT, n0 = (blockIdx.x / ntm) * GT;
@@ -382,6 +396,7 @@ void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cuda
     const int tiles = ((max_m + GT - 1) / GT) * ((max_n + GT - 1) / GT);
     dim3 grid(tiles, njobs);
     gemm_jobs_kernel<<<grid, 128, 0, st>>>(jobs);
+    launch_oz_gemm_jobs(jobs, njobs, max_m, max_n, st);
 }
 
 void launch_finalize(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st) {

@@ -151,6 +151,13 @@ int hcgb_set_concurrency(hcgb_context *ctx, int groups);
  * within the accuracy bound).  The expensive updates of all tiles then share a few k-waves. */
 int hcgb_set_k_order(hcgb_context *ctx, int policy);
 
+/* Factor products of k >= 48 with at least 2048 outputs run on the 16-bit tensor cores by
+ * error-free splitting (each FP64 operand cut into eight 7-bit integer digit planes relative to its
+ * row / column maximum, plane products accumulated exactly in FP32 and combined in FP64; result
+ * error below 2^-44 max|A_i| max|B_j|, the order of an FP64 product's worst-case bound).
+ * enable = 0 keeps every product on the FP64 DMMA path.  Default 1.  Schedule-independent. */
+int hcgb_set_tensor_products(hcgb_context *ctx, int enable);
+
 /* Single tile update, the drop-in for HCore<T>::Gemm (src/api/HCore.cpp:23-344).  op_a/op_b
  * accept HCGB_NOTRANS and HCGB_TRANS.  Synchronous: on return *c's rank on the device has been
  * updated; *new_rank (if not NULL) receives it on the host, like CompressedTile::Gemm updating

@@ -304,3 +304,34 @@ def test_tile_packer_gemm_through_packed_tiles(T):
     assert outs[0][0] == outs[1][0]
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
     np.testing.assert_array_equal(outs[0][2], outs[1][2])
+
+
+@pytest.mark.parametrize("scaled", [False, True])
+def test_tensor_core_products_fp64_accurate(T, scaled):
+    """Dense products on the 16-bit tensor cores (error-free splitting) match an extended-precision
+    product to FP64 worst-case accuracy, with rows / columns spanning 2^+-40, zero rows and columns
+    and mixed signs; the FP64 DMMA path gives the same to rounding."""
+    rng = np.random.default_rng(12)
+    m, n, k = 96, 40, 200
+    a = rng.standard_normal((m, k))
+    b = rng.standard_normal((k, n))
+    c = rng.standard_normal((m, n))
+    if scaled:
+        a *= np.exp2(rng.integers(-40, 40, size=(m, 1)))
+        b *= np.exp2(rng.integers(-40, 40, size=(1, n)))
+        a[5, :] = 0.0
+        b[:, 7] = 0.0
+        a[:, 3] *= 1e-12
+    exact = (a.astype(np.longdouble) @ b.astype(np.longdouble)) * np.longdouble(1.5) + np.longdouble(0.25) * c
+    bound = np.abs(a).max(axis=1, keepdims=True) * np.abs(b).max(axis=0, keepdims=True) * 1.5
+    ctx = T.run_context()
+    out = {}
+    for oz in (True, False):
+        ctx.set_tensor_products(oz)
+        gc = T.DenseTile(m, n, c)
+        T.HCore.Gemm(1.5, T.DenseTile(m, k, a), 0, T.DenseTile(k, n, b), 0, 0.25, gc)
+        out[oz] = gc.to_dense()
+    ctx.set_tensor_products(True)
+    for oz, got in out.items():
+        err = np.abs(got.astype(np.longdouble) - exact) / (bound + np.abs(0.25 * c))
+        assert float(err.max()) < 2e-14, (oz, float(err.max()))
