@@ -220,7 +220,18 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     }
     mark(HCGB_STAGE_APPLY_Q);
     if (sh.any_compressed_c) {
-        launch_apply_q(dups, n, ws, st);
+        if (p.oz && ws.off_w) {
+            // Full WY form: the Grams, Y = V^T X and X -= V W are products (tensor-core eligible),
+            // only the small triangular solve stays on the FP64 pipe.
+            const int lk = ws.kmax, lx = ws.ld;
+            launch_plan_wy(dups, n, ws, p, djobs, st);
+            launch_gemm_jobs(djobs, 2 * n, lk, lk, st);
+            launch_gemm_jobs(djobs + 2 * (size_t) n, 2 * n, lk, lk, st);
+            launch_wy_solve(n, ws, st);
+            launch_gemm_jobs(djobs + 4 * (size_t) n, 2 * n, lx, lk, st);
+        } else {
+            launch_apply_q(dups, n, ws, st);
+        }
         cnt[HCGB_STAGE_APPLY_Q]++;
     }
     mark(HCGB_STAGE_FINALIZE);
@@ -235,7 +246,7 @@ int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, 
     const size_t smem_limit = 227 * 1024;
     if (sh.any_compressed_c && (qr_smem_bytes(sh.ld, sh.kmax) > smem_limit || svd_smem_bytes(sh.kmax) > smem_limit))
         return fail(ctx, HCGB_POOL_TOO_SMALL, "tile too large: the QR panel or core bookkeeping exceeds shared memory");
-    Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, ddc);
+    Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, ddc, ctx->oz != 0);
     size_t need = workspace_bytes_for(w, n);
     int rc = ensure_device(ctx, &ctx->ws, &ctx->ws_bytes, need);
     if (rc) return rc;
@@ -249,7 +260,7 @@ int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, 
 // Upload `n` device update descriptors and make room for 3n jobs; returns device pointers.
 int upload_updates(hcgb_context *ctx, const std::vector<DevUpdate> &dv, DevUpdate **dups, GemmJob **djobs) {
     const size_t n = dv.size();
-    const size_t ub = sizeof(DevUpdate) * n, jb = sizeof(GemmJob) * 3 * n;
+    const size_t ub = sizeof(DevUpdate) * n, jb = sizeof(GemmJob) * JOBS_PER_UPDATE * n;
     const size_t ub_al = (ub + 255) / 256 * 256;
     int rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb);
     if (rc) return rc;
@@ -450,7 +461,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     int rc = prepare_workspace(ctx, sh, n, false, &ws);
     if (rc) return rc;
     const size_t ub = sizeof(DevUpdate) * dv.size(), ub_al = (ub + 255) / 256 * 256;
-    const size_t jb = sizeof(GemmJob) * 3 * (size_t) n;
+    const size_t jb = sizeof(GemmJob) * JOBS_PER_UPDATE * (size_t) n;
     if ((rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb))) return rc;
     if ((rc = ensure_stage(ctx, ub))) return rc;
     std::memcpy(ctx->stage, dv.data(), ub);
@@ -486,7 +497,8 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
             shw.ld = sh.ld;
             shw.kmax = sh.kmax;
             shw.rmax = sh.rmax;
-            launch_pipeline(ctx, st, dups + off, djobs + 3 * (size_t) first[g], ng, alpha, beta, wg, shw, p, info_dev);
+            launch_pipeline(ctx, st, dups + off, djobs + JOBS_PER_UPDATE * (size_t) first[g], ng, alpha, beta, wg,
+                            shw, p, info_dev);
         }
         if (!single) {
             HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[g + 1], st));

@@ -51,8 +51,23 @@ struct GemmJob {
     int lda, ldb, ldc;
     int opA, opB;
     double alpha, beta;
-    int oz;  // 1: computed on the 16-bit tensor cores by error-free splitting (oz_gemm.cu)
+    int oz;          // 1: computed on the 16-bit tensor cores by error-free splitting (oz_gemm.cu)
+    int triA, triB;  // 1: the stored operand is read as unit lower trapezoidal (Householder vectors)
 };
+
+constexpr int JOBS_PER_UPDATE = 6;  // job slots per update: 3 factor-product phases, 6 for the WY application
+
+// Element (i, k) of op(A) with the job's op / unit-lower view (both GEMM kernels).
+__device__ __forceinline__ double job_a(const GemmJob &jb, int i, int k) {
+    const int r = jb.opA == 0 ? i : k, c = jb.opA == 0 ? k : i;
+    if (jb.triA && r <= c) return r == c ? 1.0 : 0.0;
+    return jb.A[r + (size_t) c * jb.lda];
+}
+__device__ __forceinline__ double job_b(const GemmJob &jb, int k, int j) {
+    const int r = jb.opB == 0 ? k : j, c = jb.opB == 0 ? j : k;
+    if (jb.triB && r <= c) return r == c ? 1.0 : 0.0;
+    return jb.B[r + (size_t) c * jb.ldb];
+}
 
 // Products worth the split (enough k for the FP64 flushes to amortise, enough outputs for a tile).
 __host__ __device__ inline bool oz_shape(int M, int N, int K) {
@@ -104,6 +119,7 @@ struct Workspace {
     int rmax;             // max rank of an A/B factor
     size_t off_ustack, off_vstack, off_tmp1, off_tmp2, off_tauu, off_tauv, off_tu, off_tv;
     size_t off_m, off_mcopy, off_xv, off_sigma, off_mixed;
+    size_t off_w;  // WY application: W_U, W_V (kmax x kmax each), present when built with wy
 
     __host__ __device__ double *slot(int s) const { return base + slot_doubles * (size_t) s; }
     // Update processed by CTA `b` of the QR / core / Q-application launches: largest first, so the
@@ -113,7 +129,7 @@ struct Workspace {
 
 // Layout of one workspace slot for stacks of up to `ld` rows and `kmax` columns; factor ranks
 // up to `rmax`.  ddc_scratch reserves an ld x ld product for the DDC combination.
-Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch);
+Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch, bool wy = false);
 
 struct Params {
     double accuracy;
@@ -132,6 +148,10 @@ void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Worksp
 void launch_order(int n, Workspace ws, cudaStream_t st);
 void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st);
 void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st);
+// Q application in full WY form (Q = I - V T V^T, T^-1 = striu(V^T V) + diag(1/tau)): jobs for
+// the Grams, Y = V^T X and X -= V W, then the triangular solve T^-1 W = Y.
+void launch_plan_wy(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob *jobs, cudaStream_t st);
+void launch_wy_solve(int n, Workspace ws, cudaStream_t st);
 void launch_qr(Workspace ws, int n, cudaStream_t st);
 void launch_core_svd(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st);
 void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st);

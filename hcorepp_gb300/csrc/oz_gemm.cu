@@ -73,12 +73,8 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const unsigned (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ double load_a(const GemmJob &jb, int i, int k) {
-    return jb.opA == 0 ? jb.A[i + (size_t) k * jb.lda] : jb.A[k + (size_t) i * jb.lda];
-}
-__device__ __forceinline__ double load_b(const GemmJob &jb, int k, int j) {
-    return jb.opB == 0 ? jb.B[k + (size_t) j * jb.ldb] : jb.B[j + (size_t) k * jb.ldb];
-}
+__device__ __forceinline__ double load_a(const GemmJob &jb, int i, int k) { return job_a(jb, i, k); }
+__device__ __forceinline__ double load_b(const GemmJob &jb, int k, int j) { return job_b(jb, k, j); }
 
 // Grid: x = output tile within the job, y = job (as the FP64 kernel); jobs without the oz mark are
 // left to the FP64 kernel.

@@ -24,6 +24,7 @@ __device__ __forceinline__ GemmJob make_job(const double *A, int lda, int opA, c
     j.alpha = alpha;
     j.beta = beta;
     j.oz = 0;
+    j.triA = j.triB = 0;
     return j;
 }
 
@@ -244,10 +245,7 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
                 i = e / GK;
             }
             const int gi = m0 + i, gk = k0 + kk;
-            double v = 0.0;
-            if (gi < jb.M && gk < jb.K)
-                v = jb.opA == 0 ? jb.A[gi + (size_t) gk * jb.lda] : jb.A[gk + (size_t) gi * jb.lda];
-            As[i][kk] = v;
+            As[i][kk] = (gi < jb.M && gk < jb.K) ? job_a(jb, gi, gk) : 0.0;
         }
         for (int e = threadIdx.x; e < GT * GK; e += blockDim.x) {
             int j, kk;
@@ -259,10 +257,7 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
                 kk = e / GT;
             }
             const int gj = n0 + j, gk = k0 + kk;
-            double v = 0.0;
-            if (gj < jb.N && gk < jb.K)
-                v = jb.opB == 0 ? jb.B[gk + (size_t) gj * jb.ldb] : jb.B[gj + (size_t) gk * jb.ldb];
-            Bs[kk][j] = v;
+            Bs[kk][j] = (gj < jb.N && gk < jb.K) ? job_b(jb, gk, gj) : 0.0;
         }
         __syncthreads();
         // The FP64 pipe is the limit: no MMA is issued for 8x8 blocks or k-steps that lie wholly
@@ -372,7 +367,83 @@ __global__ void __launch_bounds__(256) transpose_kernel(const double *src, int l
     transpose_scaled(src, lds, rows, cols, dst, ldd, 1.0, tile);
 }
 
+// One thread per update: the six jobs of the WY application of both Q factors (after the core).
+//   0/1: G = V^T V of the U / V stack (unit lower Householder vectors), into off_m / off_mcopy
+//   2/3: Y = V^T X, X = the new U (C's U buffer) / XV, into W (off_w); X is zero below row kk
+//   4/5: X <- X - V W
+__global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob *jobs) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    GemmJob none;
+    none.M = none.N = none.K = 0;
+    none.oz = none.triA = none.triB = 0;
+    for (int q = 0; q < 6; q++) jobs[(size_t) q * n + s] = none;
+    const int *meta = ws.meta + (size_t) s * META_INTS;
+    const int st = meta[META_STATUS];
+    if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;
+    const int k = meta[META_K], m = meta[META_M], nn = meta[META_N], r = meta[META_NEWRANK];
+    double *base = ws.slot(s);
+    const int ld = ws.ld, lk = ws.kmax;
+    for (int side = 0; side < 2; side++) {
+        const int rows = side ? nn : m, kk = rows < k ? rows : k;
+        double *Vst = base + (side ? ws.off_vstack : ws.off_ustack);
+        double *G = base + (side ? ws.off_mcopy : ws.off_m);
+        double *W = base + ws.off_w + (size_t) side * lk * lk;
+        double *X = side ? base + ws.off_xv : ups[s].c.data;
+        const int ldx = side ? ld : ups[s].c.rows;
+        GemmJob g = make_job(Vst, ld, 1, Vst, ld, 0, G, lk, kk, kk, rows, 1.0, 0.0);
+        g.triA = g.triB = 1;
+        GemmJob y = make_job(Vst, ld, 1, X, ldx, 0, W, lk, kk, r, kk, 1.0, 0.0);
+        y.triA = 1;
+        GemmJob u = make_job(Vst, ld, 0, W, lk, 0, X, ldx, rows, r, kk, -1.0, 1.0);
+        u.triA = 1;
+        GemmJob *out[3] = {&g, &y, &u};
+        for (int q = 0; q < 3; q++) {
+            GemmJob &j = *out[q];
+            j.oz = (p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K)) ? 1 : 0;
+            jobs[(size_t) (2 * q + side) * n + s] = j;
+        }
+    }
+}
+
+// Two CTAs per update (U side, V side): solve T^-1 W = Y in place, T^-1 = striu(G) + diag(1/tau),
+// by back substitution; one warp per column of W, lanes split the inner products (G is symmetric,
+// so row i of its upper part is read as column i).  tau_i = 0 (an identity reflector) gives W_i = 0.
+__global__ void __launch_bounds__(256) wy_solve_kernel(Workspace ws) {
+    const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
+    const int *meta = ws.meta + (size_t) slot * META_INTS;
+    const int st = meta[META_STATUS];
+    if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;
+    const int k = meta[META_K], rows = side ? meta[META_N] : meta[META_M], r = meta[META_NEWRANK];
+    const int kk = rows < k ? rows : k;
+    double *base = ws.slot(slot);
+    const double *G = base + (side ? ws.off_mcopy : ws.off_m);
+    const double *tau = base + (side ? ws.off_tauv : ws.off_tauu);
+    double *W = base + ws.off_w + (size_t) side * ws.kmax * ws.kmax;
+    const int lk = ws.kmax;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int c = warp; c < r; c += nw) {
+        double *w = W + (size_t) c * lk;
+        for (int i = kk - 1; i >= 0; i--) {
+            const double *gi = G + (size_t) i * lk;
+            double part = 0.0;
+            for (int j = i + 1 + lane; j < kk; j += 32) part = fma(gi[j], w[j], part);
+            part = warp_sum(part);
+            if (lane == 0) w[i] = tau[i] * (w[i] - part);
+            __syncwarp();
+        }
+    }
+}
+
 }  // namespace
+
+void launch_plan_wy(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob *jobs, cudaStream_t st) {
+    plan_wy_kernel<<<(n + 127) / 128, 128, 0, st>>>(ups, n, ws, p, jobs);
+}
+
+void launch_wy_solve(int n, Workspace ws, cudaStream_t st) {
+    wy_solve_kernel<<<2 * n, 256, 0, st>>>(ws);
+}
 
 void launch_transpose(const double *src, int lds, int rows, int cols, double *dst, int ldd, cudaStream_t st) {
     transpose_kernel<<<1, 256, 0, st>>>(src, lds, rows, cols, dst, ldd);
@@ -407,7 +478,7 @@ void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t
     ddc_finalize_kernel<<<n, 256, 0, st>>>(ups, ws);
 }
 
-Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch) {
+Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch, bool wy) {
     Workspace w{};
     w.ld = ld;
     w.kmax = kmax;
@@ -428,6 +499,8 @@ Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch) {
     w.off_xv = off;     off += round((size_t) ld * kmax);
     w.off_sigma = off;  off += round(kmax);
     w.off_mixed = off;  off += round(((size_t) kmax * (size_t) (kmax + ld) + 1) / 2);  // float X32 + J32
+    w.off_w = wy ? off : 0;  // 0: absent (no region starts at 0 but the U stack)
+    off += wy ? round(2 * (size_t) kmax * kmax) : 0;
     w.slot_doubles = off;
     return w;
 }

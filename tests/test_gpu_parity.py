@@ -165,10 +165,11 @@ def test_trans_operands(T):
     assert rel_fro(gc2.to_dense(), exact2) < 1e-10
 
 
-@pytest.mark.parametrize("k_order", [0, 1])
-def test_tlr_multiply_vs_oracle(T, k_order):
+@pytest.mark.parametrize("k_order,oz", [(0, True), (1, True), (0, False)])
+def test_tlr_multiply_vs_oracle(T, k_order, oz):
     """A 4x4-tile multiply (nb=128) through hcgb_tlr_gemm against the oracle's tile loop, in the
-    reference's k order and in the cost-first order (same sum, other rounding order)."""
+    reference's k order and in the cost-first order (same sum, other rounding order), with the
+    large products and the WY Q application on the tensor cores (oz) and all on the FP64 pipe."""
     import torch
     from hcorepp_gb300 import _lib as L
     from hcorepp_gb300.problems import KernelMatrix
@@ -199,9 +200,14 @@ def test_tlr_multiply_vs_oracle(T, k_order):
     info = T.info_buffer(nt * nt * nt)
     ctx = T.run_context()
     ctx.set_k_order(k_order)
-    T.tlr_gemm(1.0, mats["A"], mats["B"], 1.0, mats["C"], T.CompressionParameters(acc, truncated_svd=True), info)
-    torch.cuda.synchronize()
-    ctx.set_k_order(0)
+    ctx.set_tensor_products(oz)
+    try:
+        T.tlr_gemm(1.0, mats["A"], mats["B"], 1.0, mats["C"], T.CompressionParameters(acc, truncated_svd=True),
+                   info)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_k_order(0)
+        ctx.set_tensor_products(True)
     info = info.cpu().numpy()
     assert int(info[:, 0].max()) == 0, info
     O.tile_matrix_multiply(otiles["A"], otiles["B"], otiles["C"], 1.0, 1.0, params)
