@@ -182,7 +182,8 @@ std::vector<cudaEvent_t> take_events(hcgb_context *ctx, int count) {
 }
 
 // Launch the full pipeline for n updates whose descriptors are already on the device.
-void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, GemmJob *djobs, int n, double alpha,
+void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, GemmJob *djobs, int *sched, int n,
+                     double alpha,
                      double beta, const Workspace &ws, const BatchShape &sh, const Params &p,
                      hcgb_update_info *info) {
     std::vector<cudaEvent_t> ev;
@@ -202,7 +203,7 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     mark(HCGB_STAGE_GEMM);
     for (int ph = 0; ph < 3; ph++)
         if (sh.p_m[ph] > 0 && sh.p_n[ph] > 0) {
-            launch_gemm_jobs(djobs + (size_t) ph * n, n, sh.p_m[ph], sh.p_n[ph], st);
+            launch_gemm_jobs(djobs + (size_t) ph * n, n, sched, st);
             cnt[HCGB_STAGE_GEMM]++;
         }
     mark(HCGB_STAGE_QR);
@@ -223,12 +224,10 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
         if (p.oz && ws.off_w) {
             // Full WY form: the Grams, Y = V^T X and X -= V W are products (tensor-core eligible),
             // only the small triangular solve stays on the FP64 pipe.
-            const int lk = ws.kmax, lx = ws.ld;
             launch_plan_wy(dups, n, ws, p, djobs, st);
-            launch_gemm_jobs(djobs, 2 * n, lk, lk, st);
-            launch_gemm_jobs(djobs + 2 * (size_t) n, 2 * n, lk, lk, st);
+            launch_gemm_jobs(djobs, 4 * n, sched, st);  // Grams and Y = V^T X (independent)
             launch_wy_solve(n, ws, st);
-            launch_gemm_jobs(djobs + 4 * (size_t) n, 2 * n, lx, lk, st);
+            launch_gemm_jobs(djobs + 4 * (size_t) n, 2 * n, sched, st);
         } else {
             launch_apply_q(dups, n, ws, st);
         }
@@ -258,11 +257,13 @@ int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, 
 }
 
 // Upload `n` device update descriptors and make room for 3n jobs; returns device pointers.
-int upload_updates(hcgb_context *ctx, const std::vector<DevUpdate> &dv, DevUpdate **dups, GemmJob **djobs) {
+int upload_updates(hcgb_context *ctx, const std::vector<DevUpdate> &dv, DevUpdate **dups, GemmJob **djobs,
+                   int **sched) {
     const size_t n = dv.size();
     const size_t ub = sizeof(DevUpdate) * n, jb = sizeof(GemmJob) * JOBS_PER_UPDATE * n;
-    const size_t ub_al = (ub + 255) / 256 * 256;
-    int rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb);
+    const size_t ub_al = (ub + 255) / 256 * 256, jb_al = (jb + 255) / 256 * 256;
+    const size_t sb = sizeof(int) * SCHED_INTS_PER_UPDATE * n;
+    int rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb_al + sb);
     if (rc) return rc;
     rc = ensure_stage(ctx, ub);
     if (rc) return rc;
@@ -271,6 +272,7 @@ int upload_updates(hcgb_context *ctx, const std::vector<DevUpdate> &dv, DevUpdat
     HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
     *dups = static_cast<DevUpdate *>(ctx->desc);
     *djobs = reinterpret_cast<GemmJob *>(static_cast<char *>(ctx->desc) + ub_al);
+    *sched = reinterpret_cast<int *>(static_cast<char *>(ctx->desc) + ub_al + jb_al);
     return HCGB_OK;
 }
 
@@ -357,8 +359,9 @@ int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const h
     if (rc) return rc;
     DevUpdate *dups;
     GemmJob *djobs;
-    if ((rc = upload_updates(ctx, dv, &dups, &djobs))) return rc;
-    launch_pipeline(ctx, ctx->stream, dups, djobs, n, alpha, beta, ws, sh, to_params(params, ctx), info_dev);
+    int *dsched;
+    if ((rc = upload_updates(ctx, dv, &dups, &djobs, &dsched))) return rc;
+    launch_pipeline(ctx, ctx->stream, dups, djobs, dsched, n, alpha, beta, ws, sh, to_params(params, ctx), info_dev);
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
 }
@@ -461,14 +464,16 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     int rc = prepare_workspace(ctx, sh, n, false, &ws);
     if (rc) return rc;
     const size_t ub = sizeof(DevUpdate) * dv.size(), ub_al = (ub + 255) / 256 * 256;
-    const size_t jb = sizeof(GemmJob) * JOBS_PER_UPDATE * (size_t) n;
-    if ((rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb))) return rc;
+    const size_t jb = sizeof(GemmJob) * JOBS_PER_UPDATE * (size_t) n, jb_al = (jb + 255) / 256 * 256;
+    const size_t sb = sizeof(int) * SCHED_INTS_PER_UPDATE * (size_t) n;
+    if ((rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb_al + sb))) return rc;
     if ((rc = ensure_stage(ctx, ub))) return rc;
     std::memcpy(ctx->stage, dv.data(), ub);
     HCGB_CUDA(ctx, cudaMemcpyAsync(ctx->desc, ctx->stage, ub, cudaMemcpyHostToDevice, ctx->stream));
     HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
     auto *dups = static_cast<DevUpdate *>(ctx->desc);
     auto *djobs = reinterpret_cast<GemmJob *>(static_cast<char *>(ctx->desc) + ub_al);
+    auto *dsched = reinterpret_cast<int *>(static_cast<char *>(ctx->desc) + ub_al + jb_al);
     const Params p = to_params(params, ctx);
     // Streams and fork/join events for the groups.
     while ((int) ctx->group_streams.size() < G) {
@@ -497,8 +502,8 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
             shw.ld = sh.ld;
             shw.kmax = sh.kmax;
             shw.rmax = sh.rmax;
-            launch_pipeline(ctx, st, dups + off, djobs + JOBS_PER_UPDATE * (size_t) first[g], ng, alpha, beta, wg,
-                            shw, p, info_dev);
+            launch_pipeline(ctx, st, dups + off, djobs + JOBS_PER_UPDATE * (size_t) first[g],
+                            dsched + SCHED_INTS_PER_UPDATE * (size_t) first[g], ng, alpha, beta, wg, shw, p, info_dev);
         }
         if (!single) {
             HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[g + 1], st));
@@ -655,7 +660,8 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
         std::vector<DevUpdate> dv{DevUpdate{to_dev(A), to_dev(B), to_dev(*c), 0}};
         DevUpdate *dups;
         GemmJob *djobs;
-        if ((rc = upload_updates(ctx, dv, &dups, &djobs))) {
+        int *dsched;
+        if ((rc = upload_updates(ctx, dv, &dups, &djobs, &dsched))) {
             cleanup();
             return rc;
         }
@@ -674,8 +680,8 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
         std::memcpy(ctx->stage, j, sizeof(j));
         HCGB_CUDA(ctx, cudaMemcpyAsync(djobs, ctx->stage, sizeof(j), cudaMemcpyHostToDevice, ctx->stream));
         HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
-        launch_gemm_jobs(djobs, 1, (int) m, (int) n, ctx->stream);
-        launch_gemm_jobs(djobs + 1, 1, (int) m, (int) n, ctx->stream);
+        launch_gemm_jobs(djobs, 1, dsched, ctx->stream);
+        launch_gemm_jobs(djobs + 1, 1, dsched, ctx->stream);
         launch_ddc_finalize(dups, 1, ws, ctx->stream);
         HCGB_CUDA(ctx, cudaGetLastError());
         fl = 2ull * m * n * kd + 2ull * m * n * (unsigned long long) rcank;
@@ -943,8 +949,9 @@ extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *gr
             if (rc) return done(rc);
             DevUpdate *dups;
             GemmJob *djobs;
-            if ((rc = upload_updates(ctx, part, &dups, &djobs))) return done(rc);
-            launch_pipeline(ctx, ctx->stream, dups, djobs, n, -1.0, 1.0, ws, sh, p, info_dev);
+            int *dsched;
+            if ((rc = upload_updates(ctx, part, &dups, &djobs, &dsched))) return done(rc);
+            launch_pipeline(ctx, ctx->stream, dups, djobs, dsched, n, -1.0, 1.0, ws, sh, p, info_dev);
             HCGB_CUDA(ctx, cudaGetLastError());
         }
     }

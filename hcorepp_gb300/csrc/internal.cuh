@@ -146,8 +146,11 @@ void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspa
 void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, cudaStream_t st);
 // ws.order <- updates sorted by decreasing stack width k (ties by index); needs ws.order != nullptr.
 void launch_order(int n, Workspace ws, cudaStream_t st);
-void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st);
-void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st);
+// Batched products: sched = device scratch of 2 * njobs + 2 ints (tile prefix sums), njobs <= 4096.
+void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t st);
+void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int sms, cudaStream_t st);
+constexpr int MAX_JOBS_PER_LAUNCH = 4096;
+constexpr int SCHED_INTS_PER_UPDATE = 10;  // >= (2 * 4n + 2) / n: one WY launch schedules 4n jobs
 // Q application in full WY form (Q = I - V T V^T, T^-1 = striu(V^T V) + diag(1/tau)): jobs for
 // the Grams, Y = V^T X and X -= V W, then the triangular solve T^-1 W = Y.
 void launch_plan_wy(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob *jobs, cudaStream_t st);

@@ -93,7 +93,8 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     const size_t meta_bytes = round_up_bytes(sizeof(int) * META_INTS);
     const size_t desc_bytes = round_up_bytes(sizeof(DevUpdate));
     const size_t job_bytes = round_up_bytes(sizeof(GemmJob) * 3);
-    if (slot_bytes + meta_bytes + desc_bytes + job_bytes > sizeof(double) * HCGB_NOALLOC_SCRATCH_DOUBLES)
+    const size_t sched_bytes = round_up_bytes(sizeof(int) * 4);
+    if (slot_bytes + meta_bytes + desc_bytes + job_bytes + sched_bytes > sizeof(double) * HCGB_NOALLOC_SCRATCH_DOUBLES)
         return HCGB_POOL_TOO_SMALL;
 
     int device = 0;
@@ -106,6 +107,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     ws.meta = reinterpret_cast<int *>(p + slot_bytes);
     auto *dup = reinterpret_cast<DevUpdate *>(p + slot_bytes + meta_bytes);
     auto *jobs = reinterpret_cast<GemmJob *>(p + slot_bytes + meta_bytes + desc_bytes);
+    auto *sched = reinterpret_cast<int *>(p + slot_bytes + meta_bytes + desc_bytes + job_bytes);
 
     auto dev_tile = [](const hcgb_tile *t) {
         DevTile d;
@@ -156,7 +158,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     launch_plan(dup, 1, alpha, beta, ws, prm, jobs, st);
     if (ck) launch_stack(dup, 1, alpha, beta, ws, st);
     for (int ph = 0; ph < 3; ph++)
-        if (pm[ph] > 0 && pn[ph] > 0) launch_gemm_jobs(jobs + ph, 1, pm[ph], pn[ph], st);
+        if (pm[ph] > 0 && pn[ph] > 0) launch_gemm_jobs(jobs + ph, 1, sched, st);
     if (ck) {
         launch_qr(ws, 1, st);
         launch_core_svd(dup, 1, ws, prm, st);

@@ -76,18 +76,10 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const unsigned (&a)[4], 
 __device__ __forceinline__ double load_a(const GemmJob &jb, int i, int k) { return job_a(jb, i, k); }
 __device__ __forceinline__ double load_b(const GemmJob &jb, int k, int j) { return job_b(jb, k, j); }
 
-// Grid: x = output tile within the job, y = job (as the FP64 kernel); jobs without the oz mark are
-// left to the FP64 kernel.
-__global__ void __launch_bounds__(OZ_THREADS) oz_gemm_jobs_kernel(const GemmJob *jobs) {
-    const GemmJob jb = jobs[blockIdx.y];
-    if (!jb.oz || jb.M <= 0 || jb.N <= 0) return;
-    const int ntm = (jb.M + OZ_TM - 1) / OZ_TM, ntn = (jb.N + OZ_TN - 1) / OZ_TN;
-    if ((int) blockIdx.x >= ntm * ntn) return;
-    const int m0 = (blockIdx.x % ntm) * OZ_TM, n0 = (blockIdx.x / ntm) * OZ_TN;
-    extern __shared__ __align__(16) unsigned char oz_smem[];
-    __half *As = reinterpret_cast<__half *>(oz_smem);  // [plane][row][k]
-    __half *Bs = As + OZ_S * OZ_TM * OZ_LDS;            // [plane][col][k]
-    __shared__ int ea[OZ_TM], eb[OZ_TN];
+// One 64 x 32 output tile of one job.
+__device__ void oz_tile(const GemmJob &jb, int tile, __half *As, __half *Bs, int *ea, int *eb) {
+    const int ntm = (jb.M + OZ_TM - 1) / OZ_TM;
+    const int m0 = (tile % ntm) * OZ_TM, n0 = (tile / ntm) * OZ_TN;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // 1. Group exponents over all of K: PA threads per row of op(A), PB per column of op(B).
@@ -218,15 +210,34 @@ __global__ void __launch_bounds__(OZ_THREADS) oz_gemm_jobs_kernel(const GemmJob 
         }
 }
 
+// Tiles of the jobs marked oz, compacted (sched: exclusive prefix of tiles per job, njobs + 1
+// entries); a grid sized to the GPU strides over them.
+__global__ void __launch_bounds__(OZ_THREADS) oz_gemm_jobs_kernel(const GemmJob *jobs, int njobs, const int *sched) {
+    extern __shared__ __align__(16) unsigned char oz_smem[];
+    __half *As = reinterpret_cast<__half *>(oz_smem);  // [plane][row][k]
+    __half *Bs = As + OZ_S * OZ_TM * OZ_LDS;            // [plane][col][k]
+    __shared__ int ea[OZ_TM], eb[OZ_TN];
+    const int total = sched[njobs];
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        int lo = 0, hi = njobs;  // sched[lo] <= w < sched[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (sched[mid] <= w) lo = mid;
+            else hi = mid;
+        }
+        const GemmJob jb = jobs[lo];
+        oz_tile(jb, w - sched[lo], As, Bs, ea, eb);
+        __syncthreads();
+    }
+}
+
 }  // namespace
 
-void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st) {
-    if (njobs <= 0 || max_m <= 0 || max_n <= 0) return;
-    const int tiles = ((max_m + OZ_TM - 1) / OZ_TM) * ((max_n + OZ_TN - 1) / OZ_TN);
+void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int sms, cudaStream_t st) {
+    if (njobs <= 0) return;
     const int smem = (int) (sizeof(__half) * OZ_S * (OZ_TM + OZ_TN) * OZ_LDS);
     cudaFuncSetAttribute(oz_gemm_jobs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    dim3 grid(tiles, njobs);
-    oz_gemm_jobs_kernel<<<grid, OZ_THREADS, smem, st>>>(jobs);
+    oz_gemm_jobs_kernel<<<sms, OZ_THREADS, smem, st>>>(jobs, njobs, sched);
 }
 
 }  // namespace hcgb

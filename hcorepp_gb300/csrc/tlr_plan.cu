@@ -211,14 +211,10 @@ __global__ void __launch_bounds__(256) stack_kernel(const DevUpdate *ups, double
 // ---------------------------------------------------------------------------------------
 constexpr int GT = 64, GK = 16, AS_LD = GK + 4, BS_LD = GT + 4;
 
-__global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
-    const GemmJob jb = jobs[blockIdx.y];
-    if (jb.M <= 0 || jb.N <= 0 || jb.oz) return;
-    const int ntm = (jb.M + GT - 1) / GT, ntn = (jb.N + GT - 1) / GT;
-    if ((int) blockIdx.x >= ntm * ntn) return;
-    const int m0 = (blockIdx.x % ntm) * GT, n0 = (blockIdx.x / ntm) * GT;
-    __shared__ double As[GT][AS_LD];
-    __shared__ double Bs[GK][BS_LD];
+// One 64 x 64 output tile of one job.
+__device__ void gemm_tile(const GemmJob &jb, int tile, double (*As)[AS_LD], double (*Bs)[BS_LD]) {
+    const int ntm = (jb.M + GT - 1) / GT;
+    const int m0 = (tile % ntm) * GT, n0 = (tile / ntm) * GT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int lr = lane >> 2, lc = lane & 3;
     // Warp w owns 8-row blocks w and w + 4 of the tile and all eight 8-column blocks, so a small
@@ -296,6 +292,73 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs) {
                     *c = v;
                 }
             }
+}
+
+// Tiles of the FP64 jobs, compacted (sched: exclusive prefix of tiles per job, njobs + 1 entries);
+// a grid sized to the GPU strides over them, so empty or small jobs cost no CTA launches.
+__global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs, int njobs, const int *sched) {
+    __shared__ double As[GT][AS_LD];
+    __shared__ double Bs[GK][BS_LD];
+    const int total = sched[njobs];
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        int lo = 0, hi = njobs;  // sched[lo] <= w < sched[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (sched[mid] <= w) lo = mid;
+            else hi = mid;
+        }
+        const GemmJob jb = jobs[lo];
+        gemm_tile(jb, w - sched[lo], As, Bs);
+        __syncthreads();
+    }
+}
+
+// Tile counts of every job for the two GEMM kernels and their exclusive prefix sums:
+// sched[0 .. njobs] (FP64 DMMA, 64 x 64 tiles) and sched[njobs + 1 .. 2 njobs + 1] (tensor-core
+// path, 64 x 32 tiles).  One CTA; njobs up to 4 * 1024.
+__global__ void __launch_bounds__(1024) schedule_kernel(const GemmJob *jobs, int njobs, int *sched) {
+    __shared__ int part[2][1024];
+    constexpr int PER = 4;
+    int cd[PER], co[PER], sd = 0, so = 0;
+    for (int q = 0; q < PER; q++) {
+        const int j = threadIdx.x * PER + q;
+        cd[q] = co[q] = 0;
+        if (j < njobs) {
+            const GemmJob &jb = jobs[j];
+            if (jb.M > 0 && jb.N > 0 && jb.K >= 0) {
+                if (jb.oz) co[q] = ((jb.M + 63) / 64) * ((jb.N + 31) / 32);
+                else cd[q] = ((jb.M + GT - 1) / GT) * ((jb.N + GT - 1) / GT);
+            }
+        }
+        sd += cd[q];
+        so += co[q];
+    }
+    part[0][threadIdx.x] = sd;
+    part[1][threadIdx.x] = so;
+    __syncthreads();
+    // inclusive scan of the per-thread sums (Hillis-Steele over 1024 entries)
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int a = threadIdx.x >= off ? part[0][threadIdx.x - off] : 0;
+        const int b = threadIdx.x >= off ? part[1][threadIdx.x - off] : 0;
+        __syncthreads();
+        part[0][threadIdx.x] += a;
+        part[1][threadIdx.x] += b;
+        __syncthreads();
+    }
+    int rd = part[0][threadIdx.x] - sd, ro = part[1][threadIdx.x] - so;  // exclusive starts
+    for (int q = 0; q < PER; q++) {
+        const int j = threadIdx.x * PER + q;
+        if (j < njobs) {
+            sched[j] = rd;
+            sched[njobs + 1 + j] = ro;
+        }
+        rd += cd[q];
+        ro += co[q];
+    }
+    if (threadIdx.x == 1023) {
+        sched[njobs] = part[0][1023];
+        sched[2 * njobs + 1] = part[1][1023];
+    }
 }
 
 // One CTA per update: V (r x n, ld r) = XV^T into the tile buffer, publish rank and record.
@@ -462,12 +525,23 @@ void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Worksp
     stack_kernel<<<n, 256, 0, st>>>(ups, alpha, beta, ws);
 }
 
-void launch_gemm_jobs(const GemmJob *jobs, int njobs, int max_m, int max_n, cudaStream_t st) {
-    if (njobs <= 0 || max_m <= 0 || max_n <= 0) return;
-    const int tiles = ((max_m + GT - 1) / GT) * ((max_n + GT - 1) / GT);
-    dim3 grid(tiles, njobs);
-    gemm_jobs_kernel<<<grid, 128, 0, st>>>(jobs);
-    launch_oz_gemm_jobs(jobs, njobs, max_m, max_n, st);
+static int device_sms() {
+    static int sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152;
+    if (!sms[dev]) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    return sms[dev] > 0 ? sms[dev] : 152;
+}
+
+void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t st) {
+    const int sms = device_sms();
+    for (int off = 0; off < njobs; off += MAX_JOBS_PER_LAUNCH) {
+        const int nj = njobs - off < MAX_JOBS_PER_LAUNCH ? njobs - off : MAX_JOBS_PER_LAUNCH;
+        schedule_kernel<<<1, 1024, 0, st>>>(jobs + off, nj, sched);
+        gemm_jobs_kernel<<<4 * sms, 128, 0, st>>>(jobs + off, nj, sched);
+        launch_oz_gemm_jobs(jobs + off, nj, sched + nj + 1, sms, st);
+    }
 }
 
 void launch_finalize(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st) {
