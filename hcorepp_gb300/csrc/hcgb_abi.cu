@@ -222,15 +222,15 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     mark(HCGB_STAGE_APPLY_Q);
     if (sh.any_compressed_c) {
         if (p.oz && ws.off_w) {
-            // Full WY form: the Grams, Y = V^T X and X -= V W are products (tensor-core eligible),
-            // only the small triangular solve stays on the FP64 pipe.
+            // Sides with >= WY_MIN_REFLECTORS reflectors in full WY form: the Grams, Y = V^T X and
+            // X -= V W are products (tensor-core eligible), only the small triangular solve stays on
+            // the FP64 pipe.  The others keep the panel-wise kernel.
             launch_plan_wy(dups, n, ws, p, djobs, st);
             launch_gemm_jobs(djobs, 4 * n, sched, st);  // Grams and Y = V^T X (independent)
             launch_wy_solve(n, ws, st);
             launch_gemm_jobs(djobs + 4 * (size_t) n, 2 * n, sched, st);
-        } else {
-            launch_apply_q(dups, n, ws, st);
         }
+        launch_apply_q(dups, n, ws, st);  // the sides not applied in WY form (plan_kernel zeroes META_WY)
         cnt[HCGB_STAGE_APPLY_Q]++;
     }
     mark(HCGB_STAGE_FINALIZE);

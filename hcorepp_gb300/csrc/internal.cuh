@@ -105,7 +105,8 @@ enum MetaField {
     META_KC_QRCP,
     META_KC_JACOBI,
     META_KC_FACTORS,
-    META_INTS = 16
+    META_WY,         // bit 0 / bit 1: the U / V factor's Q is applied in WY form (else apply_q_kernel)
+    META_INTS = 17
 };
 
 // Device workspace: n slots of `slot_doubles` doubles plus an int meta block.
@@ -152,7 +153,10 @@ void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int s
 constexpr int MAX_JOBS_PER_LAUNCH = 4096;
 constexpr int SCHED_INTS_PER_UPDATE = 10;  // >= (2 * 4n + 2) / n: one WY launch schedules 4n jobs
 // Q application in full WY form (Q = I - V T V^T, T^-1 = striu(V^T V) + diag(1/tau)): jobs for
-// the Grams, Y = V^T X and X -= V W, then the triangular solve T^-1 W = Y.
+// the Grams, Y = V^T X and X -= V W, then the triangular solve T^-1 W = Y.  Used for the sides
+// with at least WY_MIN_REFLECTORS reflectors (their products run on the tensor cores); the
+// others keep the panel-wise apply_q_kernel, which skips the WY sides.
+constexpr int WY_MIN_REFLECTORS = 48;
 void launch_plan_wy(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob *jobs, cudaStream_t st);
 void launch_wy_solve(int n, Workspace ws, cudaStream_t st);
 void launch_qr(Workspace ws, int n, cudaStream_t st);

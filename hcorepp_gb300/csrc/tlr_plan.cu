@@ -441,7 +441,8 @@ __global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params
     none.M = none.N = none.K = 0;
     none.oz = none.triA = none.triB = 0;
     for (int q = 0; q < 6; q++) jobs[(size_t) q * n + s] = none;
-    const int *meta = ws.meta + (size_t) s * META_INTS;
+    int *meta = ws.meta + (size_t) s * META_INTS;
+    meta[META_WY] = 0;
     const int st = meta[META_STATUS];
     if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;
     const int k = meta[META_K], m = meta[META_M], nn = meta[META_N], r = meta[META_NEWRANK];
@@ -449,6 +450,8 @@ __global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params
     const int ld = ws.ld, lk = ws.kmax;
     for (int side = 0; side < 2; side++) {
         const int rows = side ? nn : m, kk = rows < k ? rows : k;
+        if (!p.oz || kk < WY_MIN_REFLECTORS) continue;  // panel-wise apply_q_kernel
+        meta[META_WY] |= 1 << side;
         double *Vst = base + (side ? ws.off_vstack : ws.off_ustack);
         double *G = base + (side ? ws.off_mcopy : ws.off_m);
         double *W = base + ws.off_w + (size_t) side * lk * lk;
@@ -476,7 +479,7 @@ __global__ void __launch_bounds__(256) wy_solve_kernel(Workspace ws) {
     const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
     const int *meta = ws.meta + (size_t) slot * META_INTS;
     const int st = meta[META_STATUS];
-    if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;
+    if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND] || !(meta[META_WY] & (1 << side))) return;
     const int k = meta[META_K], rows = side ? meta[META_N] : meta[META_M], r = meta[META_NEWRANK];
     const int kk = rows < k ? rows : k;
     double *base = ws.slot(slot);

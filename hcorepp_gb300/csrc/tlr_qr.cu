@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(QR_THREADS) apply_q_kernel(const DevUpdate *up
     const int *meta = ws.meta + (size_t) slot * META_INTS;
     const int st = meta[META_STATUS];
     if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;
+    if (meta[META_WY] & (1 << side)) return;  // applied in WY form
     const int k = meta[META_K];
     const int m = side ? meta[META_N] : meta[META_M];
     const int r = meta[META_NEWRANK];
