@@ -473,9 +473,15 @@ __global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params
 }
 
 // Two CTAs per update (U side, V side): solve T^-1 W = Y in place, T^-1 = striu(G) + diag(1/tau),
-// by back substitution; one warp per column of W, lanes split the inner products (G is symmetric,
-// so row i of its upper part is read as column i).  tau_i = 0 (an identity reflector) gives W_i = 0.
+// by blocked back substitution over row blocks of 32 (bottom up): the block's rows first take the
+// product of the already solved rows (every thread a few (row, column) dot products; G is
+// symmetric, so row i of its upper part is read as column i, contiguous), then the 32 x 32
+// triangle is solved with one thread per column from shared memory.  tau_i = 0 (an identity
+// reflector) gives W_i = 0.
 __global__ void __launch_bounds__(256) wy_solve_kernel(Workspace ws) {
+    constexpr int BS = 32;
+    __shared__ double Gb[BS][BS + 1];
+    __shared__ double tb[BS];
     const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
     const int *meta = ws.meta + (size_t) slot * META_INTS;
     const int st = meta[META_STATUS];
@@ -487,17 +493,51 @@ __global__ void __launch_bounds__(256) wy_solve_kernel(Workspace ws) {
     const double *tau = base + (side ? ws.off_tauv : ws.off_tauu);
     double *W = base + ws.off_w + (size_t) side * ws.kmax * ws.kmax;
     const int lk = ws.kmax;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int c = warp; c < r; c += nw) {
-        double *w = W + (size_t) c * lk;
-        for (int i = kk - 1; i >= 0; i--) {
-            const double *gi = G + (size_t) i * lk;
-            double part = 0.0;
-            for (int j = i + 1 + lane; j < kk; j += 32) part = fma(gi[j], w[j], part);
-            part = warp_sum(part);
-            if (lane == 0) w[i] = tau[i] * (w[i] - part);
-            __syncwarp();
+    for (int bs = ((kk - 1) / BS) * BS; bs >= 0; bs -= BS) {
+        const int be = bs + BS < kk ? bs + BS : kk, nbk = be - bs;
+        // 1. rows bs..be-1 of W -= G[bs:be, be:kk] W[be:kk, :]
+        if (be < kk) {
+            for (int e = threadIdx.x; e < nbk * r; e += blockDim.x) {
+                const int i = bs + e % nbk, c = e / nbk;
+                const double *gi = G + (size_t) i * lk;
+                const double *wc = W + (size_t) c * lk;
+                double s0 = 0.0, s1 = 0.0;
+                int j = be;
+                for (; j + 1 < kk; j += 2) {
+                    s0 = fma(gi[j], wc[j], s0);
+                    s1 = fma(gi[j + 1], wc[j + 1], s1);
+                }
+                if (j < kk) s0 = fma(gi[j], wc[j], s0);
+                W[i + (size_t) c * lk] -= s0 + s1;
+            }
         }
+        // 2. the diagonal block: G[bs:be, bs:be] (upper part) and tau into shared memory
+        for (int e = threadIdx.x; e < nbk * nbk; e += blockDim.x) {
+            const int a = e % nbk, b = e / nbk;
+            Gb[a][b] = G[(size_t) (bs + b) * lk + bs + a];  // symmetric: G(a, b)
+        }
+        if (threadIdx.x < nbk) tb[threadIdx.x] = tau[bs + threadIdx.x];
+        __syncthreads();
+        for (int c = threadIdx.x; c < r; c += blockDim.x) {
+            double *wc = W + (size_t) c * lk + bs;
+            double x[BS];
+#pragma unroll
+            for (int a = 0; a < BS; a++) x[a] = a < nbk ? wc[a] : 0.0;
+#pragma unroll
+            for (int a = BS - 1; a >= 0; a--) {
+                if (a < nbk) {
+                    double sacc = x[a];
+#pragma unroll
+                    for (int b = a + 1; b < BS; b++)
+                        if (b < nbk) sacc = fma(-Gb[a][b], x[b], sacc);
+                    x[a] = tb[a] * sacc;
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < BS; a++)
+                if (a < nbk) wc[a] = x[a];
+        }
+        __syncthreads();
     }
 }
 
