@@ -7,14 +7,16 @@
 //   * each element becomes a 56-bit fixed-point integer relative to its group's exponent (rounded
 //     to nearest; the rounding error is 2^-57 of the group maximum) and is cut into S = 8 signed
 //     7-bit digits, A = sum_s 2^(e_i - 7 s) A^(s) with integer planes |A^(s)| <= 127, exact in FP16;
-//   * the plane products A^(s) B^(t) are integers; over a k-span of 128 every partial sum of a
-//     level L = s + t (at most 8 terms of 127 * 127 per k) stays below 2^24, so the FP32
-//     accumulators of the tensor cores hold them exactly;
+//   * the plane products A^(s) B^(t) are integers; over a k-chunk of 32 every partial sum of a
+//     level L = s + t (at most 8 terms of 127 * 127 per k) stays below 2^22, so the FP32
+//     accumulators of the tensor cores hold them exactly and an FP32 add of 1.5 * 2^23 exposes
+//     them as integers in the low mantissa bits;
 //   * levels s + t <= S + 1 are kept (the dropped ones sum to < 2^-44 of max|A_i| max|B_j| for
-//     k <= 512, the order of FP64's own worst-case bound) and every 128 k-steps each level is
-//     added into an FP64 accumulator with its power of two: C_ij = sum_L 2^(e_i + f_j - 7L) Q_L.
-// All of the splitting is integer work on the bit patterns; FP64 instructions are spent only on
-// the level flushes (16 per element per 128 k-steps) and the epilogue.
+//     k <= 512, the order of FP64's own worst-case bound); after every chunk the levels are added
+//     into two 64-bit integers (levels 2-5 and 6-9, each shifted to a common scale), which stay
+//     exact for k up to 2^14, and the tile ends with C_ij = 2^(e_i + f_j) (hi 2^-35 + lo 2^-63).
+// All of the splitting and combining is integer work; an output element costs 4 FP64
+// instructions (two conversions, two scalings) plus the epilogue.
 #include <cuda_fp16.h>
 
 #include "internal.cuh"
@@ -29,7 +31,6 @@ constexpr int OZ_W = OZ_S * OZ_B;       // fixed-point width (56 bits)
 constexpr int OZ_TM = 64, OZ_TN = 32;   // output tile per CTA
 constexpr int OZ_KC = 32;               // k-chunk staged in shared memory
 constexpr int OZ_LDS = 40;              // padded row of a plane in halves (conflict-free fragment loads)
-constexpr int OZ_FLUSH = 4;             // k-chunks per FP64 flush (4 x 32 = 128 keeps FP32 exact)
 constexpr int OZ_THREADS = 256;         // 8 warps (4 x 2), each a 16 x 16 piece of the tile
 constexpr int OZ_NOGROUP = -1100;       // exponent of an all-zero group
 
@@ -105,7 +106,7 @@ __device__ void oz_tile(const GemmJob &jb, int tile, __half *As, __half *Bs, int
     const int g = lane >> 2, c = lane & 3;
     const int wm = warp & 3, wn = warp >> 2;  // 4 x 2 warps, 16 x 16 each
     float acc[OZ_S][2][4];
-    double acc64[2][4];
+    long long hi[2][4], lo[2][4];  // levels 2-5 at scale 2^-35, levels 6-9 at scale 2^-63
 #pragma unroll
     for (int l = 0; l < OZ_S; l++)
 #pragma unroll
@@ -115,7 +116,7 @@ __device__ void oz_tile(const GemmJob &jb, int tile, __half *As, __half *Bs, int
 #pragma unroll
     for (int t = 0; t < 2; t++)
 #pragma unroll
-        for (int q = 0; q < 4; q++) acc64[t][q] = 0.0;
+        for (int q = 0; q < 4; q++) hi[t][q] = lo[t][q] = 0;
     // group-exponent sums of this thread's eight outputs
     int ebase[2][4];
 #pragma unroll
@@ -180,18 +181,18 @@ __device__ void oz_tile(const GemmJob &jb, int tile, __half *As, __half *Bs, int
             }
         }
         __syncthreads();
-        // 4. Flush the levels into FP64 every 128 k-steps and at the end.
-        if ((chunk + 1) % OZ_FLUSH == 0 || k0 + OZ_KC >= jb.K) {
+        // 4. Levels into the 64-bit integers (exact: |level| < 2^22 per chunk).
 #pragma unroll
-            for (int l = 0; l < OZ_S; l++)
+        for (int l = 0; l < OZ_S; l++)
 #pragma unroll
-                for (int t = 0; t < 2; t++)
+            for (int t = 0; t < 2; t++)
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        acc64[t][q] = fma((double) acc[l][t][q], pow2(ebase[t][q] - OZ_B * (l + 2)), acc64[t][q]);
-                        acc[l][t][q] = 0.f;
-                    }
-        }
+                for (int q = 0; q < 4; q++) {
+                    const long long v = (long long) (__float_as_int(acc[l][t][q] + 12582912.0f) - 0x4B400000);
+                    if (l < 4) hi[t][q] += v << (OZ_B * (3 - l));
+                    else lo[t][q] += v << (OZ_B * (7 - l));
+                    acc[l][t][q] = 0.f;
+                }
     }
     // 5. Epilogue: C = alpha * product + beta * C.
     const bool scale = jb.alpha != 1.0, accum = jb.beta != 0.0;
@@ -203,7 +204,9 @@ __device__ void oz_tile(const GemmJob &jb, int tile, __half *As, __half *Bs, int
             const int col = n0 + wn * 16 + t * 8 + 2 * c + (q & 1);
             if (row < jb.M && col < jb.N) {
                 double *cp = jb.C + row + (size_t) col * jb.ldc;
-                double v = scale ? jb.alpha * acc64[t][q] : acc64[t][q];
+                const double prod = fma((double) hi[t][q], pow2(ebase[t][q] - 35),
+                                        (double) lo[t][q] * pow2(ebase[t][q] - 63));
+                double v = scale ? jb.alpha * prod : prod;
                 if (accum) v = fma(jb.beta, *cp, v);
                 *cp = v;
             }
