@@ -69,9 +69,10 @@ __device__ __forceinline__ double job_b(const GemmJob &jb, int k, int j) {
     return jb.B[r + (size_t) c * jb.ldb];
 }
 
-// Products worth the split (enough k for the FP64 flushes to amortise, enough outputs for a tile).
+// Products worth the split (enough k to amortise the 4 FP64 instructions per output, enough outputs
+// for a tile).
 __host__ __device__ inline bool oz_shape(int M, int N, int K) {
-    return K >= 48 && M >= 16 && N >= 8 && (long long) M * N >= 2048;
+    return K >= 16 && M >= 16 && N >= 8 && (long long) M * N >= 2048;
 }
 
 struct DevTile {

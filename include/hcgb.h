@@ -151,7 +151,7 @@ int hcgb_set_concurrency(hcgb_context *ctx, int groups);
  * within the accuracy bound).  The expensive updates of all tiles then share a few k-waves. */
 int hcgb_set_k_order(hcgb_context *ctx, int policy);
 
-/* Factor products of k >= 48 with at least 2048 outputs run on the 16-bit tensor cores by
+/* Factor products of k >= 16 with at least 2048 outputs run on the 16-bit tensor cores by
  * error-free splitting (each FP64 operand cut into eight 7-bit integer digit planes relative to its
  * row / column maximum, plane products accumulated exactly in FP32 and combined in FP64; result
  * error below 2^-44 max|A_i| max|B_j|, the order of an FP64 product's worst-case bound).
