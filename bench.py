@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--k-order", type=int, default=1, choices=[0, 1],
                     help="0: ascending k per C tile (reference order); 1: costliest updates first")
     ap.add_argument("--mode", default="plain", choices=["plain", "mixed"],
-                    help="plain: FP64 throughout; mixed: single-precision Jacobi preconditioning of the core")
+                    help="plain: FP64 core Jacobi; mixed: float-float (48-bit) core Jacobi on the FP32 pipe")
     return ap.parse_args()
 
 
@@ -395,7 +395,7 @@ def gpu_arm(args, rank, world, local):
         "config": {"workload": args.workload, "n": w["n"], "nb": w["nb"], "tiles": f"{nt}x{nt}",
                    "updates_per_step": n_updates, "accuracy": w["accuracy"], "threshold": "relative",
                    "dense_diagonal": w["dense_diagonal"], "max_rank": maxr,
-                   "form": "plain_fp64" if args.mode == "plain" else "mixed (fp32-preconditioned core Jacobi)",
+                   "form": "plain_fp64" if args.mode == "plain" else "mixed (float-float core Jacobi)",
                    "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups, "k_order": "ascending" if args.k_order == 0 else "cost-descending",
                    "l2": "inputs larger than L2 (A, C arenas 1.4 GB each), no flush"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

@@ -40,6 +40,69 @@ __device__ __forceinline__ T group_sum(T v, int G) {
 __device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
 __device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
 
+// Float-float ("double-float") arithmetic for the mixed form's Jacobi: a value is the unevaluated
+// sum h + l of two floats (|l| <= ulp(h) / 2), 48 significant bits, on the FP32 pipe (about 70x the
+// FP64 rate on this GPU).  Error-free transformations (Dekker / Knuth two-sum, FMA two-product)
+// with explicitly rounded intrinsics so that nothing is contracted or reassociated.
+struct df {
+    float h, l;
+    __device__ __forceinline__ df() {}
+    __device__ __forceinline__ df(double v) {
+        h = __double2float_rn(v);
+        l = __double2float_rn(v - (double) h);
+    }
+    __device__ __forceinline__ explicit operator double() const { return (double) h + (double) l; }
+};
+__device__ __forceinline__ df operator-(df a) {
+    df r;
+    r.h = -a.h;
+    r.l = -a.l;
+    return r;
+}
+// c + a * b
+__device__ __forceinline__ df df_fma(df a, df b, df c) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    const float s = __fadd_rn(c.h, p);
+    const float bb = __fsub_rn(s, c.h);
+    float err = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    err = __fadd_rn(err, __fadd_rn(c.l, e));
+    df r;
+    r.h = __fadd_rn(s, err);
+    r.l = __fsub_rn(err, __fsub_rn(r.h, s));
+    return r;
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+    const float s = __fadd_rn(a.h, b.h);
+    const float bb = __fsub_rn(s, a.h);
+    float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    err = __fadd_rn(err, __fadd_rn(a.l, b.l));
+    df r;
+    r.h = __fadd_rn(s, err);
+    r.l = __fsub_rn(err, __fsub_rn(r.h, s));
+    return r;
+}
+// a * b + c in the Jacobi element type.
+__device__ __forceinline__ double tfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float tfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ df tfma(df a, df b, df c) { return df_fma(a, b, c); }
+
+template <>
+__device__ __forceinline__ df group_sum<df>(df v, int G) {
+    for (int o = G >> 1; o > 0; o >>= 1) {
+        df w;
+        w.h = __shfl_xor_sync(0xffffffffu, v.h, o);
+        w.l = __shfl_xor_sync(0xffffffffu, v.l, o);
+        v = df_add(v, w);
+    }
+    return v;
+}
+// Unit roundoff used for the noise floor of a Jacobi run in type T.
+template <typename T> __device__ __forceinline__ double unit_roundoff() { return DBL_EPSILON; }
+template <> __device__ __forceinline__ double unit_roundoff<df>() { return 3.552713678800501e-15; }  // 2^-48
+
 // Tangent of the Jacobi angle that orthogonalises a pair with squared norms a, b and inner
 // product c: zeta = (b - a) / (2 c), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)) (Rutishauser).
 // Evaluated in single precision after scaling both terms by the same power of two (read off the
@@ -101,7 +164,7 @@ __device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, dou
                         xr[q] = x[r];
                         yr[q] = y[r];
                     }
-                    c = fma(xr[q], yr[q], c);
+                    c = tfma(xr[q], yr[q], c);
                 }
             }
             c = group_sum(c, G);
@@ -112,8 +175,10 @@ __device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, dou
                 dj = dsc[j];
             }
             const double cd = ACC ? (double) c : (double) c * di * dj;  // true inner product
+            (void) cd;
             const bool rot = act && a > tiny && b > tiny && cd * cd > tol2 * a * b;
-            if (!ACC && rot) {
+            if constexpr (!ACC) {
+              if (rot) {
                 const double tt = (double) jacobi_tangent(a, b, cd);
                 const double q = fma(tt, tt, 1.0);
                 const double cs = rsqrt(q);
@@ -124,8 +189,8 @@ __device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, dou
                     if (G * q2 < rows) {
                         const int r = gl + G * q2;
                         if (r < rows) {
-                            x[r] = fma(-t1, yr[q2], xr[q2]);
-                            y[r] = fma(t2, xr[q2], yr[q2]);
+                            x[r] = tfma(-t1, yr[q2], xr[q2]);
+                            y[r] = tfma(t2, xr[q2], yr[q2]);
                         }
                     }
                 }
@@ -138,7 +203,8 @@ __device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, dou
                     dsc[dstride + j] = dvj * q * cs;
                     rotations++;
                 }
-            } else if (ACC && rot) {
+              }
+            } else if (rot) {
                 const float tf = jacobi_tangent(a, b, cd);
                 const T tt = (T) tf;
                 const T cs = rsqrt_t(fma(tt, tt, T(1)));
@@ -182,7 +248,7 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
     const double tol2 = tol * tol;
     // Noise floor from double precision also for single-precision sweeps: X is graded (each column
     // accurate relative to its own norm), so small columns are data, not rounding noise.
-    const double noise = DBL_EPSILON * (double) (rows > 1 ? rows : 1);
+    const double noise = unit_roundoff<T>() * (double) (rows > 1 ? rows : 1);
     const int n2 = ncols + (ncols & 1);
     int sweeps = 0;
     bool converged = ncols < 2;
@@ -502,45 +568,36 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     bool converged = true;
     const double tol64 = 8.0 * DBL_EPSILON * (double) (kV > 1 ? kV : 1);
     if (p.mode == 1) {
-        // Mixed form: single-precision sweeps on a copy of X accumulate the rotations J32, then
-        // X <- X J32 on DMMA and double-precision sweeps finish (J32 is orthogonal to ~1e-6, so
-        // X J32 keeps the singular values to that relative accuracy and its columns start nearly
-        // orthogonal: typically one or two double-precision sweeps remain).
-        float *X32 = reinterpret_cast<float *>(base + ws.off_mixed);
-        float *J32 = X32 + (size_t) kV * rk;
-        for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) X32[e] = (float) X[(e % kV) + (size_t) (e / kV) * ldx];
-        for (int e = threadIdx.x; e < rk * rk; e += blockDim.x) J32[e] = (e % rk) == (e / rk) ? 1.0f : 0.0f;
+        // Mixed form: the sweeps run in float-float arithmetic on the FP32 pipe (48-bit
+        // significands; see struct df), after an exact power-of-two scaling that brings the largest
+        // entry of X near 1 (float range).  The rotation parameters, norms and tests stay in double;
+        // convergence is judged against 16 * 2^-48 * rows.
+        __shared__ int s_emax;
+        if (threadIdx.x == 0) s_emax = 0;
         __syncthreads();
-        int sw32 = 0;
-        bool conv32 = true;
-        jacobi_dispatch<float, true, RPL>(X32, kV, kV, rk, nrm, &s_rot, &s_amax, &sw32, &conv32,
-                                          4.0 * FLT_EPSILON * sqrt((double) kV), MAX_JACOBI_SWEEPS, J32, rk, dsc,
-                                          ws.kmax);
-        // W = X J32 (kV x rk) on DMMA into XV, then back into X.
-        {
-            const int ntr = (kV + 7) >> 3, ntc = (rk + 7) >> 3;
-            for (int idx = warp; idx < ntr * ntc; idx += nw) {
-                const int tr = idx % ntr, tc = idx / ntr;
-                const int irow = tr * 8 + lr, icol = tc * 8 + lr;
-                double d0 = 0.0, d1 = 0.0;
-                for (int l4 = 0; l4 < rk; l4 += 4) {
-                    const int l = l4 + lc;
-                    const double av = (irow < kV && l < rk) ? X[irow + (size_t) l * ldx] : 0.0;
-                    const double bv = (icol < rk && l < rk) ? (double) J32[l + (size_t) icol * rk] : 0.0;
-                    dmma(d0, d1, av, bv);
-                }
-                const int col = tc * 8 + 2 * lc;
-                if (irow < kV && col < rk) XV[irow + (size_t) col * ld] = d0;
-                if (irow < kV && col + 1 < rk) XV[irow + (size_t) (col + 1) * ld] = d1;
-            }
-            __syncthreads();
-            for (int i = warp; i < rk; i += nw)
-                for (int l = lane; l < kV; l += 32) X[l + (size_t) i * ldx] = XV[l + (size_t) i * ld];
-            __syncthreads();
+        int em = 0;
+        for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) {
+            const int ef = (int) ((__double_as_longlong(X[(e % kV) + (size_t) (e / kV) * ldx]) >> 52) & 0x7ff);
+            em = em > ef ? em : ef;
         }
-        jacobi_dispatch<double, false, RPL>(X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
-                                            MAX_JACOBI_SWEEPS, (double *) nullptr, 0, dsc, ws.kmax);
-        sweeps += 100 * sw32;  // record: single-precision sweeps in the hundreds
+        atomicMax(&s_emax, em);
+        __syncthreads();
+        const int eshift = s_emax ? s_emax - 1023 : 0;  // X * 2^-eshift has entries below 2
+        const double down = __hiloint2double((1023 - eshift) << 20, 0), up = __hiloint2double((1023 + eshift) << 20, 0);
+        df *Xd = reinterpret_cast<df *>(X);
+        for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) {
+            const size_t o = (e % kV) + (size_t) (e / kV) * ldx;
+            Xd[o] = df(X[o] * down);
+        }
+        __syncthreads();
+        const double tol_df = 16.0 * 3.552713678800501e-15 * (double) (kV > 1 ? kV : 1);
+        jacobi_dispatch<df, false, RPL>(Xd, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol_df,
+                                        MAX_JACOBI_SWEEPS, (df *) nullptr, 0, dsc, ws.kmax);
+        for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) {
+            const size_t o = (e % kV) + (size_t) (e / kV) * ldx;
+            X[o] = (double) Xd[o] * up;
+        }
+        __syncthreads();
     } else {
         jacobi_dispatch<double, false, RPL>(X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
                                             MAX_JACOBI_SWEEPS, (double *) nullptr, 0, dsc, ws.kmax);
