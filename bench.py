@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--groups", type=int, default=8, help="independent C-tile groups (streams)")
     ap.add_argument("--k-order", type=int, default=1, choices=[0, 1],
                     help="0: ascending k per C tile (reference order); 1: costliest updates first")
-    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"],
+    ap.add_argument("--mode", default="mixed", choices=["plain", "mixed"],
                     help="plain: FP64 core Jacobi; mixed: float-float (48-bit) core Jacobi on the FP32 pipe")
     return ap.parse_args()
 

@@ -165,11 +165,12 @@ def test_trans_operands(T):
     assert rel_fro(gc2.to_dense(), exact2) < 1e-10
 
 
-@pytest.mark.parametrize("k_order,oz", [(0, True), (1, True), (0, False)])
-def test_tlr_multiply_vs_oracle(T, k_order, oz):
+@pytest.mark.parametrize("k_order,oz,mixed", [(0, True, False), (1, True, False), (0, False, False), (1, True, True)])
+def test_tlr_multiply_vs_oracle(T, k_order, oz, mixed):
     """A 4x4-tile multiply (nb=128) through hcgb_tlr_gemm against the oracle's tile loop, in the
     reference's k order and in the cost-first order (same sum, other rounding order), with the
-    large products and the WY Q application on the tensor cores (oz) and all on the FP64 pipe."""
+    large products and the WY Q application on the tensor cores (oz) and all on the FP64 pipe, and
+    with the float-float core Jacobi (mixed)."""
     import torch
     from hcorepp_gb300 import _lib as L
     from hcorepp_gb300.problems import KernelMatrix
@@ -202,8 +203,8 @@ def test_tlr_multiply_vs_oracle(T, k_order, oz):
     ctx.set_k_order(k_order)
     ctx.set_tensor_products(oz)
     try:
-        T.tlr_gemm(1.0, mats["A"], mats["B"], 1.0, mats["C"], T.CompressionParameters(acc, truncated_svd=True),
-                   info)
+        T.tlr_gemm(1.0, mats["A"], mats["B"], 1.0, mats["C"],
+                   T.CompressionParameters(acc, truncated_svd=True, mode=L.MIXED if mixed else L.PLAIN_FP64), info)
         torch.cuda.synchronize()
     finally:
         ctx.set_k_order(0)
