@@ -306,6 +306,195 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
 }
 
 // Lane-group / register-tile choice for a column length: G lanes per pair, RPL rows per lane.
+// ---------------------------------------------------------------------------------------------
+// Float-float Jacobi (mixed form): the columns, the tracked squared norms and the scales d, 1/d are
+// all float-float values, so neither the rows nor the per-pair bookkeeping touch the FP64 pipe.
+// Same method as jacobi_sweep (round-robin ordering, scaled rotations, tracked norms); the rotation
+// tangent is a float (any tangent gives an exact rotation once cos = 1/sqrt(1 + t^2) is formed to
+// float-float accuracy, which one Newton step on the float reciprocal square root does).
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ df df_mul(df a, df b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    df r;
+    r.h = __fadd_rn(p, e);
+    r.l = __fsub_rn(e, __fsub_rn(r.h, p));
+    return r;
+}
+__device__ __forceinline__ df df_f(float v) {
+    df r;
+    r.h = v;
+    r.l = 0.f;
+    return r;
+}
+// 1 / sqrt(q) for q >= 1 to float-float accuracy: two Newton steps r <- r + r (1 - q r^2) / 2 from
+// the float reciprocal square root (about 22 -> 44 -> 48 correct bits).
+__device__ __forceinline__ df df_rsqrt(df q) {
+    df r = df_f(rsqrtf(q.h));
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const df res = df_add(df_f(1.f), -df_mul(q, df_mul(r, r)));  // 1 - q r^2, small
+        r = df_add(r, df_mul(df_mul(r, res), df_f(0.5f)));
+    }
+    return r;
+}
+
+template <int G, int RPL>
+__device__ int jacobi_sweep_df(df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, float tol, float tiny,
+                               int n2) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    constexpr int PPW = 32 / G;
+    const int gl = lane % G, grp = lane / G;
+    const int npairs = n2 / 2;
+    const int nchunks = (npairs + PPW - 1) / PPW;
+    int rotations = 0;
+    for (int t = 0; t < n2 - 1; t++) {
+        for (int ch = warp; ch < nchunks; ch += nw) {
+            const int pp = ch * PPW + grp;
+            int i = 0, j = 0;
+            bool act = pp < npairs;
+            if (act) {
+                jacobi_pair(t, pp, n2, i, j);
+                act = i < ncols && j < ncols;
+            }
+            df *x = X + (size_t) (act ? i : 0) * ldx;
+            df *y = X + (size_t) (act ? j : 0) * ldx;
+            df xr[RPL], yr[RPL];
+            df c = df_f(0.f);
+#pragma unroll
+            for (int q = 0; q < RPL; q++) {
+                xr[q] = yr[q] = df_f(0.f);
+                if (G * q < rows) {
+                    const int r = gl + G * q;
+                    if (act && r < rows) {
+                        xr[q] = x[r];
+                        yr[q] = y[r];
+                    }
+                    c = df_fma(xr[q], yr[q], c);
+                }
+            }
+            c = group_sum(c, G);
+            df a = df_f(0.f), b = df_f(0.f), di = df_f(1.f), dj = df_f(1.f);
+            if (act) {
+                a = nrm[i];
+                b = nrm[j];
+                di = ds[i];
+                dj = ds[j];
+            }
+            const df cd = df_mul(df_mul(c, di), dj);  // true inner product
+            // |c| / sqrt(a b) > tol, in float (all quantities well inside the float range)
+            const bool rot = act && a.h > tiny && b.h > tiny && fabsf(cd.h) * rsqrtf(a.h) * rsqrtf(b.h) > tol;
+            if (rot) {
+                const float num = df_add(b, -a).h, den = 2.f * cd.h;
+                const float zf = num / den;
+                const float tt = fabsf(zf) > 1.0e18f ? 0.5f / zf
+                                                     : copysignf(1.0f, zf) / (fabsf(zf) + sqrtf(fmaf(zf, zf, 1.0f)));
+                const df q = df_add(df_f(1.f), df_mul(df_f(tt), df_f(tt)));
+                const df cs = df_rsqrt(q);
+                const df dvi = dv[i], dvj = dv[j];
+                const df t1 = df_mul(df_mul(df_f(tt), dj), dvi), t2 = df_mul(df_mul(df_f(tt), di), dvj);
+                const df mt1 = -t1;
+#pragma unroll
+                for (int q2 = 0; q2 < RPL; q2++) {
+                    if (G * q2 < rows) {
+                        const int r = gl + G * q2;
+                        if (r < rows) {
+                            x[r] = df_fma(mt1, yr[q2], xr[q2]);
+                            y[r] = df_fma(t2, xr[q2], yr[q2]);
+                        }
+                    }
+                }
+                if (gl == 0) {
+                    const df tc = df_mul(df_f(tt), cd);
+                    nrm[i] = df_add(a, -tc);
+                    nrm[j] = df_add(b, tc);
+                    ds[i] = df_mul(di, cs);
+                    ds[j] = df_mul(dj, cs);
+                    const df qcs = df_mul(q, cs);
+                    dv[i] = df_mul(dvi, qcs);
+                    dv[j] = df_mul(dvj, qcs);
+                    rotations++;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    return rotations;
+}
+
+template <int G, int RPL>
+__device__ void jacobi_df(df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, int *s_rot, float *s_amax,
+                          int *sweeps_out, bool *converged_out, float tol, int max_sweeps) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const float noise = 3.5527137e-15f * (float) (rows > 1 ? rows : 1);  // 2^-48 rows
+    const int n2 = ncols + (ncols & 1);
+    int sweeps = 0;
+    bool converged = ncols < 2;
+    for (int jj = threadIdx.x; jj < ncols; jj += blockDim.x) ds[jj] = dv[jj] = df_f(1.f);
+    __syncthreads();
+    // Exact squared norms; the scales of the previous sweep are folded into the columns.
+    auto fold_and_norms = [&](float &amax) {
+        for (int jj = warp; jj < ncols; jj += nw) {
+            df *col = X + (size_t) jj * ldx;
+            const df d = ds[jj];
+            const bool scale = d.h != 1.f || d.l != 0.f;
+            df sq = df_f(0.f);
+            for (int r = lane; r < rows; r += 32) {
+                df v = col[r];
+                if (scale) {
+                    v = df_mul(v, d);
+                    col[r] = v;
+                }
+                sq = df_fma(v, v, sq);
+            }
+            sq = group_sum(sq, 32);
+            __syncwarp();
+            if (lane == 0) {
+                nrm[jj] = sq;
+                ds[jj] = dv[jj] = df_f(1.f);
+            }
+            amax = fmaxf(amax, sq.h);
+        }
+    };
+    while (!converged && sweeps < max_sweeps) {
+        if (threadIdx.x == 0) {
+            *s_rot = 0;
+            *s_amax = 0.f;
+        }
+        __syncthreads();
+        float amax = 0.f;
+        fold_and_norms(amax);
+        if (lane == 0) atomicMax(reinterpret_cast<int *>(s_amax), __float_as_int(amax));  // amax >= 0
+        __syncthreads();
+        const float tiny = *s_amax * noise * noise;
+        const int rot = jacobi_sweep_df<G, RPL>(X, ldx, rows, ncols, nrm, ds, dv, tol, tiny, n2);
+        if (rot) atomicAdd(s_rot, rot);
+        __syncthreads();
+        sweeps++;
+        converged = (*s_rot == 0);
+        __syncthreads();
+    }
+    float amax = 0.f;
+    fold_and_norms(amax);  // a sweep limit can leave scales unfolded
+    __syncthreads();
+    *sweeps_out = sweeps;
+    *converged_out = converged;
+}
+
+template <int MAXRPL>
+__device__ void jacobi_df_dispatch(df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, int *s_rot,
+                                   float *s_amax, int *sweeps, bool *conv, float tol, int max_sweeps) {
+    if (rows <= 32) jacobi_df<4, 8>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 64) jacobi_df<8, 8>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 128 && MAXRPL >= 16) jacobi_df<8, 16>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 128) jacobi_df<16, 8>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 256 && MAXRPL >= 16) jacobi_df<16, 16>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 256 || MAXRPL <= 8) jacobi_df<32, 8>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else jacobi_df<32, MAXRPL>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+}
+
 template <typename T, bool ACC, int MAXRPL>
 __device__ void jacobi_dispatch(T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax,
                                 int *sweeps, bool *conv, double tol, int max_sweeps, T *J, int ldj, double *dsc,
@@ -590,9 +779,11 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
             Xd[o] = df(X[o] * down);
         }
         __syncthreads();
-        const double tol_df = 16.0 * 3.552713678800501e-15 * (double) (kV > 1 ? kV : 1);
-        jacobi_dispatch<df, false, RPL>(Xd, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol_df,
-                                        MAX_JACOBI_SWEEPS, (df *) nullptr, 0, dsc, ws.kmax);
+        const float tol_df = 16.f * 3.5527137e-15f * (float) (kV > 1 ? kV : 1);
+        // norms and scales as float-float values in the (double-sized) nrm and dsc arrays
+        jacobi_df_dispatch<RPL>(Xd, ldx, kV, rk, reinterpret_cast<df *>(nrm), reinterpret_cast<df *>(dsc),
+                                reinterpret_cast<df *>(dsc + ws.kmax), &s_rot, reinterpret_cast<float *>(&s_amax),
+                                &sweeps, &converged, tol_df, MAX_JACOBI_SWEEPS);
         for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) {
             const size_t o = (e % kV) + (size_t) (e / kV) * ldx;
             X[o] = (double) Xd[o] * up;
