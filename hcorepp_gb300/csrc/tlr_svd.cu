@@ -651,6 +651,167 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
     return rkeep;
 }
 
+// Float-float reciprocal and square root (one correction step each from the float result).
+__device__ __forceinline__ df df_div(df a, df b) {
+    const float q0 = __fdiv_rn(a.h, b.h);
+    const df r = df_add(a, -df_mul(df_f(q0), b));  // a - q0 b
+    const float q1 = __fdiv_rn(r.h, b.h);
+    df q;
+    q.h = __fadd_rn(q0, q1);
+    q.l = __fsub_rn(q1, __fsub_rn(q.h, q0));
+    return q;
+}
+__device__ __forceinline__ df df_sqrt(df v) {
+    if (v.h <= 0.f) return df_f(0.f);
+    const float s0 = sqrtf(v.h);
+    const df r = df_add(v, -df_mul(df_f(s0), df_f(s0)));  // v - s0^2
+    const float s1 = __fdiv_rn(r.h, 2.f * s0);
+    df q;
+    q.h = __fadd_rn(s0, s1);
+    q.l = __fsub_rn(s1, __fsub_rn(q.h, s0));
+    return q;
+}
+
+// Float-float version of qrcp_truncated (mixed form), on a matrix scaled so that its entries are
+// near 1: same pivoting, early stop (stop2 on squared norms; stop2 == 0 with rel2 > 0 sets
+// stop2 = rel2 * |r_00|^2 after the first pivot; stop2 < 0 disables it) and norm downdating with
+// exact recomputation when a downdate cancels.  Pivot keys are the float norms' bit patterns
+// (non-negative floats order like their bits).
+__device__ int qrcp_truncated_df(df *A, int lda, int mrows, int ncols, float stop2, float rel2, df *nrm, df *nref,
+                                 int *pvt, float *red, int *redi) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int j = warp; j < ncols; j += nw) {
+        const df *col = A + (size_t) j * lda;
+        df t = df_f(0.f);
+        for (int i = lane; i < mrows; i += 32) t = df_fma(col[i], col[i], t);
+        t = group_sum(t, 32);
+        if (lane == 0) nrm[j] = nref[j] = t;
+    }
+    for (int j = threadIdx.x; j < ncols; j += blockDim.x) pvt[j] = j;
+    __syncthreads();
+    const int kk = mrows < ncols ? mrows : ncols;
+    int rkeep = kk;
+    for (int s = 0; s < kk; s++) {
+        int bv = -1, bi = s;  // float bits of the largest remaining squared norm
+        for (int j = s + threadIdx.x; j < ncols; j += blockDim.x) {
+            const int v = __float_as_int(nrm[j].h);
+            if (v > bv) {
+                bv = v;
+                bi = j;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const int ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            redi[warp] = bv;
+            redi[8 + warp] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int v = redi[0], b = redi[8];
+            for (int w = 1; w < nw; w++)
+                if (redi[w] > v || (redi[w] == v && redi[8 + w] < b)) {
+                    v = redi[w];
+                    b = redi[8 + w];
+                }
+            redi[16] = v;
+            redi[17] = b;
+            if (s == 0) red[33] = (stop2 == 0.f && rel2 > 0.f) ? rel2 * __int_as_float(v) : stop2;
+        }
+        __syncthreads();
+        const float bvf = __int_as_float(redi[16]);
+        bi = redi[17];
+        const float lim = red[33];
+        if (bvf <= lim || bvf <= 0.f) {
+            rkeep = s;
+            break;
+        }
+        if (bi != s) {
+            df *cs = A + (size_t) s * lda, *cb = A + (size_t) bi * lda;
+            for (int i = threadIdx.x; i < mrows; i += blockDim.x) {
+                const df t = cs[i];
+                cs[i] = cb[i];
+                cb[i] = t;
+            }
+            if (threadIdx.x == 0) {
+                const df t = nrm[s];
+                nrm[s] = nrm[bi];
+                nrm[bi] = t;
+                const df tr = nref[s];
+                nref[s] = nref[bi];
+                nref[bi] = tr;
+                const int ti = pvt[s];
+                pvt[s] = pvt[bi];
+                pvt[bi] = ti;
+            }
+        }
+        __syncthreads();
+        // Householder vector of column s (rows s..mrows-1), dlarfg convention.
+        df *x = A + (size_t) s * lda;
+        df ss = df_f(0.f);
+        for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) ss = df_fma(x[i], x[i], ss);
+        ss = group_sum(ss, 32);
+        __syncthreads();
+        df *redd = reinterpret_cast<df *>(red + 40);  // 8 warp partials, then tau and scale
+        if (lane == 0) redd[warp] = ss;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            df t = df_f(0.f);
+            for (int w = 0; w < nw; w++) t = df_add(t, redd[w]);
+            const df alpha = x[s];
+            df tau = df_f(0.f), scale = df_f(0.f), beta = alpha;
+            if (t.h != 0.f) {
+                const df nrmx = df_sqrt(df_fma(alpha, alpha, t));
+                beta = alpha.h >= 0.f ? -nrmx : nrmx;
+                tau = df_div(df_add(beta, -alpha), beta);
+                scale = df_div(df_f(1.f), df_add(alpha, -beta));
+            }
+            x[s] = beta;
+            redd[8] = tau;
+            redd[9] = scale;
+        }
+        __syncthreads();
+        const df tau = redd[8], scale = redd[9];
+        for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) x[i] = df_mul(x[i], scale);
+        __syncthreads();
+        const bool has_tau = tau.h != 0.f;
+        for (int j = s + 1 + warp; j < ncols; j += nw) {
+            df *y = A + (size_t) j * lda;
+            df w = df_f(0.f);
+            if (has_tau) {
+                w = lane == 0 ? y[s] : df_f(0.f);
+                for (int i = s + 1 + lane; i < mrows; i += 32) w = df_fma(x[i], y[i], w);
+                w = df_mul(group_sum(w, 32), tau);
+                const df mw = -w;
+                for (int i = s + 1 + lane; i < mrows; i += 32) y[i] = df_fma(mw, x[i], y[i]);
+            }
+            const df ys = df_add(y[s], -w);  // all lanes read the old y[s] before lane 0 writes it
+            __syncwarp();
+            if (lane == 0) y[s] = ys;
+            df nn = df_add(nrm[j], -df_mul(ys, ys));
+            const bool exact = !(nn.h > 1e-8f * nref[j].h);  // lost 4+ digits since the last exact value
+            if (exact) {
+                nn = df_f(0.f);
+                for (int i = s + 1 + lane; i < mrows; i += 32) nn = df_fma(y[i], y[i], nn);
+                nn = group_sum(nn, 32);
+            }
+            __syncwarp();
+            if (lane == 0) {
+                nrm[j] = nn;
+                if (exact) nref[j] = nn;
+            }
+        }
+        __syncthreads();
+    }
+    return rkeep;
+}
+
 template <int RPL>
 __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdate *ups, Workspace ws, Params p,
                                                                int smem_doubles) {
@@ -737,7 +898,35 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         }
     }
     const long long t1 = clock64();
-    int rk = qrcp_truncated(Mw, ldw, kU, kV, stop2, rel, nrm, inv, pvt, red, redi);
+    int rk;
+    int eshift = 0;  // mixed form: Mw holds float-float values of M * 2^-eshift from here to step 4
+    if (p.mode == 1) {
+        // Exact power-of-two scaling that brings the largest entry of M near 1 (float range), then
+        // the pivoted QR and the Jacobi sweeps in float-float arithmetic on the FP32 pipe.
+        __shared__ int s_emax;
+        if (threadIdx.x == 0) s_emax = 0;
+        __syncthreads();
+        int em = 0;
+        for (int e = threadIdx.x; e < kU * kV; e += blockDim.x) {
+            const int ef = (int) ((__double_as_longlong(Mw[(e % kU) + (size_t) (e / kU) * ldw]) >> 52) & 0x7ff);
+            em = em > ef ? em : ef;
+        }
+        atomicMax(&s_emax, em);
+        __syncthreads();
+        eshift = s_emax ? s_emax - 1023 : 0;
+        const double down = __hiloint2double((1023 - eshift) << 20, 0);
+        df *Md = reinterpret_cast<df *>(Mw);
+        for (int e = threadIdx.x; e < kU * kV; e += blockDim.x) {
+            const size_t o = (e % kU) + (size_t) (e / kU) * ldw;
+            Md[o] = df(Mw[o] * down);
+        }
+        __syncthreads();
+        const float stop2f = stop2 > 0.0 ? (float) (stop2 * down * down) : (float) stop2;
+        rk = qrcp_truncated_df(Md, ldw, kU, kV, stop2f, (float) (rel * rel), reinterpret_cast<df *>(nrm),
+                               reinterpret_cast<df *>(inv), pvt, reinterpret_cast<float *>(red), redi);
+    } else {
+        rk = qrcp_truncated(Mw, ldw, kU, kV, stop2, rel, nrm, inv, pvt, red, redi);
+    }
     const long long t2 = clock64();
     if (rk < 1) rk = 1;
     double *XV = base + ws.off_xv;
@@ -757,28 +946,10 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     bool converged = true;
     const double tol64 = 8.0 * DBL_EPSILON * (double) (kV > 1 ? kV : 1);
     if (p.mode == 1) {
-        // Mixed form: the sweeps run in float-float arithmetic on the FP32 pipe (48-bit
-        // significands; see struct df), after an exact power-of-two scaling that brings the largest
-        // entry of X near 1 (float range).  The rotation parameters, norms and tests stay in double;
-        // convergence is judged against 16 * 2^-48 * rows.
-        __shared__ int s_emax;
-        if (threadIdx.x == 0) s_emax = 0;
-        __syncthreads();
-        int em = 0;
-        for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) {
-            const int ef = (int) ((__double_as_longlong(X[(e % kV) + (size_t) (e / kV) * ldx]) >> 52) & 0x7ff);
-            em = em > ef ? em : ef;
-        }
-        atomicMax(&s_emax, em);
-        __syncthreads();
-        const int eshift = s_emax ? s_emax - 1023 : 0;  // X * 2^-eshift has entries below 2
-        const double down = __hiloint2double((1023 - eshift) << 20, 0), up = __hiloint2double((1023 + eshift) << 20, 0);
+        // Mixed form: X = R_rk^T is already float-float (scaled by 2^-eshift); the sweeps run in
+        // float-float arithmetic, every per-pair quantity included (see jacobi_sweep_df).
         df *Xd = reinterpret_cast<df *>(X);
-        for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) {
-            const size_t o = (e % kV) + (size_t) (e / kV) * ldx;
-            Xd[o] = df(X[o] * down);
-        }
-        __syncthreads();
+        const double up = __hiloint2double((1023 + eshift) << 20, 0);
         const float tol_df = 16.f * 3.5527137e-15f * (float) (kV > 1 ? kV : 1);
         // norms and scales as float-float values in the (double-sized) nrm and dsc arrays
         jacobi_df_dispatch<RPL>(Xd, ldx, kV, rk, reinterpret_cast<df *>(nrm), reinterpret_cast<df *>(dsc),
