@@ -211,7 +211,7 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     // that carries it (a single update included).
     if (sh.any_compressed_c && ws.order) launch_order(n, ws, st);
     if (sh.any_compressed_c) {
-        launch_qr(ws, n, st);
+        launch_qr(ws, n, p.mode == 1, st);
         cnt[HCGB_STAGE_QR]++;
     }
     mark(HCGB_STAGE_CORE_SVD);

@@ -160,7 +160,7 @@ constexpr int SCHED_INTS_PER_UPDATE = 10;  // >= (2 * 4n + 2) / n: one WY launch
 constexpr int WY_MIN_REFLECTORS = 48;
 void launch_plan_wy(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob *jobs, cudaStream_t st);
 void launch_wy_solve(int n, Workspace ws, cudaStream_t st);
-void launch_qr(Workspace ws, int n, cudaStream_t st);
+void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st);
 void launch_core_svd(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st);
 void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st);
 void launch_finalize(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st);

@@ -160,7 +160,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     for (int ph = 0; ph < 3; ph++)
         if (pm[ph] > 0 && pn[ph] > 0) launch_gemm_jobs(jobs + ph, 1, sched, st);
     if (ck) {
-        launch_qr(ws, 1, st);
+        launch_qr(ws, 1, prm.mode == 1, st);
         launch_core_svd(dup, 1, ws, prm, st);
         launch_apply_q(dup, 1, ws, st);
     }

@@ -10,6 +10,7 @@
 // kept for the later Q application; the trailing update A <- (I - V T^T V^T) A is two FP64
 // tensor-core (DMMA) products with V and W = V^T A staged in shared memory.
 #include "internal.cuh"
+#include "df.cuh"
 
 namespace hcgb {
 
@@ -76,6 +77,54 @@ __device__ void factor_panel(double *Ps, int ldp, int mr, int nbp, double *tau_s
                 w = warp_sum(w) * tau;
                 if (lane == 0) y[j] -= w;
                 for (int r = j + 1 + lane; r < mr; r += 32) y[r] = fma(-w, x[r], y[r]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Float-float version of factor_panel (mixed form), in place on the panel held as float-float
+// values of (panel * 2^-eshift); same dlarfg convention.  red: >= 24 doubles of scratch.
+__device__ void factor_panel_df(df *Ps, int ldp, int mr, int nbp, double *tau_s, double *red) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    df *redd = reinterpret_cast<df *>(red);
+    for (int j = 0; j < nbp; j++) {
+        df *x = Ps + (size_t) j * ldp;
+        df ss = df_f(0.f);
+        for (int r = j + 1 + threadIdx.x; r < mr; r += blockDim.x) ss = df_fma(x[r], x[r], ss);
+        ss = df_group_sum(ss, 32);
+        __syncthreads();
+        if (lane == 0) redd[warp] = ss;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            df t = df_f(0.f);
+            for (int w = 0; w < nw; w++) t = df_add(t, redd[w]);
+            const df alpha = x[j];
+            df tau = df_f(0.f), scale = df_f(0.f), beta = alpha;
+            if (t.h != 0.f) {
+                const df nrmx = df_sqrt(df_fma(alpha, alpha, t));
+                beta = alpha.h >= 0.f ? -nrmx : nrmx;
+                tau = df_div(df_add(beta, -alpha), beta);
+                scale = df_div(df_f(1.f), df_add(alpha, -beta));
+            }
+            tau_s[j] = (double) tau;
+            redd[8] = scale;
+            redd[9] = tau;
+            x[j] = beta;
+        }
+        __syncthreads();
+        const df scale = redd[8], tau = redd[9];
+        for (int r = j + 1 + threadIdx.x; r < mr; r += blockDim.x) x[r] = df_mul(x[r], scale);
+        __syncthreads();
+        if (tau.h != 0.f) {
+            for (int c = j + 1 + warp; c < nbp; c += nw) {
+                df *y = Ps + (size_t) c * ldp;
+                df w = lane == 0 ? y[j] : df_f(0.f);
+                for (int r = j + 1 + lane; r < mr; r += 32) w = df_fma(x[r], y[r], w);
+                w = df_mul(df_group_sum(w, 32), tau);
+                if (lane == 0) y[j] = df_add(y[j], -w);
+                const df mw = -w;
+                for (int r = j + 1 + lane; r < mr; r += 32) y[r] = df_fma(mw, x[r], y[r]);
             }
         }
         __syncthreads();
@@ -239,7 +288,7 @@ __device__ QrShared carve(double *sm, int ld, int kmax) {
 }
 
 // grid = 2 * n: block 2s factors the U stack of update s, block 2s+1 its V stack.
-__global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws) {
+__global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws, int mixed) {
     extern __shared__ double sm[];
     const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
     const int *meta = ws.meta + (size_t) slot * META_INTS;
@@ -261,7 +310,35 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws) {
             s.Ps[e] = (c < nbp && r < mr) ? A[(j0 + r) + (size_t) (j0 + c) * lda] : 0.0;
         }
         __syncthreads();
-        factor_panel(s.Ps, s.ldp, mr, nbp, s.tau, s.red);
+        if (mixed) {
+            // Panel in float-float arithmetic after an exact power-of-two scaling (float range);
+            // the reflectors and tau are scale-free, R (on and above the diagonal) is scaled back.
+            __shared__ int s_emax;
+            if (threadIdx.x == 0) s_emax = 0;
+            __syncthreads();
+            int em = 0;
+            for (int e = threadIdx.x; e < nbp * s.ldp; e += blockDim.x) {
+                const int ef = (int) ((__double_as_longlong(s.Ps[e]) >> 52) & 0x7ff);
+                em = em > ef ? em : ef;
+            }
+            atomicMax(&s_emax, em);
+            __syncthreads();
+            const int eshift = s_emax ? s_emax - 1023 : 0;
+            const double down = __hiloint2double((1023 - eshift) << 20, 0);
+            const double up = __hiloint2double((1023 + eshift) << 20, 0);
+            df *Pd = reinterpret_cast<df *>(s.Ps);
+            for (int e = threadIdx.x; e < nbp * s.ldp; e += blockDim.x) Pd[e] = df(s.Ps[e] * down);
+            __syncthreads();
+            factor_panel_df(Pd, s.ldp, mr, nbp, s.tau, s.red);
+            for (int e = threadIdx.x; e < nbp * s.ldp; e += blockDim.x) {
+                const int c = e / s.ldp, r = e % s.ldp;
+                const double v = (double) Pd[e];
+                s.Ps[e] = r <= c ? v * up : v;
+            }
+            __syncthreads();
+        } else {
+            factor_panel(s.Ps, s.ldp, mr, nbp, s.tau, s.red);
+        }
         for (int e = threadIdx.x; e < nbp * mr; e += blockDim.x) {
             const int c = e / mr, r = e % mr;
             A[(j0 + r) + (size_t) (j0 + c) * lda] = s.Ps[(size_t) c * s.ldp + r];
@@ -327,10 +404,10 @@ size_t qr_smem_bytes(int ld, int kmax) {
     return sizeof(double) * ((size_t) NB * ldp + (size_t) NB * ldw + 2 * NB * NB + 64 + NB);
 }
 
-void launch_qr(Workspace ws, int n, cudaStream_t st) {
+void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st) {
     const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
     cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws);
+    qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws, mixed ? 1 : 0);
 }
 
 void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st) {

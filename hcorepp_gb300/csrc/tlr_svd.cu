@@ -13,6 +13,7 @@
 #include <cfloat>
 
 #include "internal.cuh"
+#include "df.cuh"
 
 namespace hcgb {
 
@@ -40,50 +41,6 @@ __device__ __forceinline__ T group_sum(T v, int G) {
 __device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
 __device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
 
-// Float-float ("double-float") arithmetic for the mixed form's Jacobi: a value is the unevaluated
-// sum h + l of two floats (|l| <= ulp(h) / 2), 48 significant bits, on the FP32 pipe (about 70x the
-// FP64 rate on this GPU).  Error-free transformations (Dekker / Knuth two-sum, FMA two-product)
-// with explicitly rounded intrinsics so that nothing is contracted or reassociated.
-struct df {
-    float h, l;
-    __device__ __forceinline__ df() {}
-    __device__ __forceinline__ df(double v) {
-        h = __double2float_rn(v);
-        l = __double2float_rn(v - (double) h);
-    }
-    __device__ __forceinline__ explicit operator double() const { return (double) h + (double) l; }
-};
-__device__ __forceinline__ df operator-(df a) {
-    df r;
-    r.h = -a.h;
-    r.l = -a.l;
-    return r;
-}
-// c + a * b
-__device__ __forceinline__ df df_fma(df a, df b, df c) {
-    const float p = __fmul_rn(a.h, b.h);
-    float e = __fmaf_rn(a.h, b.h, -p);
-    e = __fmaf_rn(a.h, b.l, e);
-    e = __fmaf_rn(a.l, b.h, e);
-    const float s = __fadd_rn(c.h, p);
-    const float bb = __fsub_rn(s, c.h);
-    float err = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-    err = __fadd_rn(err, __fadd_rn(c.l, e));
-    df r;
-    r.h = __fadd_rn(s, err);
-    r.l = __fsub_rn(err, __fsub_rn(r.h, s));
-    return r;
-}
-__device__ __forceinline__ df df_add(df a, df b) {
-    const float s = __fadd_rn(a.h, b.h);
-    const float bb = __fsub_rn(s, a.h);
-    float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
-    err = __fadd_rn(err, __fadd_rn(a.l, b.l));
-    df r;
-    r.h = __fadd_rn(s, err);
-    r.l = __fsub_rn(err, __fsub_rn(r.h, s));
-    return r;
-}
 // a * b + c in the Jacobi element type.
 __device__ __forceinline__ double tfma(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float tfma(float a, float b, float c) { return fmaf(a, b, c); }
@@ -91,13 +48,7 @@ __device__ __forceinline__ df tfma(df a, df b, df c) { return df_fma(a, b, c); }
 
 template <>
 __device__ __forceinline__ df group_sum<df>(df v, int G) {
-    for (int o = G >> 1; o > 0; o >>= 1) {
-        df w;
-        w.h = __shfl_xor_sync(0xffffffffu, v.h, o);
-        w.l = __shfl_xor_sync(0xffffffffu, v.l, o);
-        v = df_add(v, w);
-    }
-    return v;
+    return df_group_sum(v, G);
 }
 // Unit roundoff used for the noise floor of a Jacobi run in type T.
 template <typename T> __device__ __forceinline__ double unit_roundoff() { return DBL_EPSILON; }
@@ -313,34 +264,6 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
 // tangent is a float (any tangent gives an exact rotation once cos = 1/sqrt(1 + t^2) is formed to
 // float-float accuracy, which one Newton step on the float reciprocal square root does).
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ df df_mul(df a, df b) {
-    const float p = __fmul_rn(a.h, b.h);
-    float e = __fmaf_rn(a.h, b.h, -p);
-    e = __fmaf_rn(a.h, b.l, e);
-    e = __fmaf_rn(a.l, b.h, e);
-    df r;
-    r.h = __fadd_rn(p, e);
-    r.l = __fsub_rn(e, __fsub_rn(r.h, p));
-    return r;
-}
-__device__ __forceinline__ df df_f(float v) {
-    df r;
-    r.h = v;
-    r.l = 0.f;
-    return r;
-}
-// 1 / sqrt(q) for q >= 1 to float-float accuracy: two Newton steps r <- r + r (1 - q r^2) / 2 from
-// the float reciprocal square root (about 22 -> 44 -> 48 correct bits).
-__device__ __forceinline__ df df_rsqrt(df q) {
-    df r = df_f(rsqrtf(q.h));
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
-        const df res = df_add(df_f(1.f), -df_mul(q, df_mul(r, r)));  // 1 - q r^2, small
-        r = df_add(r, df_mul(df_mul(r, res), df_f(0.5f)));
-    }
-    return r;
-}
-
 template <int G, int RPL>
 __device__ int jacobi_sweep_df(df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, float tol, float tiny,
                                int n2) {
@@ -649,27 +572,6 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
         __syncthreads();
     }
     return rkeep;
-}
-
-// Float-float reciprocal and square root (one correction step each from the float result).
-__device__ __forceinline__ df df_div(df a, df b) {
-    const float q0 = __fdiv_rn(a.h, b.h);
-    const df r = df_add(a, -df_mul(df_f(q0), b));  // a - q0 b
-    const float q1 = __fdiv_rn(r.h, b.h);
-    df q;
-    q.h = __fadd_rn(q0, q1);
-    q.l = __fsub_rn(q1, __fsub_rn(q.h, q0));
-    return q;
-}
-__device__ __forceinline__ df df_sqrt(df v) {
-    if (v.h <= 0.f) return df_f(0.f);
-    const float s0 = sqrtf(v.h);
-    const df r = df_add(v, -df_mul(df_f(s0), df_f(s0)));  // v - s0^2
-    const float s1 = __fdiv_rn(r.h, 2.f * s0);
-    df q;
-    q.h = __fadd_rn(s0, s1);
-    q.l = __fsub_rn(s1, __fsub_rn(q.h, s0));
-    return q;
 }
 
 // Float-float version of qrcp_truncated (mixed form), on a matrix scaled so that its entries are
