@@ -354,6 +354,182 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws, int mixed)
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Mixed form of the stack QR: the whole stack is held as float-float values (scaled by a power of
+// two) while it is factored, so the panels, the compact-WY T and the trailing updates run on the
+// FP32 pipe; R and the reflectors are written back in double at the end (R scaled back, the
+// reflectors and tau are scale-free).
+// ---------------------------------------------------------------------------------------------
+__device__ void make_explicit_v_df(df *Ps, int ldp, int nbp) {
+    for (int e = threadIdx.x; e < NB * ldp; e += blockDim.x) {
+        const int c = e / ldp, r = e % ldp;
+        if (c >= nbp || r < c) Ps[e] = df_f(0.f);
+        else if (r == c) Ps[e] = df_f(1.f);
+    }
+}
+
+__device__ void build_t_df(const df *Ps, int ldp, int mr, int nbp, const double *tau_s, df *Ts, df *Gs) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) Ts[e] = df_f(0.f);
+    const int npairs = nbp * (nbp - 1) / 2;
+    for (int p = warp; p < npairs; p += nw) {
+        int i = 1, base = 0;
+        while (base + i <= p) {
+            base += i;
+            i++;
+        }
+        const int l = p - base;
+        const df *vl = Ps + (size_t) l * ldp, *vi = Ps + (size_t) i * ldp;
+        df sacc = df_f(0.f);
+        for (int r = i + lane; r < mr; r += 32) sacc = df_fma(vl[r], vi[r], sacc);
+        sacc = df_group_sum(sacc, 32);
+        if (lane == 0) Gs[l * NB + i] = sacc;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int j = lane;
+        for (int i = 0; i < nbp; i++) {
+            const df ti = df(tau_s[i]);
+            df v = df_f(0.f);
+            if (j < i) {
+                for (int l = j; l < i; l++) v = df_fma(Ts[j * NB + l], Gs[l * NB + i], v);
+                v = -df_mul(v, ti);
+            }
+            __syncwarp();
+            if (j < i) Ts[j * NB + i] = v;
+            if (j == i) Ts[i * NB + i] = ti;
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+}
+
+// X (mr x nt, ld ldx, float-float) <- (I - V op(T) V^T) X, columns in chunks of ldw.
+__device__ void apply_block_reflector_df(const df *Ps, int ldp, const df *Ts, bool trans_t, df *X, int ldx, int mr,
+                                         int nt, df *Ws, int ldw) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int c0 = 0; c0 < nt; c0 += ldw) {
+        const int ntc = nt - c0 < ldw ? nt - c0 : ldw;
+        df *Xc = X + (size_t) c0 * ldx;
+        // A: W = V^T X, a warp per column, lanes over rows
+        for (int c = warp; c < ntc; c += nw) {
+            df acc[NB];
+#pragma unroll
+            for (int i = 0; i < NB; i++) acc[i] = df_f(0.f);
+            const df *xc = Xc + (size_t) c * ldx;
+            for (int r = lane; r < mr; r += 32) {
+                const df xv = xc[r];
+#pragma unroll
+                for (int i = 0; i < NB; i++) acc[i] = df_fma(Ps[(size_t) i * ldp + r], xv, acc[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < NB; i++) {
+                const df v = df_group_sum(acc[i], 32);
+                if (lane == 0) Ws[i * ldw + c] = v;
+            }
+        }
+        __syncthreads();
+        // B: W <- -op(T) W, a thread per column
+        for (int c = threadIdx.x; c < ntc; c += blockDim.x) {
+            df w[NB], o[NB];
+#pragma unroll
+            for (int i = 0; i < NB; i++) w[i] = Ws[i * ldw + c];
+#pragma unroll
+            for (int i = 0; i < NB; i++) {
+                df sacc = df_f(0.f);
+                if (trans_t) {
+#pragma unroll
+                    for (int l = 0; l <= i; l++) sacc = df_fma(Ts[l * NB + i], w[l], sacc);
+                } else {
+#pragma unroll
+                    for (int l = i; l < NB; l++) sacc = df_fma(Ts[i * NB + l], w[l], sacc);
+                }
+                o[i] = -sacc;
+            }
+#pragma unroll
+            for (int i = 0; i < NB; i++) Ws[i * ldw + c] = o[i];
+        }
+        __syncthreads();
+        // C: X += V W, a thread per element (rows fastest: coalesced)
+        for (int e = threadIdx.x; e < mr * ntc; e += blockDim.x) {
+            const int r = e % mr, c = e / mr;
+            df x = Xc[r + (size_t) c * ldx];
+#pragma unroll
+            for (int i = 0; i < NB; i++) x = df_fma(Ps[(size_t) i * ldp + r], Ws[i * ldw + c], x);
+            Xc[r + (size_t) c * ldx] = x;
+        }
+        __syncthreads();
+    }
+}
+
+// grid = 2 * n, as qr_kernel; the mixed form.
+__global__ void __launch_bounds__(QR_THREADS) qr_kernel_df(Workspace ws) {
+    extern __shared__ double sm[];
+    const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
+    const int *meta = ws.meta + (size_t) slot * META_INTS;
+    if (meta[META_STATUS] != HCGB_OK || !meta[META_CKIND]) return;
+    const int k = meta[META_K];
+    const int m = side ? meta[META_N] : meta[META_M];
+    double *base = ws.slot(slot);
+    double *A = base + (side ? ws.off_vstack : ws.off_ustack);
+    double *tau = base + (side ? ws.off_tauv : ws.off_tauu);
+    double *Tg = base + (side ? ws.off_tv : ws.off_tu);
+    const int lda = ws.ld;
+    QrShared s = carve(sm, ws.ld, ws.kmax);
+    df *Psd = reinterpret_cast<df *>(s.Ps), *Wsd = reinterpret_cast<df *>(s.Ws);
+    df *Tsd = reinterpret_cast<df *>(s.Ts), *Gsd = reinterpret_cast<df *>(s.Gs);
+    df *Ad = reinterpret_cast<df *>(A);
+    // 1. the stack as float-float values of A * 2^-eshift (entries below 2)
+    __shared__ int s_emax;
+    if (threadIdx.x == 0) s_emax = 0;
+    __syncthreads();
+    int em = 0;
+    for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
+        const int ef = (int) ((__double_as_longlong(A[(e % m) + (size_t) (e / m) * lda]) >> 52) & 0x7ff);
+        em = em > ef ? em : ef;
+    }
+    atomicMax(&s_emax, em);
+    __syncthreads();
+    const int eshift = s_emax ? s_emax - 1023 : 0;
+    const double down = __hiloint2double((1023 - eshift) << 20, 0), up = __hiloint2double((1023 + eshift) << 20, 0);
+    for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
+        const size_t o = (e % m) + (size_t) (e / m) * lda;
+        Ad[o] = df(A[o] * down);
+    }
+    __syncthreads();
+    // 2. panels
+    const int kk = m < k ? m : k;
+    for (int j0 = 0; j0 < kk; j0 += NB) {
+        const int nbp = (kk - j0) < NB ? (kk - j0) : NB;
+        const int mr = m - j0;
+        for (int e = threadIdx.x; e < NB * s.ldp; e += blockDim.x) {
+            const int c = e / s.ldp, r = e % s.ldp;
+            Psd[e] = (c < nbp && r < mr) ? Ad[(j0 + r) + (size_t) (j0 + c) * lda] : df_f(0.f);
+        }
+        __syncthreads();
+        factor_panel_df(Psd, s.ldp, mr, nbp, s.tau, s.red);
+        for (int e = threadIdx.x; e < nbp * mr; e += blockDim.x) {
+            const int c = e / mr, r = e % mr;
+            Ad[(j0 + r) + (size_t) (j0 + c) * lda] = Psd[(size_t) c * s.ldp + r];
+        }
+        if (threadIdx.x < nbp) tau[j0 + threadIdx.x] = s.tau[threadIdx.x];
+        __syncthreads();
+        make_explicit_v_df(Psd, s.ldp, nbp);
+        __syncthreads();
+        build_t_df(Psd, s.ldp, mr, nbp, s.tau, Tsd, Gsd);
+        for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) Tg[(size_t) (j0 / NB) * NB * NB + e] = (double) Tsd[e];
+        const int c0 = j0 + nbp;
+        apply_block_reflector_df(Psd, s.ldp, Tsd, true, Ad + j0 + (size_t) c0 * lda, lda, mr, k - c0, Wsd, s.ldw);
+    }
+    // 3. back to double: R (on and above the diagonal) scaled back, reflectors as they are
+    for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
+        const int r = e % m, c = e / m;
+        const size_t o = r + (size_t) c * lda;
+        const double v = (double) Ad[o];
+        A[o] = r <= c ? v * up : v;
+    }
+}
+
 // grid = 2 * n: X <- Q X for the U side (X = the C tile's U, m x r) and the V side (X = XV, n x r).
 __global__ void __launch_bounds__(QR_THREADS) apply_q_kernel(const DevUpdate *ups, Workspace ws) {
     extern __shared__ double sm[];
@@ -407,7 +583,12 @@ size_t qr_smem_bytes(int ld, int kmax) {
 void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st) {
     const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
     cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws, mixed ? 1 : 0);
+    if (mixed) {
+        cudaFuncSetAttribute(qr_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+        qr_kernel_df<<<2 * n, QR_THREADS, smem, st>>>(ws);
+    } else {
+        qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws, 0);
+    }
 }
 
 void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st) {
