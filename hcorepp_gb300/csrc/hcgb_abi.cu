@@ -230,7 +230,7 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
             launch_wy_solve(n, ws, st);
             launch_gemm_jobs(djobs + 4 * (size_t) n, 2 * n, sched, st);
         }
-        launch_apply_q(dups, n, ws, st);  // the sides not applied in WY form (plan_kernel zeroes META_WY)
+        launch_apply_q(dups, n, ws, p.mode == 1, st);  // the sides not applied in WY form (plan_kernel zeroes META_WY)
         cnt[HCGB_STAGE_APPLY_Q]++;
     }
     mark(HCGB_STAGE_FINALIZE);

@@ -162,7 +162,7 @@ void launch_plan_wy(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob
 void launch_wy_solve(int n, Workspace ws, cudaStream_t st);
 void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st);
 void launch_core_svd(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st);
-void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st);
+void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, bool mixed, cudaStream_t st);
 void launch_finalize(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st);
 // FP64 throughput probes (TFLOP/s): tensor-core DMMA and SIMT DFMA.
 int measure_fp64_peak(cudaStream_t st, double *dmma_tflops, double *dfma_tflops);

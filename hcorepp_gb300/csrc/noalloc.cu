@@ -162,7 +162,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     if (ck) {
         launch_qr(ws, 1, prm.mode == 1, st);
         launch_core_svd(dup, 1, ws, prm, st);
-        launch_apply_q(dup, 1, ws, st);
+        launch_apply_q(dup, 1, ws, prm.mode == 1, st);
     }
     launch_finalize(dup, 1, ws, info_dev, st);
     return cudaGetLastError() == cudaSuccess ? HCGB_OK : HCGB_CUDA_ERROR;

@@ -573,6 +573,73 @@ __global__ void __launch_bounds__(QR_THREADS) apply_q_kernel(const DevUpdate *up
     }
 }
 
+// grid = 2 * n, as apply_q_kernel; the mixed form: X is held as float-float values (scaled by a
+// power of two) while the panels are applied, then written back in double.
+__global__ void __launch_bounds__(QR_THREADS) apply_q_kernel_df(const DevUpdate *ups, Workspace ws) {
+    extern __shared__ double sm[];
+    const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
+    const int *meta = ws.meta + (size_t) slot * META_INTS;
+    const int st = meta[META_STATUS];
+    if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;
+    if (meta[META_WY] & (1 << side)) return;  // applied in WY form
+    const int k = meta[META_K];
+    const int m = side ? meta[META_N] : meta[META_M];
+    const int r = meta[META_NEWRANK];
+    double *base = ws.slot(slot);
+    const double *A = base + (side ? ws.off_vstack : ws.off_ustack);
+    const double *Tg = base + (side ? ws.off_tv : ws.off_tu);
+    double *X;
+    int ldx;
+    if (side == 0) {
+        X = ups[slot].c.data;
+        ldx = ups[slot].c.rows;
+    } else {
+        X = base + ws.off_xv;
+        ldx = ws.ld;
+    }
+    const int lda = ws.ld;
+    QrShared s = carve(sm, ws.ld, ws.kmax);
+    df *Psd = reinterpret_cast<df *>(s.Ps), *Wsd = reinterpret_cast<df *>(s.Ws), *Tsd = reinterpret_cast<df *>(s.Ts);
+    df *Xd = reinterpret_cast<df *>(X);
+    __shared__ int s_emax;
+    if (threadIdx.x == 0) s_emax = 0;
+    __syncthreads();
+    int em = 0;
+    for (int e = threadIdx.x; e < m * r; e += blockDim.x) {
+        const int ef = (int) ((__double_as_longlong(X[(e % m) + (size_t) (e / m) * ldx]) >> 52) & 0x7ff);
+        em = em > ef ? em : ef;
+    }
+    atomicMax(&s_emax, em);
+    __syncthreads();
+    const int eshift = s_emax ? s_emax - 1023 : 0;
+    const double down = __hiloint2double((1023 - eshift) << 20, 0), up = __hiloint2double((1023 + eshift) << 20, 0);
+    for (int e = threadIdx.x; e < m * r; e += blockDim.x) {
+        const size_t o = (e % m) + (size_t) (e / m) * ldx;
+        Xd[o] = df(X[o] * down);
+    }
+    __syncthreads();
+    const int kk = m < k ? m : k;
+    const int npan = (kk + NB - 1) / NB;
+    for (int p = npan - 1; p >= 0; p--) {
+        const int j0 = p * NB;
+        const int nbp = (kk - j0) < NB ? (kk - j0) : NB;
+        const int mr = m - j0;
+        for (int e = threadIdx.x; e < NB * s.ldp; e += blockDim.x) {
+            const int c = e / s.ldp, rr = e % s.ldp;
+            double v = 0.0;
+            if (c < nbp && rr < mr) v = rr > c ? A[(j0 + rr) + (size_t) (j0 + c) * lda] : (rr == c ? 1.0 : 0.0);
+            Psd[e] = df(v);
+        }
+        for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) Tsd[e] = df(Tg[(size_t) p * NB * NB + e]);
+        __syncthreads();
+        apply_block_reflector_df(Psd, s.ldp, Tsd, false, Xd + j0, ldx, mr, r, Wsd, s.ldw);
+    }
+    for (int e = threadIdx.x; e < m * r; e += blockDim.x) {
+        const size_t o = (e % m) + (size_t) (e / m) * ldx;
+        X[o] = (double) Xd[o] * up;
+    }
+}
+
 }  // namespace
 
 size_t qr_smem_bytes(int ld, int kmax) {
@@ -591,7 +658,13 @@ void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st) {
     }
 }
 
-void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st) {
+void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, bool mixed, cudaStream_t st) {
+    if (mixed) {
+        const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
+        cudaFuncSetAttribute(apply_q_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+        apply_q_kernel_df<<<2 * n, QR_THREADS, smem, st>>>(ups, ws);
+        return;
+    }
     const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
     cudaFuncSetAttribute(apply_q_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     apply_q_kernel<<<2 * n, QR_THREADS, smem, st>>>(ups, ws);
