@@ -221,7 +221,7 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     }
     mark(HCGB_STAGE_APPLY_Q);
     if (sh.any_compressed_c) {
-        if (p.oz && ws.off_w) {
+        if (p.oz && p.mode != 1 && ws.off_w) {  // the mixed form's float-float panels are faster
             // Sides with >= WY_MIN_REFLECTORS reflectors in full WY form: the Grams, Y = V^T X and
             // X -= V W are products (tensor-core eligible), only the small triangular solve stays on
             // the FP64 pipe.  The others keep the panel-wise kernel.

@@ -156,7 +156,8 @@ constexpr int SCHED_INTS_PER_UPDATE = 10;  // >= (2 * 4n + 2) / n: one WY launch
 // Q application in full WY form (Q = I - V T V^T, T^-1 = striu(V^T V) + diag(1/tau)): jobs for
 // the Grams, Y = V^T X and X -= V W, then the triangular solve T^-1 W = Y.  Used for the sides
 // with at least WY_MIN_REFLECTORS reflectors (their products run on the tensor cores); the
-// others keep the panel-wise apply_q_kernel, which skips the WY sides.
+// others keep the panel-wise apply_q_kernel, which skips the WY sides.  Plain form only: the mixed
+// form's float-float panels are faster than either.
 constexpr int WY_MIN_REFLECTORS = 48;
 void launch_plan_wy(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob *jobs, cudaStream_t st);
 void launch_wy_solve(int n, Workspace ws, cudaStream_t st);
