@@ -1,6 +1,6 @@
 """Tile-Cholesky throughput and accuracy on one GPU (hcgb_tile_cholesky).
 
-  python -m hcorepp_gb300.cholesky_bench [--n 16384] [--nb 1024] [--steps 1] [--warmup 1]
+  python -m hcorepp_gb300.cholesky_bench [--n 16384] [--nb 1024] [--steps 1] [--warmup 1] [--mode mixed]
 
 Matrix: n points uniform in [0,1]^3 (seeded), Morton-sorted; a_ij = exp(-|x_i - x_j| / 0.2) with
 1e-2 added to the diagonal (SPD).  Diagonal tiles dense, off-diagonal tiles compressed on the GPU
@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--mode", choices=["plain", "mixed"], default="mixed",
+                    help="recompression arithmetic of the trailing updates (FP64 or float-float)")
     return ap.parse_args()
 
 
@@ -92,7 +94,8 @@ def main():
     build_s = time.time() - t0
     pristine_arena, pristine_ranks = tm.arena.clone(), tm.ranks.clone()
     in_ranks = tm.ranks.cpu().numpy()
-    params = T.CompressionParameters(args.accuracy, truncated_svd=True)
+    params = T.CompressionParameters(args.accuracy, truncated_svd=True,
+                                     mode=L.MIXED if args.mode == "mixed" else L.PLAIN_FP64)
     n_updates = nt * (nt * nt - 1) // 6
     info = T.info_buffer(max(n_updates, 1))
     ctx = T.run_context()
@@ -132,7 +135,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"tile_cholesky_n{args.n}_nb{args.nb}", "n": args.n, "nb": args.nb, "tiles": nt,
                    "points_dim": args.d, "length_scale": args.ell, "diag_shift": args.shift,
-                   "accuracy": args.accuracy, "trailing_updates": n_updates},
+                   "accuracy": args.accuracy, "trailing_updates": n_updates, "mode": args.mode},
         "residual_llt": fact_res, "solve_residual": solve_res,
         "input_rank_mean": float(off.mean()) if off.size else 0.0,
         "input_rank_clamped_frac": float((off >= tm.max_rank).mean()) if off.size else 0.0,

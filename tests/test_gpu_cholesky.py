@@ -110,7 +110,8 @@ def _chol_pair(T, nb, rank, rng, max_rank):
 
 
 @pytest.mark.parametrize("nb,ra,rb,rc", [(60, 7, 9, 5), (96, 20, 12, 0), (128, 30, 30, 30)])
-def test_gemm_cholesky_branch_vs_oracle(T, nb, ra, rb, rc):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_gemm_cholesky_branch_vs_oracle(T, nb, ra, rb, rc, mode):
     """Gemm(-1, A, NoTrans, B, Trans, 0.5, C, aCholesky = true): compressed_vt operands through
     hcgb_tile_gemm against the oracle's restatement (pinned to HCore++'s own branch)."""
     rng = np.random.default_rng(nb + ra)
@@ -122,8 +123,8 @@ def test_gemm_cholesky_branch_vs_oracle(T, nb, ra, rb, rc):
     params = O.CompressionParameters(1e-8, truncated_svd=True)
     O.hcore_gemm_cholesky(-1.0, oa, ob, 0.5, oc, params)
     from hcorepp_gb300 import _lib as L
-    T.HCore.Gemm(-1.0, ga, L.NOTRANS, gb, L.TRANS, 0.5, gc, T.CompressionParameters(1e-8, truncated_svd=True),
-                 cholesky=True)
+    T.HCore.Gemm(-1.0, ga, L.NOTRANS, gb, L.TRANS, 0.5, gc,
+                 T.CompressionParameters(1e-8, truncated_svd=True, mode=mode), cholesky=True)
     assert abs(gc.rank - oc.rank) <= 1
     got = gc.u() @ gc.w().T
     assert rel_fro(got, want) <= 2 * max(rel_fro(oc.to_dense(), want), 1e-8)
@@ -184,7 +185,8 @@ def test_vt_layout_is_bitwise_equal_to_plain(T):
                 np.testing.assert_array_equal(q.v(), p.v())
 
 
-def test_tile_cholesky_residual(T):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_tile_cholesky_residual(T, mode):
     """Tile Cholesky of an SPD exponential-kernel matrix (2-D points, length scale 0.1, 4 x 4 tiles
     of 256, dense diagonal tiles, off-diagonal tiles compressed at 1e-8 with the reference's
     capacity nb/3, Cholesky-flow layout): residual ||L L^T - A||_F / ||A||_F and agreement with the
@@ -209,7 +211,7 @@ def test_tile_cholesky_residual(T):
                 t = compressed_from_dense(blk, acc)
                 tm.set_tile(i, j, u=t.u, v=t.v)
                 og[i][j] = O.CholeskyTile(t.u, t.v.T, t.max_rank)
-    params = T.CompressionParameters(acc, truncated_svd=True)
+    params = T.CompressionParameters(acc, truncated_svd=True, mode=mode)
     tm2 = T.TileMatrix(nt, nt, nb, kinds, nb // 3, vt=True)
     tm2.arena.copy_(tm.arena)
     tm2.ranks.copy_(tm.ranks)

@@ -81,7 +81,8 @@ def _make(kind, d, acc):
 
 @pytest.mark.parametrize("combo", COMBOS)
 @pytest.mark.parametrize("nb", [96, 256])
-def test_single_update_vs_oracle(T, combo, nb):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_single_update_vs_oracle(T, combo, nb, mode):
     from hcorepp_gb300.problems import KernelMatrix
     acc = 1e-8
     km = KernelMatrix(4 * nb, nb, 2, 0.1, 1)
@@ -93,7 +94,7 @@ def test_single_update_vs_oracle(T, combo, nb):
     exact = alpha * oa.to_dense() @ ob.to_dense() + beta * oc.to_dense()
     params = O.CompressionParameters(acc, truncated_svd=True)
     info = O.hcore_gemm(alpha, oa, ob, beta, oc, params)
-    T.HCore.Gemm(alpha, ga, 0, gb, 0, beta, gc, T.CompressionParameters(acc, truncated_svd=True))
+    T.HCore.Gemm(alpha, ga, 0, gb, 0, beta, gc, T.CompressionParameters(acc, truncated_svd=True, mode=mode))
     e_o = rel_fro(oc.to_dense(), exact)
     e_g = rel_fro(gc.to_dense(), exact)
     assert e_g <= 2 * max(e_o, acc), (e_g, e_o)
@@ -104,7 +105,8 @@ def test_single_update_vs_oracle(T, combo, nb):
 
 
 @pytest.mark.parametrize("accuracy,truncated", [(1e-4, False), (1e-6, True), (1e-10, True)])
-def test_rank_rule_modes(T, accuracy, truncated):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_rank_rule_modes(T, accuracy, truncated, mode):
     rng = np.random.default_rng(7)
     m = n = 128
     a = random_lowrank(m, n, 40, rng, 0.6)
@@ -114,25 +116,27 @@ def test_rank_rule_modes(T, accuracy, truncated):
     oa, ob, oc = (compressed_from_dense(x, 1e-14, True, max_rank=60) for x in (a, b, c))
     ga, gb, gc = (_gpu_tile(T, t) for t in (oa, ob, oc))
     O.hcore_gemm(1.0, oa, ob, 1.0, oc, p)
-    T.HCore.Gemm(1.0, ga, 0, gb, 0, 1.0, gc, T.CompressionParameters(accuracy, truncated_svd=truncated))
+    T.HCore.Gemm(1.0, ga, 0, gb, 0, 1.0, gc, T.CompressionParameters(accuracy, truncated_svd=truncated, mode=mode))
     assert abs(gc.rank - oc.rank) <= 1
     exact = a @ b + c
     assert rel_fro(gc.to_dense(), exact) <= 2 * max(rel_fro(oc.to_dense(), exact), 1e-15)
 
 
-def test_fixed_rank(T):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_fixed_rank(T, mode):
     rng = np.random.default_rng(3)
     a, b, c = (random_lowrank(64, 64, 20, rng, 0.7) for _ in range(3))
     oa, ob, oc = (compressed_from_dense(x, 1e-14, True, max_rank=30) for x in (a, b, c))
     ga, gb, gc = (_gpu_tile(T, t) for t in (oa, ob, oc))
     p = O.CompressionParameters(1e-8, fixed_rank=7)
     O.hcore_gemm(1.0, oa, ob, 1.0, oc, p)
-    T.HCore.Gemm(1.0, ga, 0, gb, 0, 1.0, gc, T.CompressionParameters(1e-8, fixed_rank=7))
+    T.HCore.Gemm(1.0, ga, 0, gb, 0, 1.0, gc, T.CompressionParameters(1e-8, fixed_rank=7, mode=mode))
     assert gc.rank == oc.rank == 7
     np.testing.assert_allclose(gc.to_dense(), oc.to_dense(), atol=1e-10 * np.abs(oc.to_dense()).max())
 
 
-def test_rank_clamp_at_capacity(T):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_rank_clamp_at_capacity(T, mode):
     # Compressed.cpp:526-527: the new rank never exceeds the tile's max rank.
     rng = np.random.default_rng(11)
     a, b, c = (random_lowrank(64, 64, 30, rng, 0.9) for _ in range(3))
@@ -142,25 +146,26 @@ def test_rank_clamp_at_capacity(T):
     ga, gb, gc = (_gpu_tile(T, t) for t in (oa, ob, oc))
     p = O.CompressionParameters(1e-12, truncated_svd=True)
     O.hcore_gemm(1.0, oa, ob, 1.0, oc, p)
-    T.HCore.Gemm(1.0, ga, 0, gb, 0, 1.0, gc, T.CompressionParameters(1e-12, truncated_svd=True))
+    T.HCore.Gemm(1.0, ga, 0, gb, 0, 1.0, gc, T.CompressionParameters(1e-12, truncated_svd=True, mode=mode))
     assert gc.rank == oc.rank == 12
     exact_o = oc.to_dense()
     assert rel_fro(gc.to_dense(), exact_o) < 1e-6
 
 
-def test_trans_operands(T):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_trans_operands(T, mode):
     # op(A) = A^T, op(B) = B^T (HCore.cpp:73-110 swaps the factor holders); C has room for the full rank.
     rng = np.random.default_rng(5)
     a, b, c = (random_lowrank(48, 48, 12, rng, 0.5) for _ in range(3))
     oa, ob = (compressed_from_dense(x, 1e-14, True) for x in (a, b))
     oc = compressed_from_dense(c, 1e-14, True, max_rank=40)
     ga, gb, gc = (_gpu_tile(T, t) for t in (oa, ob, oc))
-    T.HCore.Gemm(1.0, ga, 1, gb, 1, 1.0, gc, T.CompressionParameters(1e-12, truncated_svd=True))
+    T.HCore.Gemm(1.0, ga, 1, gb, 1, 1.0, gc, T.CompressionParameters(1e-12, truncated_svd=True, mode=mode))
     exact = oa.to_dense().T @ ob.to_dense().T + oc.to_dense()
     assert rel_fro(gc.to_dense(), exact) < 1e-10
     gd = T.DenseTile(48, 48, a)
     gc2 = _gpu_tile(T, compressed_from_dense(c, 1e-14, True, max_rank=40))
-    T.HCore.Gemm(2.0, gd, 1, gb, 0, 1.0, gc2, T.CompressionParameters(1e-12, truncated_svd=True))
+    T.HCore.Gemm(2.0, gd, 1, gb, 0, 1.0, gc2, T.CompressionParameters(1e-12, truncated_svd=True, mode=mode))
     exact2 = 2.0 * a.T @ ob.to_dense() + oc.to_dense()
     assert rel_fro(gc2.to_dense(), exact2) < 1e-10
 
@@ -276,7 +281,8 @@ def test_mixed_mode_vs_oracle(T, combo):
 
 
 @pytest.mark.parametrize("truncated,acc", [(True, 1e-8), (False, 1e-6)])
-def test_compress_tile_vs_oracle(T, truncated, acc):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_compress_tile_vs_oracle(T, truncated, acc, mode):
     """GPU dense -> compressed construction vs the reference's constructor restated in the oracle
     (Compressed.cpp:75-146): rank +-1, reconstruction error at the oracle's level."""
     from hcorepp_gb300.problems import KernelMatrix
@@ -284,7 +290,7 @@ def test_compress_tile_vs_oracle(T, truncated, acc):
     for (i, j) in [(0, 1), (0, 3), (2, 2)]:
         d = km.tile(i, j)
         o = O.CompressedTile.from_dense(d, O.CompressionParameters(acc, truncated_svd=truncated))
-        g = T.CompressedTile.from_dense(d, T.CompressionParameters(acc, truncated_svd=truncated))
+        g = T.CompressedTile.from_dense(d, T.CompressionParameters(acc, truncated_svd=truncated, mode=mode))
         assert g.max_rank == o.max_rank == 256 // 3
         assert abs(g.rank - o.rank) <= 1, (i, j, g.rank, o.rank)
         e_o = rel_fro(o.to_dense(), d)
