@@ -288,7 +288,7 @@ __device__ QrShared carve(double *sm, int ld, int kmax) {
 }
 
 // grid = 2 * n: block 2s factors the U stack of update s, block 2s+1 its V stack.
-__global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws, int mixed) {
+__global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws) {
     extern __shared__ double sm[];
     const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
     const int *meta = ws.meta + (size_t) slot * META_INTS;
@@ -310,35 +310,7 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws, int mixed)
             s.Ps[e] = (c < nbp && r < mr) ? A[(j0 + r) + (size_t) (j0 + c) * lda] : 0.0;
         }
         __syncthreads();
-        if (mixed) {
-            // Panel in float-float arithmetic after an exact power-of-two scaling (float range);
-            // the reflectors and tau are scale-free, R (on and above the diagonal) is scaled back.
-            __shared__ int s_emax;
-            if (threadIdx.x == 0) s_emax = 0;
-            __syncthreads();
-            int em = 0;
-            for (int e = threadIdx.x; e < nbp * s.ldp; e += blockDim.x) {
-                const int ef = (int) ((__double_as_longlong(s.Ps[e]) >> 52) & 0x7ff);
-                em = em > ef ? em : ef;
-            }
-            atomicMax(&s_emax, em);
-            __syncthreads();
-            const int eshift = s_emax ? s_emax - 1023 : 0;
-            const double down = __hiloint2double((1023 - eshift) << 20, 0);
-            const double up = __hiloint2double((1023 + eshift) << 20, 0);
-            df *Pd = reinterpret_cast<df *>(s.Ps);
-            for (int e = threadIdx.x; e < nbp * s.ldp; e += blockDim.x) Pd[e] = df(s.Ps[e] * down);
-            __syncthreads();
-            factor_panel_df(Pd, s.ldp, mr, nbp, s.tau, s.red);
-            for (int e = threadIdx.x; e < nbp * s.ldp; e += blockDim.x) {
-                const int c = e / s.ldp, r = e % s.ldp;
-                const double v = (double) Pd[e];
-                s.Ps[e] = r <= c ? v * up : v;
-            }
-            __syncthreads();
-        } else {
-            factor_panel(s.Ps, s.ldp, mr, nbp, s.tau, s.red);
-        }
+        factor_panel(s.Ps, s.ldp, mr, nbp, s.tau, s.red);
         for (int e = threadIdx.x; e < nbp * mr; e += blockDim.x) {
             const int c = e / mr, r = e % mr;
             A[(j0 + r) + (size_t) (j0 + c) * lda] = s.Ps[(size_t) c * s.ldp + r];
@@ -649,12 +621,12 @@ size_t qr_smem_bytes(int ld, int kmax) {
 
 void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st) {
     const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
-    cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (mixed) {
         cudaFuncSetAttribute(qr_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
         qr_kernel_df<<<2 * n, QR_THREADS, smem, st>>>(ws);
     } else {
-        qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws, 0);
+        cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+        qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws);
     }
 }
 
