@@ -36,6 +36,18 @@ __device__ __forceinline__ void dmma(double &d0, double &d1, double a, double b)
                  : "d"(a), "d"(b));
 }
 
+// A set of NTH threads (whole warps) of one CTA that works on one update together: the thread's
+// index in the team and the named barrier its members synchronise on (bar.sync id, NTH), so that
+// two teams of one CTA never wait for each other.
+template <int NTH>
+struct Team {
+    static constexpr int nth = NTH;
+    int tid, bar;
+    __device__ __forceinline__ int warp() const { return tid >> 5; }
+    __device__ __forceinline__ static constexpr int nw() { return NTH >> 5; }
+    __device__ __forceinline__ void sync() const { asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(NTH) : "memory"); }
+};
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -146,7 +158,8 @@ struct Params {
 void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p, GemmJob *jobs,
                  cudaStream_t st);
 void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, cudaStream_t st);
-// ws.order <- updates sorted by decreasing stack width k (ties by index); needs ws.order != nullptr.
+// ws.order <- updates sorted by decreasing stack width k (0 for a dense C; ties by index); needs
+// ws.order != nullptr.  The key ignores the status, so it cannot change while the heavy stages run.
 void launch_order(int n, Workspace ws, cudaStream_t st);
 // Batched products: sched = device scratch of 2 * njobs + 2 ints (tile prefix sums), njobs <= 4096.
 void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t st);

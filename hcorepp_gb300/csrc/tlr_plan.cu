@@ -413,11 +413,11 @@ __global__ void __launch_bounds__(256) ddc_finalize_kernel(const DevUpdate *ups,
 __global__ void __launch_bounds__(1024) order_kernel(int n, Workspace ws) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int *mi = ws.meta + (size_t) i * META_INTS;
-        const int ki = (mi[META_STATUS] == HCGB_OK && mi[META_CKIND]) ? mi[META_K] : 0;
+        const int ki = mi[META_CKIND] ? mi[META_K] : 0;
         int pos = 0;
         for (int j = 0; j < n; j++) {
             const int *mj = ws.meta + (size_t) j * META_INTS;
-            const int kj = (mj[META_STATUS] == HCGB_OK && mj[META_CKIND]) ? mj[META_K] : 0;
+            const int kj = mj[META_CKIND] ? mj[META_K] : 0;
             pos += (kj > ki) || (kj == ki && j < i);
         }
         ws.order[pos] = i;

@@ -19,7 +19,9 @@ namespace hcgb {
 
 namespace {
 
-constexpr int SVD_THREADS = 256;
+constexpr int SVD_THREADS = 512;
+constexpr int SVD_RED_DOUBLES = 64, SVD_REDI_INTS = 128;  // reduction area (up to 32 warps)
+constexpr int SVD_AUX_FIXED = 1 + SVD_RED_DOUBLES + SVD_REDI_INTS / 2;  // aux = 6 kmax + this
 
 __device__ __forceinline__ void jacobi_pair(int t, int pp, int n2, int &i, int &j) {
     const int nm1 = n2 - 1;
@@ -84,10 +86,10 @@ __device__ __forceinline__ float jacobi_tangent(double a, double b, double c) {
 // becomes x_i' = x_i - t (d_j / d_i) x_j, x_j' = x_j + t (d_i / d_j) x_i, d' = cos d: one FMA per
 // element instead of a multiply and an FMA.  d and 1/d live in dsc[0..) and dsc[dstride..);
 // the caller folds them back into the columns at the start of every sweep.
-template <typename T, int G, int RPL, bool ACC>
-__device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, double tol2, double tiny, int n2,
+template <typename T, int G, int RPL, bool ACC, class TM>
+__device__ int jacobi_sweep(const TM &tm, T *X, int ldx, int rows, int ncols, double *nrm, double tol2, double tiny, int n2,
                             T *J, int ldj, double *dsc, int dstride) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     constexpr int PPW = 32 / G;
     const int gl = lane % G, grp = lane / G;
     const int npairs = n2 / 2;
@@ -185,17 +187,17 @@ __device__ int jacobi_sweep(T *X, int ldx, int rows, int ncols, double *nrm, dou
                 }
             }
         }
-        __syncthreads();
+        tm.sync();
     }
     return rotations;
 }
 
 // Jacobi iteration on X: exact squared column norms at the start of every sweep, then sweeps
 // until no pair rotates (or max_sweeps).
-template <typename T, int G, int RPL, bool ACC>
-__device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax, int *sweeps_out,
+template <typename T, int G, int RPL, bool ACC, class TM>
+__device__ void jacobi(const TM &tm, T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax, int *sweeps_out,
                        bool *converged_out, double tol, int max_sweeps, T *J, int ldj, double *dsc, int dstride) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     const double tol2 = tol * tol;
     // Noise floor from double precision also for single-precision sweeps: X is graded (each column
     // accurate relative to its own norm), so small columns are data, not rounding noise.
@@ -204,8 +206,8 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
     int sweeps = 0;
     bool converged = ncols < 2;
     if (!ACC) {
-        for (int j = threadIdx.x; j < ncols; j += blockDim.x) dsc[j] = dsc[dstride + j] = 1.0;
-        __syncthreads();
+        for (int j = tm.tid; j < ncols; j += tm.nth) dsc[j] = dsc[dstride + j] = 1.0;
+        tm.sync();
     }
     // Exact squared norms; the scales d of the previous sweep are folded into the columns.
     auto fold_and_norms = [&](double &amax) {
@@ -230,27 +232,27 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
         }
     };
     while (!converged && sweeps < max_sweeps) {
-        if (threadIdx.x == 0) {
+        if (tm.tid == 0) {
             *s_rot = 0;
             *s_amax = 0.0;
         }
-        __syncthreads();
+        tm.sync();
         double amax = 0.0;
         fold_and_norms(amax);
         if (lane == 0) atomicMax(reinterpret_cast<unsigned long long *>(s_amax), __double_as_longlong(amax));
-        __syncthreads();
+        tm.sync();
         const double tiny = *s_amax * noise * noise;
-        const int rot = jacobi_sweep<T, G, RPL, ACC>(X, ldx, rows, ncols, nrm, tol2, tiny, n2, J, ldj, dsc, dstride);
+        const int rot = jacobi_sweep<T, G, RPL, ACC>(tm, X, ldx, rows, ncols, nrm, tol2, tiny, n2, J, ldj, dsc, dstride);
         if (rot) atomicAdd(s_rot, rot);
-        __syncthreads();
+        tm.sync();
         sweeps++;
         converged = (*s_rot == 0);
-        __syncthreads();
+        tm.sync();
     }
     if (!ACC) {  // a sweep limit can leave scales unfolded
         double amax = 0.0;
         fold_and_norms(amax);
-        __syncthreads();
+        tm.sync();
     }
     *sweeps_out = sweeps;
     *converged_out = converged;
@@ -264,10 +266,10 @@ __device__ void jacobi(T *X, int ldx, int rows, int ncols, double *nrm, int *s_r
 // tangent is a float (any tangent gives an exact rotation once cos = 1/sqrt(1 + t^2) is formed to
 // float-float accuracy, which one Newton step on the float reciprocal square root does).
 // ---------------------------------------------------------------------------------------------
-template <int G, int RPL>
-__device__ int jacobi_sweep_df(df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, float tol, float tiny,
+template <int G, int RPL, class TM>
+__device__ int jacobi_sweep_df(const TM &tm, df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, float tol, float tiny,
                                int n2) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     constexpr int PPW = 32 / G;
     const int gl = lane % G, grp = lane / G;
     const int npairs = n2 / 2;
@@ -342,21 +344,21 @@ __device__ int jacobi_sweep_df(df *X, int ldx, int rows, int ncols, df *nrm, df 
                 }
             }
         }
-        __syncthreads();
+        tm.sync();
     }
     return rotations;
 }
 
-template <int G, int RPL>
-__device__ void jacobi_df(df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, int *s_rot, float *s_amax,
+template <int G, int RPL, class TM>
+__device__ void jacobi_df(const TM &tm, df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, int *s_rot, float *s_amax,
                           int *sweeps_out, bool *converged_out, float tol, int max_sweeps) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     const float noise = 3.5527137e-15f * (float) (rows > 1 ? rows : 1);  // 2^-48 rows
     const int n2 = ncols + (ncols & 1);
     int sweeps = 0;
     bool converged = ncols < 2;
-    for (int jj = threadIdx.x; jj < ncols; jj += blockDim.x) ds[jj] = dv[jj] = df_f(1.f);
-    __syncthreads();
+    for (int jj = tm.tid; jj < ncols; jj += tm.nth) ds[jj] = dv[jj] = df_f(1.f);
+    tm.sync();
     // Exact squared norms; the scales of the previous sweep are folded into the columns.
     auto fold_and_norms = [&](float &amax) {
         for (int jj = warp; jj < ncols; jj += nw) {
@@ -382,55 +384,55 @@ __device__ void jacobi_df(df *X, int ldx, int rows, int ncols, df *nrm, df *ds, 
         }
     };
     while (!converged && sweeps < max_sweeps) {
-        if (threadIdx.x == 0) {
+        if (tm.tid == 0) {
             *s_rot = 0;
             *s_amax = 0.f;
         }
-        __syncthreads();
+        tm.sync();
         float amax = 0.f;
         fold_and_norms(amax);
         if (lane == 0) atomicMax(reinterpret_cast<int *>(s_amax), __float_as_int(amax));  // amax >= 0
-        __syncthreads();
+        tm.sync();
         const float tiny = *s_amax * noise * noise;
-        const int rot = jacobi_sweep_df<G, RPL>(X, ldx, rows, ncols, nrm, ds, dv, tol, tiny, n2);
+        const int rot = jacobi_sweep_df<G, RPL>(tm, X, ldx, rows, ncols, nrm, ds, dv, tol, tiny, n2);
         if (rot) atomicAdd(s_rot, rot);
-        __syncthreads();
+        tm.sync();
         sweeps++;
         converged = (*s_rot == 0);
-        __syncthreads();
+        tm.sync();
     }
     float amax = 0.f;
     fold_and_norms(amax);  // a sweep limit can leave scales unfolded
-    __syncthreads();
+    tm.sync();
     *sweeps_out = sweeps;
     *converged_out = converged;
 }
 
-template <int MAXRPL>
-__device__ void jacobi_df_dispatch(df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, int *s_rot,
+template <int MAXRPL, class TM>
+__device__ void jacobi_df_dispatch(const TM &tm, df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, int *s_rot,
                                    float *s_amax, int *sweeps, bool *conv, float tol, int max_sweeps) {
-    if (rows <= 32) jacobi_df<4, 8>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
-    else if (rows <= 64) jacobi_df<8, 8>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
-    else if (rows <= 128 && MAXRPL >= 16) jacobi_df<8, 16>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
-    else if (rows <= 128) jacobi_df<16, 8>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
-    else if (rows <= 256 && MAXRPL >= 16) jacobi_df<16, 16>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
-    else if (rows <= 256 || MAXRPL <= 8) jacobi_df<32, 8>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
-    else jacobi_df<32, MAXRPL>(X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    if (rows <= 32) jacobi_df<4, 8>(tm, X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 64) jacobi_df<8, 8>(tm, X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 128 && MAXRPL >= 16) jacobi_df<8, 16>(tm, X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 128) jacobi_df<16, 8>(tm, X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 256 && MAXRPL >= 16) jacobi_df<16, 16>(tm, X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else if (rows <= 256 || MAXRPL <= 8) jacobi_df<32, 8>(tm, X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
+    else jacobi_df<32, MAXRPL>(tm, X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
 }
 
-template <typename T, bool ACC, int MAXRPL>
-__device__ void jacobi_dispatch(T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax,
+template <typename T, bool ACC, int MAXRPL, class TM>
+__device__ void jacobi_dispatch(const TM &tm, T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax,
                                 int *sweeps, bool *conv, double tol, int max_sweeps, T *J, int ldj, double *dsc,
                                 int dstride) {
     // Fewer lanes per pair put more pairs in one warp instruction, so the per-pair scalar work
     // (tangent, tests, norm updates) is shared by 2-4 pairs; RPL rows per lane stay in registers.
-    if (rows <= 32) jacobi<T, 4, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 64) jacobi<T, 8, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 128 && MAXRPL >= 16) jacobi<T, 8, 16, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 128) jacobi<T, 16, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 256 && MAXRPL >= 16) jacobi<T, 16, 16, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 256 || MAXRPL <= 8) jacobi<T, 32, 8, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else jacobi<T, 32, MAXRPL, ACC>(X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    if (rows <= 32) jacobi<T, 4, 8, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 64) jacobi<T, 8, 8, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 128 && MAXRPL >= 16) jacobi<T, 8, 16, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 128) jacobi<T, 16, 8, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 256 && MAXRPL >= 16) jacobi<T, 16, 16, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else if (rows <= 256 || MAXRPL <= 8) jacobi<T, 32, 8, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    else jacobi<T, 32, MAXRPL, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
 }
 
 // Householder QR with column pivoting of A (mrows x ncols, ld lda) in place, stopped early once
@@ -439,9 +441,10 @@ __device__ void jacobi_dispatch(T *X, int ldx, int rows, int ncols, double *nrm,
 // stop2 < 0 disables the early stop; stop2 == 0 with rel > 0 sets stop2 = (rel * |r_00|)^2 after
 // the first pivot.  Column norms are recomputed exactly while each column is updated, so no
 // norm downdating is needed.  Returns the number of rows of R that were computed.
-__device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double stop2, double rel, double *nrm,
+template <class TM>
+__device__ int qrcp_truncated(const TM &tm, double *A, int lda, int mrows, int ncols, double stop2, double rel, double *nrm,
                               double *nref, int *pvt, double *red, int *redi) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     for (int j = warp; j < ncols; j += nw) {
         const double *col = A + (size_t) j * lda;
         double t = 0.0;
@@ -449,15 +452,15 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
         t = warp_sum(t);
         if (lane == 0) nrm[j] = nref[j] = t;
     }
-    for (int j = threadIdx.x; j < ncols; j += blockDim.x) pvt[j] = j;
-    __syncthreads();
+    for (int j = tm.tid; j < ncols; j += tm.nth) pvt[j] = j;
+    tm.sync();
     const int kk = mrows < ncols ? mrows : ncols;
     int rkeep = kk;
     for (int s = 0; s < kk; s++) {
         // pivot = argmax of the remaining squared norms (ties to the lower index)
         double bv = -1.0;
         int bi = s;
-        for (int j = s + threadIdx.x; j < ncols; j += blockDim.x)
+        for (int j = s + tm.tid; j < ncols; j += tm.nth)
             if (nrm[j] > bv) {
                 bv = nrm[j];
                 bi = j;
@@ -474,8 +477,8 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
             red[warp] = bv;
             redi[warp] = bi;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        tm.sync();
+        if (tm.tid == 0) {
             double v = red[0];
             int b = redi[0];
             for (int w = 1; w < nw; w++)
@@ -488,7 +491,7 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
             if (s == 0 && stop2 == 0.0 && rel > 0.0) red[33] = rel * rel * v;
             else if (s == 0) red[33] = stop2;
         }
-        __syncthreads();
+        tm.sync();
         bv = red[32];
         bi = redi[32];
         const double lim = red[33];
@@ -498,12 +501,12 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
         }
         if (bi != s) {
             double *cs = A + (size_t) s * lda, *cb = A + (size_t) bi * lda;
-            for (int i = threadIdx.x; i < mrows; i += blockDim.x) {
+            for (int i = tm.tid; i < mrows; i += tm.nth) {
                 const double t = cs[i];
                 cs[i] = cb[i];
                 cb[i] = t;
             }
-            if (threadIdx.x == 0) {
+            if (tm.tid == 0) {
                 const double t = nrm[s];
                 nrm[s] = nrm[bi];
                 nrm[bi] = t;
@@ -515,16 +518,16 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
                 pvt[bi] = ti;
             }
         }
-        __syncthreads();
+        tm.sync();
         // Householder vector of column s (rows s..mrows-1), dlarfg convention.
         double *x = A + (size_t) s * lda;
         double ss = 0.0;
-        for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) ss = fma(x[i], x[i], ss);
+        for (int i = s + 1 + tm.tid; i < mrows; i += tm.nth) ss = fma(x[i], x[i], ss);
         ss = warp_sum(ss);
-        __syncthreads();
+        tm.sync();
         if (lane == 0) red[warp] = ss;
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        tm.sync();
+        if (tm.tid == 0) {
             double t = 0.0;
             for (int w = 0; w < nw; w++) t += red[w];
             const double alpha = x[s];
@@ -538,10 +541,10 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
             red[40] = tau;
             red[41] = scale;
         }
-        __syncthreads();
+        tm.sync();
         const double tau = red[40], scale = red[41];
-        for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) x[i] *= scale;
-        __syncthreads();
+        for (int i = s + 1 + tm.tid; i < mrows; i += tm.nth) x[i] *= scale;
+        tm.sync();
         // Apply H to the remaining columns; downdate their squared norms below row s
         // (nrm -= y_s^2) and recompute exactly when the downdate cancels (LAPACK dlaqp2's guard).
         for (int j = s + 1 + warp; j < ncols; j += nw) {
@@ -569,7 +572,7 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
                 if (exact) nref[j] = nn;
             }
         }
-        __syncthreads();
+        tm.sync();
     }
     return rkeep;
 }
@@ -579,9 +582,10 @@ __device__ int qrcp_truncated(double *A, int lda, int mrows, int ncols, double s
 // stop2 = rel2 * |r_00|^2 after the first pivot; stop2 < 0 disables it) and norm downdating with
 // exact recomputation when a downdate cancels.  Pivot keys are the float norms' bit patterns
 // (non-negative floats order like their bits).
-__device__ int qrcp_truncated_df(df *A, int lda, int mrows, int ncols, float stop2, float rel2, df *nrm, df *nref,
+template <class TM>
+__device__ int qrcp_truncated_df(const TM &tm, df *A, int lda, int mrows, int ncols, float stop2, float rel2, df *nrm, df *nref,
                                  int *pvt, float *red, int *redi) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     for (int j = warp; j < ncols; j += nw) {
         const df *col = A + (size_t) j * lda;
         df t = df_f(0.f);
@@ -589,13 +593,13 @@ __device__ int qrcp_truncated_df(df *A, int lda, int mrows, int ncols, float sto
         t = group_sum(t, 32);
         if (lane == 0) nrm[j] = nref[j] = t;
     }
-    for (int j = threadIdx.x; j < ncols; j += blockDim.x) pvt[j] = j;
-    __syncthreads();
+    for (int j = tm.tid; j < ncols; j += tm.nth) pvt[j] = j;
+    tm.sync();
     const int kk = mrows < ncols ? mrows : ncols;
     int rkeep = kk;
     for (int s = 0; s < kk; s++) {
         int bv = -1, bi = s;  // float bits of the largest remaining squared norm
-        for (int j = s + threadIdx.x; j < ncols; j += blockDim.x) {
+        for (int j = s + tm.tid; j < ncols; j += tm.nth) {
             const int v = __float_as_int(nrm[j].h);
             if (v > bv) {
                 bv = v;
@@ -612,23 +616,23 @@ __device__ int qrcp_truncated_df(df *A, int lda, int mrows, int ncols, float sto
         }
         if (lane == 0) {
             redi[warp] = bv;
-            redi[8 + warp] = bi;
+            redi[32 + warp] = bi;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int v = redi[0], b = redi[8];
+        tm.sync();
+        if (tm.tid == 0) {
+            int v = redi[0], b = redi[32];
             for (int w = 1; w < nw; w++)
-                if (redi[w] > v || (redi[w] == v && redi[8 + w] < b)) {
+                if (redi[w] > v || (redi[w] == v && redi[32 + w] < b)) {
                     v = redi[w];
-                    b = redi[8 + w];
+                    b = redi[32 + w];
                 }
-            redi[16] = v;
-            redi[17] = b;
+            redi[64] = v;
+            redi[65] = b;
             if (s == 0) red[33] = (stop2 == 0.f && rel2 > 0.f) ? rel2 * __int_as_float(v) : stop2;
         }
-        __syncthreads();
-        const float bvf = __int_as_float(redi[16]);
-        bi = redi[17];
+        tm.sync();
+        const float bvf = __int_as_float(redi[64]);
+        bi = redi[65];
         const float lim = red[33];
         if (bvf <= lim || bvf <= 0.f) {
             rkeep = s;
@@ -636,12 +640,12 @@ __device__ int qrcp_truncated_df(df *A, int lda, int mrows, int ncols, float sto
         }
         if (bi != s) {
             df *cs = A + (size_t) s * lda, *cb = A + (size_t) bi * lda;
-            for (int i = threadIdx.x; i < mrows; i += blockDim.x) {
+            for (int i = tm.tid; i < mrows; i += tm.nth) {
                 const df t = cs[i];
                 cs[i] = cb[i];
                 cb[i] = t;
             }
-            if (threadIdx.x == 0) {
+            if (tm.tid == 0) {
                 const df t = nrm[s];
                 nrm[s] = nrm[bi];
                 nrm[bi] = t;
@@ -653,17 +657,18 @@ __device__ int qrcp_truncated_df(df *A, int lda, int mrows, int ncols, float sto
                 pvt[bi] = ti;
             }
         }
-        __syncthreads();
+        tm.sync();
         // Householder vector of column s (rows s..mrows-1), dlarfg convention.
         df *x = A + (size_t) s * lda;
         df ss = df_f(0.f);
-        for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) ss = df_fma(x[i], x[i], ss);
+        for (int i = s + 1 + tm.tid; i < mrows; i += tm.nth) ss = df_fma(x[i], x[i], ss);
         ss = group_sum(ss, 32);
-        __syncthreads();
-        df *redd = reinterpret_cast<df *>(red + 40);  // 8 warp partials, then tau and scale
+        tm.sync();
+        df *redd = reinterpret_cast<df *>(red + 64);  // per-warp partials (floats 64..127)
+        df *rts = reinterpret_cast<df *>(red + 40);   // tau and scale
         if (lane == 0) redd[warp] = ss;
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        tm.sync();
+        if (tm.tid == 0) {
             df t = df_f(0.f);
             for (int w = 0; w < nw; w++) t = df_add(t, redd[w]);
             const df alpha = x[s];
@@ -675,13 +680,13 @@ __device__ int qrcp_truncated_df(df *A, int lda, int mrows, int ncols, float sto
                 scale = df_div(df_f(1.f), df_add(alpha, -beta));
             }
             x[s] = beta;
-            redd[8] = tau;
-            redd[9] = scale;
+            rts[0] = tau;
+            rts[1] = scale;
         }
-        __syncthreads();
-        const df tau = redd[8], scale = redd[9];
-        for (int i = s + 1 + threadIdx.x; i < mrows; i += blockDim.x) x[i] = df_mul(x[i], scale);
-        __syncthreads();
+        tm.sync();
+        const df tau = rts[0], scale = rts[1];
+        for (int i = s + 1 + tm.tid; i < mrows; i += tm.nth) x[i] = df_mul(x[i], scale);
+        tm.sync();
         const bool has_tau = tau.h != 0.f;
         for (int j = s + 1 + warp; j < ncols; j += nw) {
             df *y = A + (size_t) j * lda;
@@ -709,21 +714,83 @@ __device__ int qrcp_truncated_df(df *A, int lda, int mrows, int ncols, float sto
                 if (exact) nref[j] = nn;
             }
         }
-        __syncthreads();
+        tm.sync();
     }
     return rkeep;
 }
 
+template <int RPL, class TM>
+__device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace &ws, const Params &p, int slot,
+                            double *sm, int smem_doubles, int &s_rot, int &s_rank, int &s_emax, double &s_amax);
+
+// Stage key of an update in ws.order (sorted by decreasing key): its stack width k when C is
+// compressed.  Both fields are written by the plan kernel only, so the key is stable while the
+// heavy stages run.
+__device__ __forceinline__ int order_key(const Workspace &ws, int slot) {
+    const int *m = ws.meta + (size_t) slot * META_INTS;
+    return m[META_CKIND] ? m[META_K] : 0;
+}
+
+// CTA of SVD_THREADS threads.  Updates with k > kthr ("heavy": their core does not fit half of the
+// shared memory) get a whole CTA each; the others are paired, one per half-CTA team of
+// SVD_THREADS / 2 threads with its own half of the shared memory and its own named barrier.  With
+// ws.order (sorted by decreasing k) the heavy updates are its first H entries: CTA b < H takes
+// order[b], CTA H + i takes order[H + 2i] and order[H + 2i + 1].  Without an order (one update per
+// CTA) the team size follows the same class rule, so an update's arithmetic never depends on the
+// launch it is part of.
 template <int RPL>
-__global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdate *ups, Workspace ws, Params p,
-                                                               int smem_doubles) {
-    extern __shared__ double sm[];
-    __shared__ int s_rot, s_rank;
-    __shared__ double s_amax;
-    const int slot = ws.heavy(blockIdx.x);
+__global__ void __launch_bounds__(SVD_THREADS, 1) core_svd_kernel(const DevUpdate *ups, int nup, Workspace ws,
+                                                               Params p, int team_doubles, int kthr) {
+    extern __shared__ double smem_all[];
+    __shared__ int s_rot_a[2], s_rank_a[2], s_emax_a[2], s_nheavy;
+    __shared__ double s_amax_a[2];
+    if (threadIdx.x == 0) {
+        int h = -1;
+        if (ws.order) {
+            int lo = 0, hi = nup;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (order_key(ws, ws.order[mid]) > kthr) lo = mid + 1;
+                else hi = mid;
+            }
+            h = lo;
+        }
+        s_nheavy = h;
+    }
+    __syncthreads();
+    const int H = s_nheavy;
+    constexpr int HALF = SVD_THREADS / 2;
+    int idx, half = 0;
+    bool heavy;
+    if (H < 0) {
+        idx = blockIdx.x;
+        heavy = order_key(ws, idx) > kthr;
+        if (!heavy && threadIdx.x >= HALF) return;
+    } else if ((int) blockIdx.x < H) {
+        idx = blockIdx.x;
+        heavy = true;
+    } else {
+        heavy = false;
+        half = threadIdx.x / HALF;
+        idx = H + 2 * ((int) blockIdx.x - H) + half;
+    }
+    if (idx >= nup) return;
+    double *sm = smem_all + (size_t) half * team_doubles;
+    if (heavy)
+        core_update<RPL>(Team<SVD_THREADS>{(int) threadIdx.x, 1}, ups, ws, p, ws.heavy(idx), sm, 2 * team_doubles,
+                         s_rot_a[0], s_rank_a[0], s_emax_a[0], s_amax_a[0]);
+    else
+        core_update<RPL>(Team<HALF>{(int) threadIdx.x % HALF, 1 + half}, ups, ws, p, ws.heavy(idx), sm, team_doubles,
+                         s_rot_a[half], s_rank_a[half], s_emax_a[half], s_amax_a[half]);
+}
+
+// The recompression core of one update (slot) by one team, with `smem_doubles` of shared memory at sm.
+template <int RPL, class TM>
+__device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace &ws, const Params &p, int slot,
+                            double *sm, int smem_doubles, int &s_rot, int &s_rank, int &s_emax, double &s_amax) {
     int *meta = ws.meta + (size_t) slot * META_INTS;
     if (meta[META_STATUS] != HCGB_OK || !meta[META_CKIND]) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     const int lr = lane >> 2, lc = lane & 3;
     const int k = meta[META_K], m = meta[META_M], n = meta[META_N];
     const int kU = m < k ? m : k, kV = n < k ? n : k;
@@ -732,8 +799,8 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     const double *RU = base + ws.off_ustack;
     const double *RV = base + ws.off_vstack;
     double *Mc = base + ws.off_mcopy;
-    // Aux arrays at the start of shared memory: sorted sigma, scratch, column norms, the sort
-    // permutation, the QR pivots and a small reduction area.
+    // Aux arrays at the start of the team's shared memory: sorted sigma, scratch, column norms,
+    // the sort permutation, the QR pivots and a reduction area (64 doubles + 128 ints).
     double *sig = sm;
     double *inv = sig + ws.kmax;
     double *nrm = inv + ws.kmax;
@@ -741,8 +808,8 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     int *pvt = perm + ws.kmax;
     double *dsc = nrm + ws.kmax + ws.kmax + 1;  // Jacobi column scales d and 1/d (2 kmax)
     double *red = dsc + 2 * ws.kmax;
-    int *redi = reinterpret_cast<int *>(red + 48);
-    double *pool = red + 48 + 24;
+    int *redi = reinterpret_cast<int *>(red + SVD_RED_DOUBLES);
+    double *pool = red + SVD_RED_DOUBLES + SVD_REDI_INTS / 2;
     const int pool_doubles = smem_doubles - (int) (pool - sm);
     // Working copy of M: shared memory when it fits, else the workspace.
     double *Mw;
@@ -781,7 +848,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
             }
         }
     }
-    __syncthreads();
+    tm.sync();
 
     // 2. Rank-revealing QR with column pivoting, M P = Q R, stopped once every remaining column
     //    is below QRCP_STOP (1e-2) of the truncation threshold.  The dropped block R22 lies far
@@ -805,29 +872,28 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     if (p.mode == 1) {
         // Exact power-of-two scaling that brings the largest entry of M near 1 (float range), then
         // the pivoted QR and the Jacobi sweeps in float-float arithmetic on the FP32 pipe.
-        __shared__ int s_emax;
-        if (threadIdx.x == 0) s_emax = 0;
-        __syncthreads();
+        if (tm.tid == 0) s_emax = 0;
+        tm.sync();
         int em = 0;
-        for (int e = threadIdx.x; e < kU * kV; e += blockDim.x) {
+        for (int e = tm.tid; e < kU * kV; e += tm.nth) {
             const int ef = (int) ((__double_as_longlong(Mw[(e % kU) + (size_t) (e / kU) * ldw]) >> 52) & 0x7ff);
             em = em > ef ? em : ef;
         }
         atomicMax(&s_emax, em);
-        __syncthreads();
+        tm.sync();
         eshift = s_emax ? s_emax - 1023 : 0;
         const double down = __hiloint2double((1023 - eshift) << 20, 0);
         df *Md = reinterpret_cast<df *>(Mw);
-        for (int e = threadIdx.x; e < kU * kV; e += blockDim.x) {
+        for (int e = tm.tid; e < kU * kV; e += tm.nth) {
             const size_t o = (e % kU) + (size_t) (e / kU) * ldw;
             Md[o] = df(Mw[o] * down);
         }
-        __syncthreads();
+        tm.sync();
         const float stop2f = stop2 > 0.0 ? (float) (stop2 * down * down) : (float) stop2;
-        rk = qrcp_truncated_df(Md, ldw, kU, kV, stop2f, (float) (rel * rel), reinterpret_cast<df *>(nrm),
+        rk = qrcp_truncated_df(tm, Md, ldw, kU, kV, stop2f, (float) (rel * rel), reinterpret_cast<df *>(nrm),
                                reinterpret_cast<df *>(inv), pvt, reinterpret_cast<float *>(red), redi);
     } else {
-        rk = qrcp_truncated(Mw, ldw, kU, kV, stop2, rel, nrm, inv, pvt, red, redi);
+        rk = qrcp_truncated(tm, Mw, ldw, kU, kV, stop2, rel, nrm, inv, pvt, red, redi);
     }
     const long long t2 = clock64();
     if (rk < 1) rk = 1;
@@ -835,12 +901,12 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
     // 3. X = R(0:rk, :)^T (kV x rk), staged through XV, then into the working buffer (ld kV).
     for (int i = warp; i < rk; i += nw)
         for (int l = lane; l < kV; l += 32) XV[l + (size_t) i * ld] = l >= i ? Mw[i + (size_t) l * ldw] : 0.0;
-    __syncthreads();
+    tm.sync();
     double *X = Mw;
     const int ldx = kV;
     for (int i = warp; i < rk; i += nw)
         for (int l = lane; l < kV; l += 32) X[l + (size_t) i * ldx] = XV[l + (size_t) i * ld];
-    __syncthreads();
+    tm.sync();
 
     // 4. One-sided Jacobi on the rk columns of X (lane group sized to the column length kV).
     //    X J = W with orthogonal columns: sigma_i = ||w_i||, right singular vectors P W Sigma^-1.
@@ -854,16 +920,16 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         const double up = __hiloint2double((1023 + eshift) << 20, 0);
         const float tol_df = 16.f * 3.5527137e-15f * (float) (kV > 1 ? kV : 1);
         // norms and scales as float-float values in the (double-sized) nrm and dsc arrays
-        jacobi_df_dispatch<RPL>(Xd, ldx, kV, rk, reinterpret_cast<df *>(nrm), reinterpret_cast<df *>(dsc),
+        jacobi_df_dispatch<RPL>(tm, Xd, ldx, kV, rk, reinterpret_cast<df *>(nrm), reinterpret_cast<df *>(dsc),
                                 reinterpret_cast<df *>(dsc + ws.kmax), &s_rot, reinterpret_cast<float *>(&s_amax),
                                 &sweeps, &converged, tol_df, MAX_JACOBI_SWEEPS);
-        for (int e = threadIdx.x; e < kV * rk; e += blockDim.x) {
+        for (int e = tm.tid; e < kV * rk; e += tm.nth) {
             const size_t o = (e % kV) + (size_t) (e / kV) * ldx;
             X[o] = (double) Xd[o] * up;
         }
-        __syncthreads();
+        tm.sync();
     } else {
-        jacobi_dispatch<double, false, RPL>(X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
+        jacobi_dispatch<double, false, RPL>(tm, X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
                                             MAX_JACOBI_SWEEPS, (double *) nullptr, 0, dsc, ws.kmax);
     }
 
@@ -876,8 +942,8 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         t = warp_sum(t);
         if (lane == 0) inv[j] = sqrt(t);  // unsorted sigma, temporarily in inv[]
     }
-    __syncthreads();
-    for (int j = threadIdx.x; j < rk; j += blockDim.x) {
+    tm.sync();
+    for (int j = tm.tid; j < rk; j += tm.nth) {
         const double sj = inv[j];
         int pos = 0;
         for (int l = 0; l < rk; l++) {
@@ -887,8 +953,8 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         perm[pos] = j;
         sig[pos] = sj;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    tm.sync();
+    if (tm.tid == 0) {
         const int sizeS = kU < kV ? kU : kV;
         int r;
         if (p.fixed_rank > 0) {
@@ -913,9 +979,9 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         meta[META_CORE_COLS] = rk;
         if (!converged) meta[META_STATUS] = HCGB_NOT_CONVERGED;
     }
-    __syncthreads();
+    tm.sync();
     const int r = s_rank;
-    for (int i = threadIdx.x; i < r; i += blockDim.x) inv[i] = sig[i] > 1e-150 ? 1.0 / (sig[i] * sig[i]) : 0.0;
+    for (int i = tm.tid; i < r; i += tm.nth) inv[i] = sig[i] > 1e-150 ? 1.0 / (sig[i] * sig[i]) : 0.0;
 
     // 6. Right factor in the small basis: XV = P W_r (= V_r Sigma_r), n rows, zero below kV.
     for (int i = warp; i < r; i += nw) {
@@ -923,7 +989,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         for (int l = lane; l < kV; l += 32) XV[pvt[l] + (size_t) i * ld] = w[l];
         for (int l = kV + lane; l < n; l += 32) XV[l + (size_t) i * ld] = 0.0;
     }
-    __syncthreads();
+    tm.sync();
 
     // 7. Left factor in the small basis: C.U[:, i] = [M XV[:, i] / sigma_i^2 ; 0] (= U_r), on DMMA.
     double *CU = ups[slot].c.data;
@@ -948,7 +1014,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
         for (int i = warp; i < r; i += nw)
             for (int l = kU + lane; l < m; l += 32) CU[l + (size_t) i * ldcu] = 0.0;
     }
-    if (threadIdx.x == 0) {
+    if (tm.tid == 0) {
         const long long t4 = clock64();
         meta[META_KC_PRODUCT] = (int) ((t1 - t0) >> 10);
         meta[META_KC_QRCP] = (int) ((t2 - t1) >> 10);
@@ -959,20 +1025,41 @@ __global__ void __launch_bounds__(SVD_THREADS, 2) core_svd_kernel(const DevUpdat
 
 }  // namespace
 
-size_t svd_smem_bytes(int kmax) {
-    size_t aux = (size_t) 6 * kmax + 1 + 48 + 24;
-    size_t want = aux + (size_t) kmax * kmax;
-    size_t cap = 110 * 1024 / sizeof(double);  // two CTAs per SM
-    if (cap < aux) cap = aux;                   // the aux arrays always fit (checked against the device limit)
-    if (want > cap) want = cap;
-    return want * sizeof(double);
+namespace {
+
+// Doubles of shared memory per half-CTA team: everything a core of kmax columns could use, capped at
+// half of the per-block opt-in limit (less a reserve for the kernel's static shared variables), and
+// never below the aux arrays.
+int svd_team_doubles(int kmax) {
+    static int optin = 0;
+    if (!optin) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (optin <= 0) optin = 48 * 1024;
+    }
+    const long aux = 6L * kmax + SVD_AUX_FIXED;
+    const long want = aux + (long) kmax * kmax;
+    const long cap = (optin - 256) / 2 / (long) sizeof(double);
+    long t = want < cap ? want : cap;
+    if (t < aux) t = aux;  // checked against the device limit by the caller
+    return (int) t;
 }
+
+}  // namespace
+
+size_t svd_smem_bytes(int kmax) { return 2 * sizeof(double) * (size_t) svd_team_doubles(kmax); }
 
 template <int RPL>
 static void launch_core_svd_t(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st) {
-    const size_t smem = svd_smem_bytes(ws.kmax);
+    const int team = svd_team_doubles(ws.kmax);
+    const size_t smem = 2 * sizeof(double) * (size_t) team;
+    // Heavy: a core of k columns (k x k working copy) does not fit the team's pool.
+    const long pool = (long) team - 6L * ws.kmax - SVD_AUX_FIXED;
+    int kthr = 0;
+    while ((long) (kthr + 1) * (kthr + 1) <= pool) kthr++;
     cudaFuncSetAttribute(core_svd_kernel<RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    core_svd_kernel<RPL><<<n, SVD_THREADS, smem, st>>>(ups, ws, p, (int) (smem / sizeof(double)));
+    core_svd_kernel<RPL><<<n, SVD_THREADS, smem, st>>>(ups, n, ws, p, team, kthr);
 }
 
 // Rows of M are at most min(ld, kmax); the register tile of a rotation covers 32 * RPL rows.
