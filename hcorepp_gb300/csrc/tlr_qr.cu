@@ -18,6 +18,8 @@ namespace {
 
 constexpr int NB = QR_NB;
 constexpr int QR_THREADS = 256;
+constexpr int QRD_THREADS = 512;  // mixed-form kernels: one heavy side, or both sides of a light update
+constexpr int QR_HEAVY_K = 95;    // sides of updates with a wider stack get a whole CTA
 
 __host__ __device__ __forceinline__ int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
@@ -85,18 +87,19 @@ __device__ void factor_panel(double *Ps, int ldp, int mr, int nbp, double *tau_s
 
 // Float-float version of factor_panel (mixed form), in place on the panel held as float-float
 // values of (panel * 2^-eshift); same dlarfg convention.  red: >= 24 doubles of scratch.
-__device__ void factor_panel_df(df *Ps, int ldp, int mr, int nbp, double *tau_s, double *red) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+template <class TM>
+__device__ void factor_panel_df(const TM &tm, df *Ps, int ldp, int mr, int nbp, double *tau_s, double *red) {
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     df *redd = reinterpret_cast<df *>(red);
     for (int j = 0; j < nbp; j++) {
         df *x = Ps + (size_t) j * ldp;
         df ss = df_f(0.f);
-        for (int r = j + 1 + threadIdx.x; r < mr; r += blockDim.x) ss = df_fma(x[r], x[r], ss);
+        for (int r = j + 1 + tm.tid; r < mr; r += tm.nth) ss = df_fma(x[r], x[r], ss);
         ss = df_group_sum(ss, 32);
-        __syncthreads();
+        tm.sync();
         if (lane == 0) redd[warp] = ss;
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        tm.sync();
+        if (tm.tid == 0) {
             df t = df_f(0.f);
             for (int w = 0; w < nw; w++) t = df_add(t, redd[w]);
             const df alpha = x[j];
@@ -108,14 +111,14 @@ __device__ void factor_panel_df(df *Ps, int ldp, int mr, int nbp, double *tau_s,
                 scale = df_div(df_f(1.f), df_add(alpha, -beta));
             }
             tau_s[j] = (double) tau;
-            redd[8] = scale;
-            redd[9] = tau;
+            redd[32] = scale;
+            redd[33] = tau;
             x[j] = beta;
         }
-        __syncthreads();
-        const df scale = redd[8], tau = redd[9];
-        for (int r = j + 1 + threadIdx.x; r < mr; r += blockDim.x) x[r] = df_mul(x[r], scale);
-        __syncthreads();
+        tm.sync();
+        const df scale = redd[32], tau = redd[33];
+        for (int r = j + 1 + tm.tid; r < mr; r += tm.nth) x[r] = df_mul(x[r], scale);
+        tm.sync();
         if (tau.h != 0.f) {
             for (int c = j + 1 + warp; c < nbp; c += nw) {
                 df *y = Ps + (size_t) c * ldp;
@@ -127,7 +130,7 @@ __device__ void factor_panel_df(df *Ps, int ldp, int mr, int nbp, double *tau_s,
                 for (int r = j + 1 + lane; r < mr; r += 32) y[r] = df_fma(mw, x[r], y[r]);
             }
         }
-        __syncthreads();
+        tm.sync();
     }
 }
 
@@ -332,17 +335,19 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(Workspace ws) {
 // FP32 pipe; R and the reflectors are written back in double at the end (R scaled back, the
 // reflectors and tau are scale-free).
 // ---------------------------------------------------------------------------------------------
-__device__ void make_explicit_v_df(df *Ps, int ldp, int nbp) {
-    for (int e = threadIdx.x; e < NB * ldp; e += blockDim.x) {
+template <class TM>
+__device__ void make_explicit_v_df(const TM &tm, df *Ps, int ldp, int nbp) {
+    for (int e = tm.tid; e < NB * ldp; e += tm.nth) {
         const int c = e / ldp, r = e % ldp;
         if (c >= nbp || r < c) Ps[e] = df_f(0.f);
         else if (r == c) Ps[e] = df_f(1.f);
     }
 }
 
-__device__ void build_t_df(const df *Ps, int ldp, int mr, int nbp, const double *tau_s, df *Ts, df *Gs) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) Ts[e] = df_f(0.f);
+template <class TM>
+__device__ void build_t_df(const TM &tm, const df *Ps, int ldp, int mr, int nbp, const double *tau_s, df *Ts, df *Gs) {
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
+    for (int e = tm.tid; e < NB * NB; e += tm.nth) Ts[e] = df_f(0.f);
     const int npairs = nbp * (nbp - 1) / 2;
     for (int p = warp; p < npairs; p += nw) {
         int i = 1, base = 0;
@@ -357,7 +362,7 @@ __device__ void build_t_df(const df *Ps, int ldp, int mr, int nbp, const double 
         sacc = df_group_sum(sacc, 32);
         if (lane == 0) Gs[l * NB + i] = sacc;
     }
-    __syncthreads();
+    tm.sync();
     if (warp == 0) {
         const int j = lane;
         for (int i = 0; i < nbp; i++) {
@@ -373,13 +378,14 @@ __device__ void build_t_df(const df *Ps, int ldp, int mr, int nbp, const double 
             __syncwarp();
         }
     }
-    __syncthreads();
+    tm.sync();
 }
 
 // X (mr x nt, ld ldx, float-float) <- (I - V op(T) V^T) X, columns in chunks of ldw.
-__device__ void apply_block_reflector_df(const df *Ps, int ldp, const df *Ts, bool trans_t, df *X, int ldx, int mr,
+template <class TM>
+__device__ void apply_block_reflector_df(const TM &tm, const df *Ps, int ldp, const df *Ts, bool trans_t, df *X, int ldx, int mr,
                                          int nt, df *Ws, int ldw) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     for (int c0 = 0; c0 < nt; c0 += ldw) {
         const int ntc = nt - c0 < ldw ? nt - c0 : ldw;
         df *Xc = X + (size_t) c0 * ldx;
@@ -400,9 +406,9 @@ __device__ void apply_block_reflector_df(const df *Ps, int ldp, const df *Ts, bo
                 if (lane == 0) Ws[i * ldw + c] = v;
             }
         }
-        __syncthreads();
+        tm.sync();
         // B: W <- -op(T) W, a thread per column
-        for (int c = threadIdx.x; c < ntc; c += blockDim.x) {
+        for (int c = tm.tid; c < ntc; c += tm.nth) {
             df w[NB], o[NB];
 #pragma unroll
             for (int i = 0; i < NB; i++) w[i] = Ws[i * ldw + c];
@@ -421,23 +427,23 @@ __device__ void apply_block_reflector_df(const df *Ps, int ldp, const df *Ts, bo
 #pragma unroll
             for (int i = 0; i < NB; i++) Ws[i * ldw + c] = o[i];
         }
-        __syncthreads();
+        tm.sync();
         // C: X += V W, a thread per element (rows fastest: coalesced)
-        for (int e = threadIdx.x; e < mr * ntc; e += blockDim.x) {
+        for (int e = tm.tid; e < mr * ntc; e += tm.nth) {
             const int r = e % mr, c = e / mr;
             df x = Xc[r + (size_t) c * ldx];
 #pragma unroll
             for (int i = 0; i < NB; i++) x = df_fma(Ps[(size_t) i * ldp + r], Ws[i * ldw + c], x);
             Xc[r + (size_t) c * ldx] = x;
         }
-        __syncthreads();
+        tm.sync();
     }
 }
 
-// grid = 2 * n, as qr_kernel; the mixed form.
-__global__ void __launch_bounds__(QR_THREADS) qr_kernel_df(Workspace ws) {
-    extern __shared__ double sm[];
-    const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
+// One side (U: 0, V: 1) of one update's stack QR in the mixed form, by one team, with the team's
+// shared memory at sm.
+template <class TM>
+__device__ void qr_side_df(const TM &tm, const Workspace &ws, int slot, int side, double *sm, int &s_emax) {
     const int *meta = ws.meta + (size_t) slot * META_INTS;
     if (meta[META_STATUS] != HCGB_OK || !meta[META_CKIND]) return;
     const int k = meta[META_K];
@@ -452,49 +458,48 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel_df(Workspace ws) {
     df *Tsd = reinterpret_cast<df *>(s.Ts), *Gsd = reinterpret_cast<df *>(s.Gs);
     df *Ad = reinterpret_cast<df *>(A);
     // 1. the stack as float-float values of A * 2^-eshift (entries below 2)
-    __shared__ int s_emax;
-    if (threadIdx.x == 0) s_emax = 0;
-    __syncthreads();
+    if (tm.tid == 0) s_emax = 0;
+    tm.sync();
     int em = 0;
-    for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
+    for (int e = tm.tid; e < m * k; e += tm.nth) {
         const int ef = (int) ((__double_as_longlong(A[(e % m) + (size_t) (e / m) * lda]) >> 52) & 0x7ff);
         em = em > ef ? em : ef;
     }
     atomicMax(&s_emax, em);
-    __syncthreads();
+    tm.sync();
     const int eshift = s_emax ? s_emax - 1023 : 0;
     const double down = __hiloint2double((1023 - eshift) << 20, 0), up = __hiloint2double((1023 + eshift) << 20, 0);
-    for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
+    for (int e = tm.tid; e < m * k; e += tm.nth) {
         const size_t o = (e % m) + (size_t) (e / m) * lda;
         Ad[o] = df(A[o] * down);
     }
-    __syncthreads();
+    tm.sync();
     // 2. panels
     const int kk = m < k ? m : k;
     for (int j0 = 0; j0 < kk; j0 += NB) {
         const int nbp = (kk - j0) < NB ? (kk - j0) : NB;
         const int mr = m - j0;
-        for (int e = threadIdx.x; e < NB * s.ldp; e += blockDim.x) {
+        for (int e = tm.tid; e < NB * s.ldp; e += tm.nth) {
             const int c = e / s.ldp, r = e % s.ldp;
             Psd[e] = (c < nbp && r < mr) ? Ad[(j0 + r) + (size_t) (j0 + c) * lda] : df_f(0.f);
         }
-        __syncthreads();
-        factor_panel_df(Psd, s.ldp, mr, nbp, s.tau, s.red);
-        for (int e = threadIdx.x; e < nbp * mr; e += blockDim.x) {
+        tm.sync();
+        factor_panel_df(tm, Psd, s.ldp, mr, nbp, s.tau, s.red);
+        for (int e = tm.tid; e < nbp * mr; e += tm.nth) {
             const int c = e / mr, r = e % mr;
             Ad[(j0 + r) + (size_t) (j0 + c) * lda] = Psd[(size_t) c * s.ldp + r];
         }
-        if (threadIdx.x < nbp) tau[j0 + threadIdx.x] = s.tau[threadIdx.x];
-        __syncthreads();
-        make_explicit_v_df(Psd, s.ldp, nbp);
-        __syncthreads();
-        build_t_df(Psd, s.ldp, mr, nbp, s.tau, Tsd, Gsd);
-        for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) Tg[(size_t) (j0 / NB) * NB * NB + e] = (double) Tsd[e];
+        if (tm.tid < nbp) tau[j0 + tm.tid] = s.tau[tm.tid];
+        tm.sync();
+        make_explicit_v_df(tm, Psd, s.ldp, nbp);
+        tm.sync();
+        build_t_df(tm, Psd, s.ldp, mr, nbp, s.tau, Tsd, Gsd);
+        for (int e = tm.tid; e < NB * NB; e += tm.nth) Tg[(size_t) (j0 / NB) * NB * NB + e] = (double) Tsd[e];
         const int c0 = j0 + nbp;
-        apply_block_reflector_df(Psd, s.ldp, Tsd, true, Ad + j0 + (size_t) c0 * lda, lda, mr, k - c0, Wsd, s.ldw);
+        apply_block_reflector_df(tm, Psd, s.ldp, Tsd, true, Ad + j0 + (size_t) c0 * lda, lda, mr, k - c0, Wsd, s.ldw);
     }
     // 3. back to double: R (on and above the diagonal) scaled back, reflectors as they are
-    for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
+    for (int e = tm.tid; e < m * k; e += tm.nth) {
         const int r = e % m, c = e / m;
         const size_t o = r + (size_t) c * lda;
         const double v = (double) Ad[o];
@@ -545,11 +550,11 @@ __global__ void __launch_bounds__(QR_THREADS) apply_q_kernel(const DevUpdate *up
     }
 }
 
-// grid = 2 * n, as apply_q_kernel; the mixed form: X is held as float-float values (scaled by a
-// power of two) while the panels are applied, then written back in double.
-__global__ void __launch_bounds__(QR_THREADS) apply_q_kernel_df(const DevUpdate *ups, Workspace ws) {
-    extern __shared__ double sm[];
-    const int slot = ws.heavy(blockIdx.x >> 1), side = blockIdx.x & 1;
+// One side of one update's Q application in the mixed form (X <- Q X, X held as float-float values
+// scaled by a power of two while the panels are applied, then written back in double), by one team.
+template <class TM>
+__device__ void apply_q_side_df(const TM &tm, const DevUpdate *ups, const Workspace &ws, int slot, int side,
+                                double *sm, int &s_emax) {
     const int *meta = ws.meta + (size_t) slot * META_INTS;
     const int st = meta[META_STATUS];
     if ((st != HCGB_OK && st != HCGB_NOT_CONVERGED) || !meta[META_CKIND]) return;
@@ -573,43 +578,123 @@ __global__ void __launch_bounds__(QR_THREADS) apply_q_kernel_df(const DevUpdate 
     QrShared s = carve(sm, ws.ld, ws.kmax);
     df *Psd = reinterpret_cast<df *>(s.Ps), *Wsd = reinterpret_cast<df *>(s.Ws), *Tsd = reinterpret_cast<df *>(s.Ts);
     df *Xd = reinterpret_cast<df *>(X);
-    __shared__ int s_emax;
-    if (threadIdx.x == 0) s_emax = 0;
-    __syncthreads();
+    if (tm.tid == 0) s_emax = 0;
+    tm.sync();
     int em = 0;
-    for (int e = threadIdx.x; e < m * r; e += blockDim.x) {
+    for (int e = tm.tid; e < m * r; e += tm.nth) {
         const int ef = (int) ((__double_as_longlong(X[(e % m) + (size_t) (e / m) * ldx]) >> 52) & 0x7ff);
         em = em > ef ? em : ef;
     }
     atomicMax(&s_emax, em);
-    __syncthreads();
+    tm.sync();
     const int eshift = s_emax ? s_emax - 1023 : 0;
     const double down = __hiloint2double((1023 - eshift) << 20, 0), up = __hiloint2double((1023 + eshift) << 20, 0);
-    for (int e = threadIdx.x; e < m * r; e += blockDim.x) {
+    for (int e = tm.tid; e < m * r; e += tm.nth) {
         const size_t o = (e % m) + (size_t) (e / m) * ldx;
         Xd[o] = df(X[o] * down);
     }
-    __syncthreads();
+    tm.sync();
     const int kk = m < k ? m : k;
     const int npan = (kk + NB - 1) / NB;
     for (int p = npan - 1; p >= 0; p--) {
         const int j0 = p * NB;
         const int nbp = (kk - j0) < NB ? (kk - j0) : NB;
         const int mr = m - j0;
-        for (int e = threadIdx.x; e < NB * s.ldp; e += blockDim.x) {
+        for (int e = tm.tid; e < NB * s.ldp; e += tm.nth) {
             const int c = e / s.ldp, rr = e % s.ldp;
             double v = 0.0;
             if (c < nbp && rr < mr) v = rr > c ? A[(j0 + rr) + (size_t) (j0 + c) * lda] : (rr == c ? 1.0 : 0.0);
             Psd[e] = df(v);
         }
-        for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) Tsd[e] = df(Tg[(size_t) p * NB * NB + e]);
-        __syncthreads();
-        apply_block_reflector_df(Psd, s.ldp, Tsd, false, Xd + j0, ldx, mr, r, Wsd, s.ldw);
+        for (int e = tm.tid; e < NB * NB; e += tm.nth) Tsd[e] = df(Tg[(size_t) p * NB * NB + e]);
+        tm.sync();
+        apply_block_reflector_df(tm, Psd, s.ldp, Tsd, false, Xd + j0, ldx, mr, r, Wsd, s.ldw);
     }
-    for (int e = threadIdx.x; e < m * r; e += blockDim.x) {
+    for (int e = tm.tid; e < m * r; e += tm.nth) {
         const size_t o = (e % m) + (size_t) (e / m) * ldx;
         X[o] = (double) Xd[o] * up;
     }
+}
+
+// Work split of the mixed-form QR and Q-application kernels (CTAs of QRD_THREADS threads): a side
+// of an update with k > QR_HEAVY_K gets a whole CTA (CTA b < 2H: side b & 1 of order[b / 2]); the
+// other updates take one CTA each, the U side in the first half-CTA team and the V side in the
+// second (named barriers 1 and 2, half of the shared memory each); when two teams' shared memory
+// does not fit one CTA (pair == 0), each such side takes a CTA of its own, served by the first
+// team.  Without an order (one update): CTA b works on side b & 1 of update b / 2 with the team its
+// class gets.  A side's team size depends only on its class, so its arithmetic never depends on
+// the launch.  Returns false for threads without work.
+__device__ bool qr_assign(const Workspace &ws, int nup, int pair, int &slot, int &side, int &half, bool &heavy) {
+    __shared__ int s_nheavy;
+    if (threadIdx.x == 0) {
+        int h = -1;
+        if (ws.order) {
+            int lo = 0, hi = nup;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                const int *m = ws.meta + (size_t) ws.order[mid] * META_INTS;
+                if ((m[META_CKIND] ? m[META_K] : 0) > QR_HEAVY_K) lo = mid + 1;
+                else hi = mid;
+            }
+            h = lo;
+        }
+        s_nheavy = h;
+    }
+    __syncthreads();
+    const int H = s_nheavy;
+    constexpr int HALF = QRD_THREADS / 2;
+    half = 0;
+    int idx;
+    if (H < 0) {
+        idx = blockIdx.x >> 1;
+        side = blockIdx.x & 1;
+        if (idx >= nup) return false;
+        const int *m = ws.meta + (size_t) idx * META_INTS;
+        heavy = (m[META_CKIND] ? m[META_K] : 0) > QR_HEAVY_K;
+        if (!heavy && threadIdx.x >= HALF) return false;
+    } else if ((int) blockIdx.x < 2 * H) {
+        idx = blockIdx.x >> 1;
+        side = blockIdx.x & 1;
+        heavy = true;
+    } else if (pair) {
+        idx = H + ((int) blockIdx.x - 2 * H);
+        half = side = threadIdx.x / HALF;
+        heavy = false;
+        if (idx >= nup) return false;
+    } else {
+        idx = H + (((int) blockIdx.x - 2 * H) >> 1);
+        side = ((int) blockIdx.x - 2 * H) & 1;
+        heavy = false;
+        if (idx >= nup || threadIdx.x >= HALF) return false;
+    }
+    slot = ws.heavy(idx);
+    return true;
+}
+
+// grid = 2 * n (an upper bound on the CTAs the split needs).
+__global__ void __launch_bounds__(QRD_THREADS, 1) qr_kernel_df(Workspace ws, int nup, int team_doubles, int pair) {
+    extern __shared__ double smq[];
+    __shared__ int s_emax[2];
+    int slot, side, half;
+    bool heavy;
+    if (!qr_assign(ws, nup, pair, slot, side, half, heavy)) return;
+    if (heavy) qr_side_df(Team<QRD_THREADS>{(int) threadIdx.x, 1}, ws, slot, side, smq, s_emax[0]);
+    else
+        qr_side_df(Team<QRD_THREADS / 2>{(int) threadIdx.x % (QRD_THREADS / 2), 1 + half}, ws, slot, side,
+                   smq + (size_t) half * team_doubles, s_emax[half]);
+}
+
+__global__ void __launch_bounds__(QRD_THREADS, 1) apply_q_kernel_df(const DevUpdate *ups, Workspace ws, int nup,
+                                                                   int team_doubles, int pair) {
+    extern __shared__ double smq[];
+    __shared__ int s_emax[2];
+    int slot, side, half;
+    bool heavy;
+    if (!qr_assign(ws, nup, pair, slot, side, half, heavy)) return;
+    if (heavy) apply_q_side_df(Team<QRD_THREADS>{(int) threadIdx.x, 1}, ups, ws, slot, side, smq, s_emax[0]);
+    else
+        apply_q_side_df(Team<QRD_THREADS / 2>{(int) threadIdx.x % (QRD_THREADS / 2), 1 + half}, ups, ws, slot, side,
+                        smq + (size_t) half * team_doubles, s_emax[half]);
 }
 
 }  // namespace
@@ -619,11 +704,24 @@ size_t qr_smem_bytes(int ld, int kmax) {
     return sizeof(double) * ((size_t) NB * ldp + (size_t) NB * ldw + 2 * NB * NB + 64 + NB);
 }
 
+// Whether two teams' panel buffers fit one CTA of the mixed-form kernels.
+static bool qr_pair_fits(size_t team_bytes) {
+    static int optin = 0;
+    if (!optin) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    return 2 * team_bytes + 256 <= (size_t) optin;
+}
+
 void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st) {
     const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
     if (mixed) {
-        cudaFuncSetAttribute(qr_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-        qr_kernel_df<<<2 * n, QR_THREADS, smem, st>>>(ws);
+        const int pair = qr_pair_fits(smem) ? 1 : 0;
+        const size_t cta = pair ? 2 * smem : smem;
+        cudaFuncSetAttribute(qr_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) cta);
+        qr_kernel_df<<<2 * n, QRD_THREADS, cta, st>>>(ws, n, (int) (smem / sizeof(double)), pair);
     } else {
         cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
         qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws);
@@ -633,8 +731,10 @@ void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st) {
 void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, bool mixed, cudaStream_t st) {
     if (mixed) {
         const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
-        cudaFuncSetAttribute(apply_q_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-        apply_q_kernel_df<<<2 * n, QR_THREADS, smem, st>>>(ups, ws);
+        const int pair = qr_pair_fits(smem) ? 1 : 0;
+        const size_t cta = pair ? 2 * smem : smem;
+        cudaFuncSetAttribute(apply_q_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) cta);
+        apply_q_kernel_df<<<2 * n, QRD_THREADS, cta, st>>>(ups, ws, n, (int) (smem / sizeof(double)), pair);
         return;
     }
     const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
