@@ -15,8 +15,12 @@ every k step, as the reference driver does), starting from the same C every step
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line (rank 0).  Inputs (A, B, C: ~1.4 GB each) exceed L2, so no flush is
-needed between steps.  The reference arm times the CPU oracle port (numpy + LAPACK) on the
-host cores over a seeded sample of C tiles, each with its full 32-update k-chain.
+needed between steps.  "value" times the multiply on device-resident tiles; "e2e" times the same
+multiply with the host's pinned A and C copied in and C copied out every step, in the
+rank-trimmed transfer format (hcgb_pack_tiles: only the factor columns the ranks use), and
+checks that the copied-out result equals the device-resident run's.  The reference arm times the
+CPU oracle port (numpy + LAPACK) on the host cores over a seeded sample of C tiles, each with its
+full 32-update k-chain.
 """
 from __future__ import annotations
 
@@ -311,29 +315,43 @@ def gpu_arm(args, rank, world, local):
     ctx.set_concurrency(args.groups)
     serial_ms = sum(v[0] for v in stages.values())
 
-    # ---- end to end through the public API: host (pinned) inputs in, result back to the host
-    a_pin = torch.from_numpy(a_host).pin_memory()
-    c_pin = torch.from_numpy(c_host).pin_memory()
+    # ---- end to end through the public API: host (pinned) inputs in, result back to the host.
+    #      Tiles travel in the rank-trimmed transfer format (hcgb_pack_tiles): the host holds A and
+    #      C packed (only the columns their ranks use); every step copies them in, unpacks them on
+    #      the device, multiplies (B = A, as in the device-resident run: one copy serves both
+    #      operands), packs C, reads the packed size and copies C and its ranks out.
+    Ae = T.TileMatrix(nt, nt, nb, A.kinds, maxr)
+    Ce = T.TileMatrix(nt, nt, nb, C0.kinds, maxr)
+    a_pk = torch.from_numpy(Ae.host_pack(a_host, a_ranks)).pin_memory()
+    c_pk = torch.from_numpy(Ce.host_pack(c_host, c_ranks)).pin_memory()
     ar_pin = torch.from_numpy(a_ranks).pin_memory()
     cr_pin = torch.from_numpy(c_ranks).pin_memory()
-    out_pin = torch.empty_like(c_pin).pin_memory()
+    a_dev = torch.empty(a_pk.numel(), dtype=torch.float64, device="cuda")
+    c_dev = torch.empty(c_pk.numel(), dtype=torch.float64, device="cuda")
+    out_dev = torch.empty(Ce.arena.numel(), dtype=torch.float64, device="cuda")
+    offs = [torch.empty(nt * nt + 1, dtype=torch.int64, device="cuda") for _ in range(3)]
+    out_pin = torch.empty(Ce.arena.numel(), dtype=torch.float64).pin_memory()
     outr_pin = torch.empty_like(cr_pin).pin_memory()
-    Ae = T.TileMatrix(nt, nt, nb, A.kinds, maxr)
-    Be = T.TileMatrix(nt, nt, nb, A.kinds, maxr)
-    Ce = T.TileMatrix(nt, nt, nb, C0.kinds, maxr)
-    h2d = 2 * (a_pin.numel() * 8 + ar_pin.numel() * 4) + c_pin.numel() * 8 + cr_pin.numel() * 4
-    d2h = out_pin.numel() * 8 + outr_pin.numel() * 4
+    total_pin = torch.empty(1, dtype=torch.int64).pin_memory()
+    moved = {}
 
     def e2e_step():
-        Ae.arena.copy_(a_pin, non_blocking=True)
         Ae.ranks.copy_(ar_pin, non_blocking=True)
-        Be.arena.copy_(a_pin, non_blocking=True)
-        Be.ranks.copy_(ar_pin, non_blocking=True)
-        Ce.arena.copy_(c_pin, non_blocking=True)
+        a_dev.copy_(a_pk, non_blocking=True)
+        Ae.unpack(a_dev, offs[0])
         Ce.ranks.copy_(cr_pin, non_blocking=True)
-        T.tlr_gemm(1.0, Ae, Be, 1.0, Ce, params, ctx=T.run_context(local))
-        out_pin.copy_(Ce.arena, non_blocking=True)
+        c_dev.copy_(c_pk, non_blocking=True)
+        Ce.unpack(c_dev, offs[1])
+        T.tlr_gemm(1.0, Ae, Ae, 1.0, Ce, params, ctx=T.run_context(local))
+        Ce.pack(out_dev, offs[2])
         outr_pin.copy_(Ce.ranks, non_blocking=True)
+        total_pin.copy_(offs[2][-1:], non_blocking=True)
+        torch.cuda.current_stream().synchronize()  # the packed size of the result
+        total = int(total_pin[0])
+        out_pin[:total].copy_(out_dev[:total], non_blocking=True)
+        moved["h2d"] = a_pk.numel() * 8 + c_pk.numel() * 8 + 4 * (ar_pin.numel() + cr_pin.numel())
+        moved["d2h"] = total * 8 + 4 * outr_pin.numel() + 8
+        moved["total"] = total
 
     e2e_step()
     torch.cuda.synchronize()
@@ -347,6 +365,10 @@ def gpu_arm(args, rank, world, local):
     torch.cuda.synchronize()
     e2e_ms = e2[0].elapsed_time(e2[1]) / args.steps
     e2e_value, e2e_ms = job_throughput(e2e_ms, n_updates, device="cuda")
+    h2d, d2h = moved["h2d"], moved["d2h"]
+    # the host copy of the result against the device-resident run's result (same multiply)
+    e2e_matches = bool(np.array_equal(out_pin[:moved["total"]].numpy(),
+                                      Cw.host_pack(Cw.arena.cpu().numpy(), Cw.ranks.cpu().numpy())))
 
     if rank != 0:
         return 0
@@ -404,7 +426,9 @@ def gpu_arm(args, rank, world, local):
                    "form": "plain_fp64" if args.mode == "plain" else "mixed (float-float QR, pivoted QR, Jacobi, Q application)",
                    "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups, "k_order": "ascending" if args.k_order == 0 else "cost-descending",
                    "l2": "inputs larger than L2 (A, C arenas 1.4 GB each), no flush"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "transfer": "rank-trimmed packed tiles (hcgb_pack_tiles / hcgb_unpack_tiles), pinned host buffers",
+                "result_matches_device_run": e2e_matches},
         "roofline": {"bound": ("fp64_equivalent" if args.mode == "mixed" and dom in ("core_svd", "qr", "apply_q")
                                else ("tensor" if dom in tensor_stages else "fp64_simt")), "kernel": dom,
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,

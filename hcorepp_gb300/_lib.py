@@ -105,6 +105,9 @@ def lib():
         L.hcgb_tile_gemm_noalloc.argtypes = [C.c_double, C.POINTER(Tile), C.POINTER(Tile), C.c_double,
                                              C.POINTER(Tile), C.POINTER(Params), vp, vp]
         L.hcgb_tile_gemm_noalloc.restype = C.c_int
+        for nm in ("hcgb_pack_tiles", "hcgb_unpack_tiles"):
+            getattr(L, nm).argtypes = [vp, ip, C.POINTER(Tile), vp, vp]
+            getattr(L, nm).restype = C.c_int
         for name in ("hcgb_context_create", "hcgb_context_destroy", "hcgb_context_set_stream", "hcgb_sync",
                      "hcgb_gemm_batch", "hcgb_tlr_gemm", "hcgb_tile_gemm", "hcgb_profile_enable",
                      "hcgb_profile_reset", "hcgb_profile_read", "hcgb_fp64_peak", "hcgb_set_concurrency"):

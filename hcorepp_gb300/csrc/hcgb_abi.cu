@@ -34,6 +34,8 @@ struct hcgb_context {
     int oz = 1;       // large factor products on the 16-bit tensor cores (FP64-accurate splitting)
     std::vector<cudaStream_t> group_streams;
     std::vector<cudaEvent_t> group_events;  // [0] fork, [1..] joins
+    void *pack_desc = nullptr;  // DevTile[] of hcgb_pack_tiles / hcgb_unpack_tiles
+    size_t pack_desc_bytes = 0;
 };
 
 namespace {
@@ -303,6 +305,7 @@ int hcgb_context_destroy(hcgb_context *ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->desc) cudaFree(ctx->desc);
+    if (ctx->pack_desc) cudaFree(ctx->pack_desc);
     if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
     for (auto &g : ctx->ev_pending)
@@ -395,29 +398,39 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
             return HCGB_OK;
         };
         // gather device ranks of every compressed tile with one synchronisation
-        std::vector<const int *> src;
         std::vector<int> ra((size_t) mt * kt), rb((size_t) kt * nt), rcv((size_t) n);
         for (size_t q = 0; q < ra.size(); q++) rank_of(a_grid[q], &ra[q]);
         for (size_t q = 0; q < rb.size(); q++) rank_of(b_grid[q], &rb[q]);
         for (size_t q = 0; q < rcv.size(); q++) rank_of(c_grid[q], &rcv[q]);
-        const size_t ntot = ra.size() + rb.size() + rcv.size();
-        int rc0;
-        if ((rc0 = ensure_stage(ctx, sizeof(int) * ntot))) return rc0;
-        int *hst = static_cast<int *>(ctx->stage);
-        auto fetch = [&](const hcgb_tile *grid, std::vector<int> &dst, size_t off) -> int {
-            for (size_t q = 0; q < dst.size(); q++)
-                if (compressed(grid[q].kind))
-                    HCGB_CUDA(ctx, cudaMemcpyAsync(hst + off + q, grid[q].rank, sizeof(int), cudaMemcpyDeviceToHost,
-                                                   ctx->stream));
-            return HCGB_OK;
+        // The device ranks of every compressed tile, gathered by one kernel and read with one copy.
+        std::vector<const int *> ptrs;
+        std::vector<int *> dst;
+        auto collect = [&](const hcgb_tile *grid, std::vector<int> &v) {
+            for (size_t q = 0; q < v.size(); q++)
+                if (compressed(grid[q].kind)) {
+                    ptrs.push_back(grid[q].rank);
+                    dst.push_back(&v[q]);
+                }
         };
-        if ((rc0 = fetch(a_grid, ra, 0)) || (rc0 = fetch(b_grid, rb, ra.size())) ||
-            (rc0 = fetch(c_grid, rcv, ra.size() + rb.size())))
-            return rc0;
-        HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        for (size_t q = 0; q < ra.size(); q++) if (ra[q] < 0) ra[q] = hst[q];
-        for (size_t q = 0; q < rb.size(); q++) if (rb[q] < 0) rb[q] = hst[ra.size() + q];
-        for (size_t q = 0; q < rcv.size(); q++) if (rcv[q] < 0) rcv[q] = hst[ra.size() + rb.size() + q];
+        collect(a_grid, ra);
+        collect(b_grid, rb);
+        collect(c_grid, rcv);
+        const size_t np = ptrs.size();
+        if (np) {
+            const size_t pb = sizeof(const int *) * np, ib = sizeof(int) * np;
+            int rc0;
+            if ((rc0 = ensure_device(ctx, &ctx->pack_desc, &ctx->pack_desc_bytes, pb + ib))) return rc0;
+            if ((rc0 = ensure_stage(ctx, pb + ib))) return rc0;
+            std::memcpy(ctx->stage, ptrs.data(), pb);
+            auto *dptrs = static_cast<const int **>(ctx->pack_desc);
+            int *dvals = reinterpret_cast<int *>(static_cast<char *>(ctx->pack_desc) + pb);
+            HCGB_CUDA(ctx, cudaMemcpyAsync(ctx->pack_desc, ctx->stage, pb, cudaMemcpyHostToDevice, ctx->stream));
+            launch_gather_ranks(dptrs, (int) np, dvals, ctx->stream);
+            int *hst = reinterpret_cast<int *>(static_cast<char *>(ctx->stage) + pb);
+            HCGB_CUDA(ctx, cudaMemcpyAsync(hst, dvals, ib, cudaMemcpyDeviceToHost, ctx->stream));
+            HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            for (size_t q = 0; q < np; q++) *dst[q] = hst[q];
+        }
         for (int idx = 0; idx < n; idx++) {
             const int i = idx % mt, j = idx / mt;
             if (!compressed(c_grid[idx].kind)) continue;
@@ -867,6 +880,48 @@ extern "C" int hcgb_fill_triangle(hcgb_context *ctx, int uplo, int n, double *A,
     launch_fill_triangle(uplo, n, A, lda, value, ctx->stream);
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
+}
+
+namespace {
+
+int pack_common(hcgb_context *ctx, int count, const hcgb_tile *tiles, double *packed, long long *offsets,
+                bool unpack) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (count < 0 || (count > 0 && (!tiles || !packed || !offsets)) || (count == 0 && !offsets))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_pack_tiles: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (count == 0) {
+        HCGB_CUDA(ctx, cudaMemsetAsync(offsets, 0, sizeof(long long), ctx->stream));
+        return HCGB_OK;
+    }
+    std::vector<DevTile> dv((size_t) count);
+    for (int t = 0; t < count; t++) {
+        int rc = check_tile(ctx, tiles[t], "tile");
+        if (rc) return rc;
+        dv[t] = to_dev(tiles[t]);
+    }
+    const size_t bytes = sizeof(DevTile) * dv.size();
+    int rc = ensure_device(ctx, &ctx->pack_desc, &ctx->pack_desc_bytes, bytes);
+    if (rc) return rc;
+    if ((rc = ensure_stage(ctx, bytes))) return rc;
+    std::memcpy(ctx->stage, dv.data(), bytes);
+    HCGB_CUDA(ctx, cudaMemcpyAsync(ctx->pack_desc, ctx->stage, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
+    launch_pack(static_cast<const DevTile *>(ctx->pack_desc), count, offsets, packed, unpack, ctx->stream);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+}  // namespace
+
+extern "C" int hcgb_pack_tiles(hcgb_context *ctx, int count, const hcgb_tile *tiles, double *packed_dev,
+                               long long *offsets_dev) {
+    return pack_common(ctx, count, tiles, packed_dev, offsets_dev, false);
+}
+
+extern "C" int hcgb_unpack_tiles(hcgb_context *ctx, int count, const hcgb_tile *tiles, const double *packed_dev,
+                                 long long *offsets_dev) {
+    return pack_common(ctx, count, tiles, const_cast<double *>(packed_dev), offsets_dev, true);
 }
 
 extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *grid, const hcgb_params *params,

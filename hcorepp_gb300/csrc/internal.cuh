@@ -161,6 +161,8 @@ void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Worksp
 // ws.order <- updates sorted by decreasing stack width k (0 for a dense C; ties by index); needs
 // ws.order != nullptr.  The key ignores the status, so it cannot change while the heavy stages run.
 void launch_order(int n, Workspace ws, cudaStream_t st);
+// out[i] = *ptrs[i] (device rank ints gathered for one host read).
+void launch_gather_ranks(const int *const *ptrs, int n, int *out, cudaStream_t st);
 // Batched products: sched = device scratch of 2 * njobs + 2 ints (tile prefix sums), njobs <= 4096.
 void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t st);
 void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int sms, cudaStream_t st);
@@ -193,6 +195,9 @@ void launch_trsm(int side, int uplo, int trans, int diag, int m, int n, double a
                  double *B, int ldb, cudaStream_t st);
 void launch_syrk(int uplo, int trans, int n, int k, double alpha, const double *A, int lda, double beta, double *C,
                  int ldc, cudaStream_t st);
+
+// Rank-trimmed packing of a tile list (pack.cu): offsets (n + 1) and the packed copy, or back.
+void launch_pack(const DevTile *tiles, int n, long long *offsets, double *packed, bool unpack, cudaStream_t st);
 
 size_t qr_smem_bytes(int ld, int kmax);
 size_t svd_smem_bytes(int kmax);

@@ -560,6 +560,15 @@ void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspa
     plan_kernel<<<(n + 127) / 128, 128, 0, st>>>(ups, n, alpha, beta, ws, p, jobs);
 }
 
+__global__ void __launch_bounds__(256) gather_ranks_kernel(const int *const *ptrs, int n, int *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = *ptrs[i];
+}
+
+void launch_gather_ranks(const int *const *ptrs, int n, int *out, cudaStream_t st) {
+    if (n > 0) gather_ranks_kernel<<<(n + 255) / 256, 256, 0, st>>>(ptrs, n, out);
+}
+
 void launch_order(int n, Workspace ws, cudaStream_t st) {
     order_kernel<<<1, 1024, 0, st>>>(n, ws);
 }

@@ -122,9 +122,9 @@ __device__ void factor_panel_df(const TM &tm, df *Ps, int ldp, int mr, int nbp, 
         if (tau.h != 0.f) {
             for (int c = j + 1 + warp; c < nbp; c += nw) {
                 df *y = Ps + (size_t) c * ldp;
-                df w = lane == 0 ? y[j] : df_f(0.f);
-                for (int r = j + 1 + lane; r < mr; r += 32) w = df_fma(x[r], y[r], w);
-                w = df_mul(df_group_sum(w, 32), tau);
+                df_acc wa = df_acc_init(lane == 0 ? y[j] : df_f(0.f));
+                for (int r = j + 1 + lane; r < mr; r += 32) df_acc_fma(wa, x[r], y[r]);
+                const df w = df_mul(df_group_sum(df_acc_value(wa), 32), tau);
                 if (lane == 0) y[j] = df_add(y[j], -w);
                 const df mw = -w;
                 for (int r = j + 1 + lane; r < mr; r += 32) y[r] = df_fma(mw, x[r], y[r]);
@@ -391,18 +391,18 @@ __device__ void apply_block_reflector_df(const TM &tm, const df *Ps, int ldp, co
         df *Xc = X + (size_t) c0 * ldx;
         // A: W = V^T X, a warp per column, lanes over rows
         for (int c = warp; c < ntc; c += nw) {
-            df acc[NB];
+            df_acc acc[NB];
 #pragma unroll
-            for (int i = 0; i < NB; i++) acc[i] = df_f(0.f);
+            for (int i = 0; i < NB; i++) acc[i] = df_acc{0.f, 0.f};
             const df *xc = Xc + (size_t) c * ldx;
             for (int r = lane; r < mr; r += 32) {
                 const df xv = xc[r];
 #pragma unroll
-                for (int i = 0; i < NB; i++) acc[i] = df_fma(Ps[(size_t) i * ldp + r], xv, acc[i]);
+                for (int i = 0; i < NB; i++) df_acc_fma(acc[i], Ps[(size_t) i * ldp + r], xv);
             }
 #pragma unroll
             for (int i = 0; i < NB; i++) {
-                const df v = df_group_sum(acc[i], 32);
+                const df v = df_group_sum(df_acc_value(acc[i]), 32);
                 if (lane == 0) Ws[i * ldw + c] = v;
             }
         }
@@ -431,10 +431,10 @@ __device__ void apply_block_reflector_df(const TM &tm, const df *Ps, int ldp, co
         // C: X += V W, a thread per element (rows fastest: coalesced)
         for (int e = tm.tid; e < mr * ntc; e += tm.nth) {
             const int r = e % mr, c = e / mr;
-            df x = Xc[r + (size_t) c * ldx];
+            df_acc x = df_acc_init(Xc[r + (size_t) c * ldx]);
 #pragma unroll
-            for (int i = 0; i < NB; i++) x = df_fma(Ps[(size_t) i * ldp + r], Ws[i * ldw + c], x);
-            Xc[r + (size_t) c * ldx] = x;
+            for (int i = 0; i < NB; i++) df_acc_fma(x, Ps[(size_t) i * ldp + r], Ws[i * ldw + c]);
+            Xc[r + (size_t) c * ldx] = df_acc_value(x);
         }
         tm.sync();
     }

@@ -287,7 +287,7 @@ __device__ int jacobi_sweep_df(const TM &tm, df *X, int ldx, int rows, int ncols
             df *x = X + (size_t) (act ? i : 0) * ldx;
             df *y = X + (size_t) (act ? j : 0) * ldx;
             df xr[RPL], yr[RPL];
-            df c = df_f(0.f);
+            df_acc ca{0.f, 0.f};
 #pragma unroll
             for (int q = 0; q < RPL; q++) {
                 xr[q] = yr[q] = df_f(0.f);
@@ -297,10 +297,10 @@ __device__ int jacobi_sweep_df(const TM &tm, df *X, int ldx, int rows, int ncols
                         xr[q] = x[r];
                         yr[q] = y[r];
                     }
-                    c = df_fma(xr[q], yr[q], c);
+                    df_acc_fma(ca, xr[q], yr[q]);
                 }
             }
-            c = group_sum(c, G);
+            const df c = group_sum(df_acc_value(ca), G);
             df a = df_f(0.f), b = df_f(0.f), di = df_f(1.f), dj = df_f(1.f);
             if (act) {
                 a = nrm[i];
@@ -692,9 +692,9 @@ __device__ int qrcp_truncated_df(const TM &tm, df *A, int lda, int mrows, int nc
             df *y = A + (size_t) j * lda;
             df w = df_f(0.f);
             if (has_tau) {
-                w = lane == 0 ? y[s] : df_f(0.f);
-                for (int i = s + 1 + lane; i < mrows; i += 32) w = df_fma(x[i], y[i], w);
-                w = df_mul(group_sum(w, 32), tau);
+                df_acc wa = df_acc_init(lane == 0 ? y[s] : df_f(0.f));
+                for (int i = s + 1 + lane; i < mrows; i += 32) df_acc_fma(wa, x[i], y[i]);
+                w = df_mul(group_sum(df_acc_value(wa), 32), tau);
                 const df mw = -w;
                 for (int i = s + 1 + lane; i < mrows; i += 32) y[i] = df_fma(mw, x[i], y[i]);
             }

@@ -391,6 +391,15 @@ class TileMatrix:
                               rank_buf=self.ranks[idx:idx + 1], vt=self.vt)
 
     def c_grid(self):
+        """The tile descriptors (device pointers into the arena and the rank array, which never move),
+        built once and reused."""
+        cached = getattr(self, "_grid", None)
+        if cached is not None:
+            return cached
+        self._grid = self._build_grid()
+        return self._grid
+
+    def _build_grid(self):
         nb = self.nb
         arr = (L.Tile * (self.mt * self.nt))()
         base = self.arena.data_ptr()
@@ -405,6 +414,38 @@ class TileMatrix:
                     arr[idx] = L.Tile(ptr, rbase + 4 * idx, nb, nb, self.max_rank,
                                       L.COMPRESSED_VT if self.vt else L.COMPRESSED)
         return arr
+
+    # ---- rank-trimmed transfer format (hcgb_pack_tiles): tiles in index order (i + j * mt), each
+    #      dense tile nb x nb, each compressed tile U (nb x rank) then its V region (rank * nb values)
+    def pack(self, packed: torch.Tensor, offsets: torch.Tensor, ctx: L.Context | None = None):
+        """Pack the used part of every tile into the device buffer `packed` (float64, at least
+        ``self.arena.numel()`` values); `offsets` (int64, mt * nt + 1, device) receives each tile's
+        start and the total.  Asynchronous on torch's current stream."""
+        ctx = ctx or run_context()
+        grid = self.c_grid()
+        ctx.check(L.lib().hcgb_pack_tiles(ctx.handle, self.mt * self.nt, grid, _dptr(packed), _dptr(offsets)))
+
+    def unpack(self, packed: torch.Tensor, offsets: torch.Tensor, ctx: L.Context | None = None):
+        """Inverse of pack; ``self.ranks`` must already hold the packed tiles' ranks."""
+        ctx = ctx or run_context()
+        grid = self.c_grid()
+        ctx.check(L.lib().hcgb_unpack_tiles(ctx.handle, self.mt * self.nt, grid, _dptr(packed), _dptr(offsets)))
+
+    def host_pack(self, arena: np.ndarray, ranks: np.ndarray) -> np.ndarray:
+        """The same format built on the host from a host copy of the arena and the ranks."""
+        nb = self.nb
+        parts = []
+        for idx in range(self.mt * self.nt):
+            i, j = idx % self.mt, idx // self.mt
+            o = int(self.offsets[idx])
+            if self.kinds[i][j] == L.DENSE:
+                parts.append(arena[o:o + nb * nb])
+            else:
+                r = int(ranks[idx])
+                parts.append(arena[o:o + nb * r])
+                vo = o + nb * self.max_rank
+                parts.append(arena[vo:vo + r * nb])
+        return np.concatenate(parts) if parts else np.zeros(0)
 
     def set_tile(self, i, j, dense=None, u=None, v=None):
         t = self.tile(i, j)

@@ -215,6 +215,21 @@ int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *grid, const h
  * applies after a compressed-A update (src/api/HCore.cpp:555-563).  Asynchronous. */
 int hcgb_fill_triangle(hcgb_context *ctx, int uplo, int n, double *A, int lda, double value);
 
+/* Rank-trimmed transfer packing of `count` tiles (the batched device side of TilePacker,
+ * include/hcorepp/operators/interface/TilePacker.hpp:18-62, whose PackTile / UnPackTile move one
+ * tile at its full capacity): each tile's used part -- dense: rows x cols; compressed: U (rows x
+ * rank) then V (rank x cols); compressed_vt: U then W = V^T (cols x rank) -- concatenated in list
+ * order into the device buffer `packed_dev`.  offsets_dev (device, count + 1 long long) receives
+ * each tile's start (in doubles) and, last, the total, computed on the device from the tiles'
+ * device ranks, so a caller reads the total (8 bytes) before copying the packed data out.
+ * packed_dev must hold the total; the sum of the tiles' capacities always suffices.
+ * hcgb_unpack_tiles is the inverse: the ranks must already be in the tiles' rank ints.
+ * Asynchronous on the context stream. */
+int hcgb_pack_tiles(hcgb_context *ctx, int count, const hcgb_tile *tiles, double *packed_dev,
+                    long long *offsets_dev);
+int hcgb_unpack_tiles(hcgb_context *ctx, int count, const hcgb_tile *tiles, const double *packed_dev,
+                      long long *offsets_dev);
+
 /* Stage timing with CUDA events on the context stream (the GB300 replacement of the reference's
  * DebuggingTimer snapshots, src/helpers/debugging-timer/ActiveTimer.cpp:47-60).  While enabled,
  * every pipeline stage is bracketed by events; hcgb_profile_read synchronises the stream and

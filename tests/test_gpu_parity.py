@@ -319,6 +319,40 @@ def test_tile_packer_gemm_through_packed_tiles(T):
     np.testing.assert_array_equal(outs[0][2], outs[1][2])
 
 
+@pytest.mark.parametrize("vt", [False, True])
+def test_rank_trimmed_pack_roundtrip(T, vt):
+    """hcgb_pack_tiles / hcgb_unpack_tiles: offsets from the device ranks (rank 0 and full capacity
+    included), packed bytes equal to the host-side format, and unpacking into a fresh tile matrix
+    restores every used value bit for bit."""
+    import torch
+    from hcorepp_gb300 import _lib as L
+    rng = np.random.default_rng(31 + vt)
+    mt, nt, nb, mr = 3, 4, 64, 20
+    kinds = [[L.DENSE if i == j else L.COMPRESSED for j in range(nt)] for i in range(mt)]
+    tm = T.TileMatrix(mt, nt, nb, kinds, mr, vt=vt)
+    tm.arena.copy_(torch.from_numpy(rng.standard_normal(tm.arena.numel())))
+    ranks = rng.integers(0, mr + 1, size=mt * nt).astype(np.int32)
+    ranks[1], ranks[2] = 0, mr
+    tm.ranks.copy_(torch.from_numpy(ranks))
+    packed = torch.full((tm.arena.numel(),), np.nan, dtype=torch.float64, device="cuda")
+    offs = torch.zeros(mt * nt + 1, dtype=torch.int64, device="cuda")
+    tm.pack(packed, offs)
+    torch.cuda.synchronize()
+    want = tm.host_pack(tm.arena.cpu().numpy(), ranks)
+    sizes = [nb * nb if kinds[idx % mt][idx // mt] == L.DENSE else 2 * nb * int(ranks[idx]) for idx in range(mt * nt)]
+    np.testing.assert_array_equal(offs.cpu().numpy(), np.concatenate([[0], np.cumsum(sizes)]))
+    total = int(offs[-1])
+    assert total == want.size
+    np.testing.assert_array_equal(packed[:total].cpu().numpy(), want)
+    tm2 = T.TileMatrix(mt, nt, nb, kinds, mr, vt=vt)
+    tm2.ranks.copy_(tm.ranks)
+    offs2 = torch.zeros_like(offs)
+    tm2.unpack(packed, offs2)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(offs2.cpu().numpy(), offs.cpu().numpy())
+    np.testing.assert_array_equal(tm2.host_pack(tm2.arena.cpu().numpy(), ranks), want)
+
+
 @pytest.mark.parametrize("scaled", [False, True])
 def test_tensor_core_products_fp64_accurate(T, scaled):
     """Dense products on the 16-bit tensor cores (error-free splitting) match an extended-precision
