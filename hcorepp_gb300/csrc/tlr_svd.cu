@@ -40,21 +40,10 @@ __device__ __forceinline__ T group_sum(T v, int G) {
     return v;
 }
 
-__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
-__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
-
-// a * b + c in the Jacobi element type.
-__device__ __forceinline__ double tfma(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ float tfma(float a, float b, float c) { return fmaf(a, b, c); }
-__device__ __forceinline__ df tfma(df a, df b, df c) { return df_fma(a, b, c); }
-
 template <>
 __device__ __forceinline__ df group_sum<df>(df v, int G) {
     return df_group_sum(v, G);
 }
-// Unit roundoff used for the noise floor of a Jacobi run in type T.
-template <typename T> __device__ __forceinline__ double unit_roundoff() { return DBL_EPSILON; }
-template <> __device__ __forceinline__ double unit_roundoff<df>() { return 3.552713678800501e-15; }  // 2^-48
 
 // Tangent of the Jacobi angle that orthogonalises a pair with squared norms a, b and inner
 // product c: zeta = (b - a) / (2 c), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)) (Rutishauser).
@@ -78,17 +67,16 @@ __device__ __forceinline__ float jacobi_tangent(double a, double b, double c) {
 // Squared column norms are tracked in nrm[] (a' = a - t c, b' = b + t c), so each pair costs one
 // inner product.  A pair is rotated when c^2 > tol2 a b and both columns are above the noise
 // floor `tiny`; columns below it hold only rounding errors of the larger ones.
-// With ACC the same rotations are accumulated into the columns of J (ncols x ncols, ld ldj).
 //
-// Without ACC the rotations are applied in scaled form (the idea of fast Givens rotations): column
-// i is stored as x_i with the true column d_i x_i, so the rotation
+// The rotations are applied in scaled form (the idea of fast Givens rotations): column i is
+// stored as x_i with the true column d_i x_i, so the rotation
 //   X_i' = cos (X_i - t X_j),  X_j' = cos (X_j + t X_i)
 // becomes x_i' = x_i - t (d_j / d_i) x_j, x_j' = x_j + t (d_i / d_j) x_i, d' = cos d: one FMA per
 // element instead of a multiply and an FMA.  d and 1/d live in dsc[0..) and dsc[dstride..);
 // the caller folds them back into the columns at the start of every sweep.
-template <typename T, int G, int RPL, bool ACC, class TM>
-__device__ int jacobi_sweep(const TM &tm, T *X, int ldx, int rows, int ncols, double *nrm, double tol2, double tiny, int n2,
-                            T *J, int ldj, double *dsc, int dstride) {
+template <int G, int RPL, class TM>
+__device__ int jacobi_sweep(const TM &tm, double *X, int ldx, int rows, int ncols, double *nrm, double tol2,
+                            double tiny, int n2, double *dsc, int dstride) {
     const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     constexpr int PPW = 32 / G;
     const int gl = lane % G, grp = lane / G;
@@ -104,46 +92,44 @@ __device__ int jacobi_sweep(const TM &tm, T *X, int ldx, int rows, int ncols, do
                 jacobi_pair(t, pp, n2, i, j);
                 act = i < ncols && j < ncols;
             }
-            T *x = X + (size_t) (act ? i : 0) * ldx;
-            T *y = X + (size_t) (act ? j : 0) * ldx;
-            T xr[RPL], yr[RPL];
-            T c = T(0);
+            double *x = X + (size_t) (act ? i : 0) * ldx;
+            double *y = X + (size_t) (act ? j : 0) * ldx;
+            double xr[RPL], yr[RPL];
+            double c = 0.0;
 #pragma unroll
             for (int q = 0; q < RPL; q++) {
-                xr[q] = yr[q] = T(0);
+                xr[q] = yr[q] = 0.0;
                 if (G * q < rows) {  // uniform across the warp: whole row slots beyond `rows` are skipped
                     const int r = gl + G * q;
                     if (act && r < rows) {
                         xr[q] = x[r];
                         yr[q] = y[r];
                     }
-                    c = tfma(xr[q], yr[q], c);
+                    c = fma(xr[q], yr[q], c);
                 }
             }
             c = group_sum(c, G);
             const double a = act ? nrm[i] : 0.0, b = act ? nrm[j] : 0.0;
             double di = 1.0, dj = 1.0;
-            if (!ACC && act) {
+            if (act) {
                 di = dsc[i];
                 dj = dsc[j];
             }
-            const double cd = ACC ? (double) c : (double) c * di * dj;  // true inner product
-            (void) cd;
+            const double cd = c * di * dj;  // true inner product
             const bool rot = act && a > tiny && b > tiny && cd * cd > tol2 * a * b;
-            if constexpr (!ACC) {
-              if (rot) {
+            if (rot) {
                 const double tt = (double) jacobi_tangent(a, b, cd);
                 const double q = fma(tt, tt, 1.0);
                 const double cs = rsqrt(q);
                 const double dvi = dsc[dstride + i], dvj = dsc[dstride + j];
-                const T t1 = (T) (tt * dj * dvi), t2 = (T) (tt * di * dvj);
+                const double t1 = tt * dj * dvi, t2 = tt * di * dvj;
 #pragma unroll
                 for (int q2 = 0; q2 < RPL; q2++) {
                     if (G * q2 < rows) {
                         const int r = gl + G * q2;
                         if (r < rows) {
-                            x[r] = tfma(-t1, yr[q2], xr[q2]);
-                            y[r] = tfma(t2, xr[q2], yr[q2]);
+                            x[r] = fma(-t1, yr[q2], xr[q2]);
+                            y[r] = fma(t2, xr[q2], yr[q2]);
                         }
                     }
                 }
@@ -156,35 +142,6 @@ __device__ int jacobi_sweep(const TM &tm, T *X, int ldx, int rows, int ncols, do
                     dsc[dstride + j] = dvj * q * cs;
                     rotations++;
                 }
-              }
-            } else if (rot) {
-                const float tf = jacobi_tangent(a, b, cd);
-                const T tt = (T) tf;
-                const T cs = rsqrt_t(fma(tt, tt, T(1)));
-                const T sn = cs * tt;
-#pragma unroll
-                for (int q = 0; q < RPL; q++) {
-                    if (G * q < rows) {
-                        const int r = gl + G * q;
-                        if (r < rows) {
-                            x[r] = fma(cs, xr[q], -sn * yr[q]);
-                            y[r] = fma(sn, xr[q], cs * yr[q]);
-                        }
-                    }
-                }
-                if (ACC) {
-                    T *ji = J + (size_t) i * ldj, *jj = J + (size_t) j * ldj;
-                    for (int r = gl; r < ncols; r += G) {
-                        const T u = ji[r], v = jj[r];
-                        ji[r] = fma(cs, u, -sn * v);
-                        jj[r] = fma(sn, u, cs * v);
-                    }
-                }
-                if (gl == 0) {
-                    nrm[i] = a - (double) tt * cd;
-                    nrm[j] = b + (double) tt * cd;
-                    rotations++;
-                }
             }
         }
         tm.sync();
@@ -192,41 +149,37 @@ __device__ int jacobi_sweep(const TM &tm, T *X, int ldx, int rows, int ncols, do
     return rotations;
 }
 
-// Jacobi iteration on X: exact squared column norms at the start of every sweep, then sweeps
-// until no pair rotates (or max_sweeps).
-template <typename T, int G, int RPL, bool ACC, class TM>
-__device__ void jacobi(const TM &tm, T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax, int *sweeps_out,
-                       bool *converged_out, double tol, int max_sweeps, T *J, int ldj, double *dsc, int dstride) {
+// Jacobi iteration on X: exact squared column norms at the start of every sweep (the scales of
+// the previous sweep folded into the columns), then sweeps until no pair rotates (or max_sweeps).
+template <int G, int RPL, class TM>
+__device__ void jacobi(const TM &tm, double *X, int ldx, int rows, int ncols, double *nrm, int *s_rot,
+                       double *s_amax, int *sweeps_out, bool *converged_out, double tol, int max_sweeps, double *dsc,
+                       int dstride) {
     const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     const double tol2 = tol * tol;
-    // Noise floor from double precision also for single-precision sweeps: X is graded (each column
-    // accurate relative to its own norm), so small columns are data, not rounding noise.
-    const double noise = unit_roundoff<T>() * (double) (rows > 1 ? rows : 1);
+    const double noise = DBL_EPSILON * (double) (rows > 1 ? rows : 1);
     const int n2 = ncols + (ncols & 1);
     int sweeps = 0;
     bool converged = ncols < 2;
-    if (!ACC) {
-        for (int j = tm.tid; j < ncols; j += tm.nth) dsc[j] = dsc[dstride + j] = 1.0;
-        tm.sync();
-    }
-    // Exact squared norms; the scales d of the previous sweep are folded into the columns.
+    for (int j = tm.tid; j < ncols; j += tm.nth) dsc[j] = dsc[dstride + j] = 1.0;
+    tm.sync();
     auto fold_and_norms = [&](double &amax) {
         for (int j = warp; j < ncols; j += nw) {
-            T *col = X + (size_t) j * ldx;
-            const double dj = ACC ? 1.0 : dsc[j];
+            double *col = X + (size_t) j * ldx;
+            const double dj = dsc[j];
             double sq = 0.0;
             for (int r = lane; r < rows; r += 32) {
-                double v = (double) col[r];
-                if (!ACC && dj != 1.0) {
+                double v = col[r];
+                if (dj != 1.0) {
                     v *= dj;
-                    col[r] = (T) v;
+                    col[r] = v;
                 }
                 sq = fma(v, v, sq);
             }
             sq = warp_sum(sq);
             if (lane == 0) {
                 nrm[j] = sq;
-                if (!ACC) dsc[j] = dsc[dstride + j] = 1.0;
+                dsc[j] = dsc[dstride + j] = 1.0;
             }
             amax = fmax(amax, sq);
         }
@@ -242,18 +195,16 @@ __device__ void jacobi(const TM &tm, T *X, int ldx, int rows, int ncols, double 
         if (lane == 0) atomicMax(reinterpret_cast<unsigned long long *>(s_amax), __double_as_longlong(amax));
         tm.sync();
         const double tiny = *s_amax * noise * noise;
-        const int rot = jacobi_sweep<T, G, RPL, ACC>(tm, X, ldx, rows, ncols, nrm, tol2, tiny, n2, J, ldj, dsc, dstride);
+        const int rot = jacobi_sweep<G, RPL>(tm, X, ldx, rows, ncols, nrm, tol2, tiny, n2, dsc, dstride);
         if (rot) atomicAdd(s_rot, rot);
         tm.sync();
         sweeps++;
         converged = (*s_rot == 0);
         tm.sync();
     }
-    if (!ACC) {  // a sweep limit can leave scales unfolded
-        double amax = 0.0;
-        fold_and_norms(amax);
-        tm.sync();
-    }
+    double amax = 0.0;
+    fold_and_norms(amax);  // a sweep limit can leave scales unfolded
+    tm.sync();
     *sweeps_out = sweeps;
     *converged_out = converged;
 }
@@ -420,19 +371,19 @@ __device__ void jacobi_df_dispatch(const TM &tm, df *X, int ldx, int rows, int n
     else jacobi_df<32, MAXRPL>(tm, X, ldx, rows, ncols, nrm, ds, dv, s_rot, s_amax, sweeps, conv, tol, max_sweeps);
 }
 
-template <typename T, bool ACC, int MAXRPL, class TM>
-__device__ void jacobi_dispatch(const TM &tm, T *X, int ldx, int rows, int ncols, double *nrm, int *s_rot, double *s_amax,
-                                int *sweeps, bool *conv, double tol, int max_sweeps, T *J, int ldj, double *dsc,
+template <int MAXRPL, class TM>
+__device__ void jacobi_dispatch(const TM &tm, double *X, int ldx, int rows, int ncols, double *nrm, int *s_rot,
+                                double *s_amax, int *sweeps, bool *conv, double tol, int max_sweeps, double *dsc,
                                 int dstride) {
     // Fewer lanes per pair put more pairs in one warp instruction, so the per-pair scalar work
     // (tangent, tests, norm updates) is shared by 2-4 pairs; RPL rows per lane stay in registers.
-    if (rows <= 32) jacobi<T, 4, 8, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 64) jacobi<T, 8, 8, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 128 && MAXRPL >= 16) jacobi<T, 8, 16, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 128) jacobi<T, 16, 8, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 256 && MAXRPL >= 16) jacobi<T, 16, 16, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else if (rows <= 256 || MAXRPL <= 8) jacobi<T, 32, 8, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
-    else jacobi<T, 32, MAXRPL, ACC>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, J, ldj, dsc, dstride);
+    if (rows <= 32) jacobi<4, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 64) jacobi<8, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 128 && MAXRPL >= 16) jacobi<8, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 128) jacobi<16, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 256 && MAXRPL >= 16) jacobi<16, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 256 || MAXRPL <= 8) jacobi<32, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else jacobi<32, MAXRPL>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
 }
 
 // Householder QR with column pivoting of A (mrows x ncols, ld lda) in place, stopped early once
@@ -929,8 +880,8 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
         }
         tm.sync();
     } else {
-        jacobi_dispatch<double, false, RPL>(tm, X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64,
-                                            MAX_JACOBI_SWEEPS, (double *) nullptr, 0, dsc, ws.kmax);
+        jacobi_dispatch<RPL>(tm, X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64, MAX_JACOBI_SWEEPS,
+                             dsc, ws.kmax);
     }
 
     const long long t3 = clock64();

@@ -60,3 +60,27 @@ def test_tile_packer_round_trip_on_host():
         T.TilePacker.PackTile(T.TileMetadata(40, 30, 14, 13, 40, "C", L.COMPRESSED), buf)
     with pytest.raises(ValueError):
         T.TilePacker.PackTile(T.TileMetadata(7, 9, 0, 0, 8, "C", L.DENSE), bd)
+
+
+def test_rank_trimmed_host_pack_layout():
+    """TileMatrix.host_pack (the host side of hcgb_pack_tiles' format): tiles in index order
+    (i + j * mt), a dense tile whole, a compressed tile's first rank columns of U followed by the
+    first rank * nb values of its V region; rank 0 contributes nothing."""
+    from hcorepp_gb300 import tiles as T
+    mt, nt, nb, mr = 2, 3, 8, 3
+    kinds = [[L.DENSE if i == j else L.COMPRESSED for j in range(nt)] for i in range(mt)]
+    tm = T.TileMatrix(mt, nt, nb, kinds, mr, device="cpu")
+    arena = np.arange(tm.arena.numel(), dtype=np.float64)
+    ranks = np.array([0, 2, 3, 0, 1, 1], dtype=np.int32)
+    got = tm.host_pack(arena, ranks)
+    want = []
+    for idx in range(mt * nt):
+        i, j = idx % mt, idx // mt
+        o = int(tm.offsets[idx])
+        if kinds[i][j] == L.DENSE:
+            want.append(arena[o:o + nb * nb])
+        else:
+            r = int(ranks[idx])
+            want += [arena[o:o + nb * r], arena[o + nb * mr:o + nb * mr + r * nb]]
+    np.testing.assert_array_equal(got, np.concatenate(want))
+    assert got.size == 2 * nb * nb + 2 * nb * (2 + 3 + 1 + 1)  # two dense tiles; compressed ranks 2, 3, 1, 1
