@@ -68,11 +68,15 @@ typedef struct {
     int mode;           /* hcgb_mode: arithmetic of the recompression core */
 } hcgb_params;
 
-/* HCGB_PLAIN_FP64: every stage in double precision.
- * HCGB_MIXED: the core SVD's Jacobi is preconditioned by single-precision sweeps (rotations
- * accumulated in single precision, applied once in double precision, then finished in double
- * precision); QR, products, Q application and the truncation test stay in double precision.
- * Singular values agree with the plain form to ~1e-6 relative; the product to working accuracy. */
+/* HCGB_PLAIN_FP64: the recompression (stack QR, core SVD, Q application) in double precision.
+ * HCGB_MIXED: the stack QR, the core SVD's pivoted QR and Jacobi sweeps and the panel-wise Q
+ * application in float-float arithmetic (a value is the unevaluated sum of two floats, 48-bit
+ * significand) on the FP32 pipe, each block scaled by an exact power of two first; the core
+ * product, the new factors, the truncation test and all factor products stay in double precision.
+ * Backward error of the float-float stages ~2^-48 relative: same ranks and product accuracy as the
+ * plain form at the accuracies this path is used at (>= 1e-12 relative), about twice as fast.
+ * In both forms the larger factor products run on the 16-bit tensor cores by FP64-accurate
+ * error-free splitting unless hcgb_set_tensor_products(ctx, 0). */
 typedef enum { HCGB_PLAIN_FP64 = 0, HCGB_MIXED = 1 } hcgb_mode;
 
 /* One tile update C <- alpha * A * B + beta * C (NoTrans operands). */
