@@ -501,28 +501,36 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     }
     const bool single = (G == 1);
     if (!single) HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[0], ctx->stream));
+    std::vector<Workspace> wgs((size_t) G);
     for (int g = 0; g < G; g++) {
-        const int ng = first[g + 1] - first[g];
         cudaStream_t st = single ? ctx->stream : ctx->group_streams[g];
         if (!single) HCGB_CUDA(ctx, cudaStreamWaitEvent(st, ctx->group_events[0], 0));
-        Workspace wg = ws;
+        Workspace &wg = wgs[g];
+        wg = ws;
         wg.base = ws.base + ws.slot_doubles * (size_t) first[g];
         wg.meta = ws.meta + (size_t) META_INTS * first[g];
         wg.order = ws.order + first[g];
-        for (int kk = 0; kk < kt; kk++) {
+    }
+    // Waves are issued round-robin over the groups, so every group starts at once instead of
+    // waiting for the host to enqueue the earlier groups' whole chains.
+    for (int kk = 0; kk < kt; kk++)
+        for (int g = 0; g < G; g++) {
+            const int ng = first[g + 1] - first[g];
+            cudaStream_t st = single ? ctx->stream : ctx->group_streams[g];
             const size_t off = (size_t) first[g] * kt + (size_t) kk * ng;
             BatchShape shw = shape_of(all.data() + off, ng);
             shw.ld = sh.ld;
             shw.kmax = sh.kmax;
             shw.rmax = sh.rmax;
             launch_pipeline(ctx, st, dups + off, djobs + JOBS_PER_UPDATE * (size_t) first[g],
-                            dsched + SCHED_INTS_PER_UPDATE * (size_t) first[g], ng, alpha, beta, wg, shw, p, info_dev);
+                            dsched + SCHED_INTS_PER_UPDATE * (size_t) first[g], ng, alpha, beta, wgs[g], shw, p,
+                            info_dev);
         }
-        if (!single) {
-            HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[g + 1], st));
+    if (!single)
+        for (int g = 0; g < G; g++) {
+            HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[g + 1], ctx->group_streams[g]));
             HCGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->group_events[g + 1], 0));
         }
-    }
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
 }
