@@ -19,7 +19,14 @@ ip = C.POINTER(C.c_int)
 
 
 def available() -> bool:
-    return os.path.exists(_PATH)
+    """Built here and loadable on this machine (the x86 build does not load on an Arm host)."""
+    if not os.path.exists(_PATH):
+        return False
+    try:
+        lib()
+    except OSError:
+        return False
+    return True
 
 
 def lib():
