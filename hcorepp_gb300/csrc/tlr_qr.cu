@@ -706,12 +706,12 @@ size_t qr_smem_bytes(int ld, int kmax) {
 
 // Whether two teams' panel buffers fit one CTA of the mixed-form kernels.
 static bool qr_pair_fits(size_t team_bytes) {
-    static int optin = 0;
-    if (!optin) {
-        int dev = 0;
+    static const int optin = [] {  // thread-safe one-time initialisation
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return v > 0 ? v : 48 * 1024;
+    }();
     return 2 * team_bytes + 256 <= (size_t) optin;
 }
 

@@ -982,13 +982,12 @@ namespace {
 // half of the per-block opt-in limit (less a reserve for the kernel's static shared variables), and
 // never below the aux arrays.
 int svd_team_doubles(int kmax) {
-    static int optin = 0;
-    if (!optin) {
-        int dev = 0;
+    static const int optin = [] {  // thread-safe one-time initialisation
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (optin <= 0) optin = 48 * 1024;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return v > 0 ? v : 48 * 1024;
+    }();
     const long aux = 6L * kmax + SVD_AUX_FIXED;
     const long want = aux + (long) kmax * kmax;
     const long cap = (optin - 256) / 2 / (long) sizeof(double);
