@@ -1,6 +1,7 @@
-// C ABI of libhcgb (declared in include/hcgb.h): contexts, workspace sizing and the
-// batched / tile-matrix / single-tile GEMM entry points.  Host code only; the kernels
-// live in tlr_plan.cu, tlr_qr.cu and tlr_svd.cu.
+// C ABI of libhcgb (declared in include/hcgb.h): contexts, workspace sizing, the batched /
+// tile-matrix / single-tile GEMM entry points, dense->compressed construction, the tile Cholesky
+// building blocks and driver, and rank-trimmed tile packing.  Host code only; the kernels live in
+// tlr_plan.cu, oz_gemm.cu, tlr_qr.cu, tlr_svd.cu, chol.cu, pack.cu and noalloc.cu.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>

@@ -6,11 +6,16 @@
 //               every factor product into a GemmJob (no host round trip)
 //   stack     : copy/scale/transpose the C factors into the stacked bases
 //               U = [Cu | alpha*Ua'] (m x k), V = [beta*Cv^T | Vb'] (n x k)
-//   gemm x3   : the factor products (FP64 DMMA), written straight into the stacks
-//               (or into a dense C)
-//   qr        : blocked Householder QR of both stacks (panel SIMT, trailing DMMA)
-//   core_svd  : M = R_U R_V^T, one-sided Jacobi, rank truncation, new left vectors
-//   apply_q   : new U = Q_U [Ut_r; 0], new V^T = Q_V [M^T Ut_r; 0] (DMMA)
+//   gemm x3   : the factor products, written straight into the stacks (or into a dense C):
+//               a schedule kernel compacts the wave's output tiles, then persistent FP64 DMMA
+//               (small) and FP64-accurate 16-bit tensor-core (large) product kernels
+//   order     : updates sorted by stack width (the heavy stages' CTA order)
+//   qr        : blocked Householder QR of both stacks (plain: panel SIMT + trailing DMMA;
+//               mixed: float-float on the FP32 pipe)
+//   core_svd  : M = R_U R_V^T, pivoted QR, one-sided Jacobi, rank truncation, new factors in
+//               the small basis
+//   apply_q   : new U = Q_U [U_r; 0], new V = Q_V [XV; 0] (panels, or full WY for wide sides
+//               in the plain form)
 //   finalize  : transpose V into the tile buffer, publish the new rank
 #pragma once
 

@@ -1,5 +1,6 @@
-// Planning, stacking, factor products (FP64 DMMA GEMM) and write-back of a batch of
-// TLR tile updates.  Follows HCore<T>::Gemm's dispatch (src/api/HCore.cpp:23-344) and the
+// Planning, stacking, factor products (FP64 DMMA GEMM; the larger ones go to oz_gemm.cu),
+// the plain form's full-WY Q application, ordering and write-back of a batch of TLR tile
+// updates.  Follows HCore<T>::Gemm's dispatch (src/api/HCore.cpp:23-344) and the
 // stacking of CompressedTile<T>::Gemm (src/operators/concrete/Compressed.cpp:331-379).
 #include "internal.cuh"
 

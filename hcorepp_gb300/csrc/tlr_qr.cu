@@ -4,11 +4,13 @@
 // (src/operators/concrete/Compressed.cpp:353, :384, :551, :611; LAPACK dgeqrf/dorgqr semantics:
 // R on and above the diagonal, unit-lower reflectors below it, tau_j = 2 / (v_j^T v_j)).
 //
-// One CTA per matrix.  The matrix stays in device memory (L2-resident working set); each
-// panel of QR_NB columns is staged in shared memory and factored there with SIMT FP64 and
-// warp-shuffle norms; the compact-WY factor T (Q_panel = I - V T V^T, LAPACK dlarft) is
-// kept for the later Q application; the trailing update A <- (I - V T^T V^T) A is two FP64
+// Plain form: one CTA per matrix.  The matrix stays in device memory (L2-resident working
+// set); each panel of QR_NB columns is staged in shared memory and factored there with SIMT FP64
+// and warp-shuffle norms; the compact-WY factor T (Q_panel = I - V T V^T, LAPACK dlarft) is kept
+// for the later Q application; the trailing update A <- (I - V T^T V^T) A is two FP64
 // tensor-core (DMMA) products with V and W = V^T A staged in shared memory.
+// Mixed form (qr_kernel_df, apply_q_kernel_df): the same panels in float-float arithmetic on the
+// FP32 pipe, one team per side (a whole 512-thread CTA for a wide stack, half a CTA otherwise).
 #include "internal.cuh"
 #include "df.cuh"
 

@@ -5,11 +5,15 @@
 // CompressedTile<T>::Gemm (src/operators/concrete/Compressed.cpp:441-527, :597-599) and the
 // host-synchronising rank scan of the CUDA backend (src/kernels/cuda/CudaKernels.cu:656-697).
 //
-// One CTA per update.  One-sided Jacobi rotates pairs of columns of M (round-robin parallel
-// ordering, one warp per pair, warp-shuffle dot products) until every pair is orthogonal to
-// working precision: M J = W, sigma_j = ||w_j||, left vectors Ut = W Sigma^-1.  The right
-// factor is formed as Z = M^T Ut_r (= V_r Sigma_r), so the rotations never need accumulating.
-// The rank rule is the reference's (omp/kernels.cpp:82-104) applied to the sorted sigma.
+// One team per update (a whole 512-thread CTA for a core that does not fit half the shared
+// memory, else half a CTA).  M = R_U R_V^T on DMMA; Householder QR with column pivoting of M,
+// stopped once the remaining columns lie far below the truncation threshold; one-sided Jacobi on
+// the rk columns of X = R^T (round-robin parallel ordering, 4-32 lanes per column pair, scaled
+// rotations, tracked norms) until every pair is orthogonal to working precision: X J = W,
+// sigma_j = ||w_j||.  The right factor is XV = P W_r (= V_r Sigma_r) and the left one
+// U = M XV Sigma^-2 (= U_r), so the rotations never need accumulating.  The pivoted QR and the
+// sweeps run in FP64 (plain form) or float-float (mixed form).  The rank rule is the reference's
+// (omp/kernels.cpp:82-104) applied to the sorted sigma.
 #include <cfloat>
 
 #include "internal.cuh"
