@@ -1,5 +1,5 @@
-// FP64 throughput probes: the roofline denominators of the FP64 path (the driver-measured
-// peaks cover only HBM copy bandwidth and bf16 tensor throughput).
+// FP64 throughput probes: the roofline denominators of the FP64 path (the measured peaks that
+// come with the machine cover only HBM copy bandwidth and bf16 tensor throughput).
 #include "internal.cuh"
 
 namespace hcgb {

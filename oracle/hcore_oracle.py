@@ -1,8 +1,8 @@
 """CPU oracle: a numpy/LAPACK restatement of HCore++'s CPU path for the TLR GEMM.
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` may import this module, and only as the checker
-(or the timed CPU baseline); the GPU product never routes through it.
+CPU-baseline leg of ``bench.py`` may import this module, and only to check results
+(or as the timed CPU baseline); the GPU product never routes through it.
 
 Every function restates one function of the reference's CPU backend
 (``src/kernels/omp/kernels.cpp``, which forwards to BLAS++/LAPACK++) or of the
