@@ -1,10 +1,15 @@
 #!/usr/bin/env python
 """TLR-GEMM tile-updates/s at 1e-8 relative accuracy on GB300.
 
-Forms (--mode): "mixed" (default) runs the stack QR, the core's pivoted QR and Jacobi and the Q
-application in float-float (48-bit) arithmetic on the FP32 pipe; "plain" keeps them in FP64.  In
-both, large factor products run on the 16-bit tensor cores by FP64-accurate error-free splitting.
-The product error against the FP64 dense product is the same for both (reported under "check").
+Headline ("value", "e2e", "roofline"): the plain FP64 form -- the stack QR, the core SVD (pivoted
+QR + one-sided Jacobi) and the Q application in double precision on the FP64 pipe (DFMA / DMMA);
+the factor products FP64-accurate (DMMA, or for the larger ones the 16-bit tensor cores by
+error-free splitting, error below FP64's own worst-case bound).
+
+Other forms, each timed in the same process on the same inputs and reported in "forms" with its
+own value, e2e, product error and speed-up over the plain form:
+  mixed_ff48 : the stack QR, the core's pivoted QR and Jacobi and the Q application in
+               float-float arithmetic (two floats, 48-bit significand) on the FP32 pipe.
 
 Workload (default): n = 16384, nb = 512 -> 32 x 32 tiles, Morton-sorted 2-D points,
 a_ij = exp(-|x_i - x_j| / 0.1); A = B from seed 1, C from seed 2; diagonal tiles dense,
@@ -12,15 +17,17 @@ off-diagonal tiles compressed at 1e-8 relative (ranks ~10-120, capacity nb/3 = 1
 One step = one full multiply C <- A B + C = 32^3 = 32,768 tile updates (beta applied on
 every k step, as the reference driver does), starting from the same C every step.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--forms a,b]
 
 Prints one JSON line (rank 0).  Inputs (A, B, C: ~1.4 GB each) exceed L2, so no flush is
 needed between steps.  "value" times the multiply on device-resident tiles; "e2e" times the same
 multiply with the host's pinned A and C copied in and C copied out every step, in the
 rank-trimmed transfer format (hcgb_pack_tiles: only the factor columns the ranks use), and
-checks that the copied-out result equals the device-resident run's.  The reference arm times the
-CPU oracle port (numpy + LAPACK) on the host cores over a seeded sample of C tiles, each with its
-full 32-update k-chain.
+checks that the copied-out result equals the device-resident run's.  "parity" runs the plain
+form once more in the reference driver's k order and compares every update of the CPU sample's
+C tiles with the oracle's (rank within +-1 after each update, final tile error within
+2 x max(oracle's error, accuracy)).  The reference arm times the CPU oracle port (numpy +
+LAPACK) on the host cores over a seeded sample of C tiles, each with its full 32-update k-chain.
 """
 from __future__ import annotations
 
@@ -32,8 +39,6 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
-import time
 
 import numpy as np
 
@@ -46,6 +51,13 @@ from hcorepp_gb300.replicas import job_throughput  # noqa: E402
 
 METRIC = "TLR-GEMM tile-updates/s at 1e-8 rel err: plain FP64 vs batched mixed+learned"
 UNIT = "tile-updates/s"
+HEADLINE_FORM = "plain_fp64"
+FORM_NOTES = {
+    "plain_fp64": "FP64 throughout: stack QR, core SVD (pivoted QR + one-sided Jacobi) and Q application on the "
+                  "FP64 pipe; factor products FP64-accurate (DMMA, or 16-bit tensor cores by error-free splitting)",
+    "mixed_ff48": "stack QR, core pivoted QR + Jacobi and Q application in float-float (48-bit significand) on the "
+                  "FP32 pipe; core product, new factors, truncation test and factor products as in plain_fp64",
+}
 
 
 def parse():
@@ -55,15 +67,15 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tlr_gemm_n16384_nb512", choices=sorted(WORKLOADS))
+    ap.add_argument("--forms", default="plain_fp64,mixed_ff48",
+                    help="comma-separated forms; plain_fp64 (the headline) always runs first")
     ap.add_argument("--cpu-tiles", type=int, default=256, help="C tiles (each with its full k-chain) in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the dense FP64 accuracy check")
+    ap.add_argument("--no-parity", action="store_true", help="skip the per-update parity run against the CPU sample")
     ap.add_argument("--groups", type=int, default=8, help="independent C-tile groups (streams)")
     ap.add_argument("--k-order", type=int, default=1, choices=[0, 1],
                     help="0: ascending k per C tile (reference order); 1: costliest updates first")
-    ap.add_argument("--mode", default="mixed", choices=["plain", "mixed"],
-                    help="plain: FP64 throughout; mixed: float-float (48-bit) stack QR, core pivoted QR and Jacobi, "
-                         "and Q application on the FP32 pipe")
     return ap.parse_args()
 
 
@@ -82,19 +94,20 @@ def workload_inputs(name, processes=None):
 
 
 def pasc_flops(ra, rb, rc, nb):
-    """The reference's CCC count (tests/api/AdvancedGemmTest.cpp:160-166): 36 nb r^2 + 157 r^3."""
+    """The reference's CCC count (tests/api/AdvancedGemmTest.cpp:160-166): 36 nb r^2 + 157 r^3 with
+    r = max(rA, rB, rC) -- an upper bound of the work on mixed ranks, reported for continuity only."""
     r = np.maximum(np.maximum(ra, rb), rc).astype(np.float64)
     return 36.0 * nb * r * r + 157.0 * r ** 3
 
 
 # ----------------------------------------------------------------------------- CPU arm
-def cpu_measure(w, a, b, c, n_tiles, processes):
+def cpu_measure(w, a, b, c, n_tiles, processes, results=None):
     from oracle import cpu_baseline
     from oracle.hcore_oracle import CompressionParameters
     nt = w["n"] // w["nb"]
     sample = cpu_baseline.sample_tiles(nt, n_tiles)
     params = CompressionParameters(w["accuracy"], truncated_svd=True)
-    updates, wall = cpu_baseline.run(a, b, c, params, sample, processes)
+    updates, wall = cpu_baseline.run(a, b, c, params, sample, processes, results)
     return updates, wall, sample
 
 
@@ -105,6 +118,7 @@ def reference_arm(args, rank, world):
     procs = cores
     w, a, b, c = workload_inputs(args.workload, procs)
     n_tiles = args.cpu_tiles or procs
+    nt = w["n"] // w["nb"]
     vals = []
     for it in range(args.warmup + args.steps):
         updates, wall, sample = cpu_measure(w, a, b, c, n_tiles, procs)
@@ -113,13 +127,13 @@ def reference_arm(args, rank, world):
     value = statistics.mean(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 32 * n_tiles / value,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * nt * n_tiles / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (Morton-sorted exponential kernel, seeded)",
         "config": {"workload": args.workload, "n": w["n"], "nb": w["nb"], "accuracy": w["accuracy"],
-                   "updates_per_multiply": (w["n"] // w["nb"]) ** 3},
+                   "updates_per_multiply": nt ** 3},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                         "sample": f"{n_tiles} seeded C tiles x {w['n'] // w['nb']} k-updates each per step"},
+                         "sample": f"{n_tiles} seeded C tiles x {nt} k-updates each per step"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -196,12 +210,12 @@ def load_tiles(T, L, tiles, nt, nb, max_rank):
     return tm, host, ranks
 
 
-def traffic_from_profiles(kernel_stage, workload, updates_per_launch):
+def traffic_from_profiles(kernel_stage, workload, form, updates_per_launch):
     """DRAM bytes per launch of `kernel_stage`: the per-update traffic of an ncu capture on a
     smaller case (profiles/ncu_traffic.json) times the updates one launch processes."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
-        ent = json.load(open(path)).get(workload, {}).get(kernel_stage)
+        ent = json.load(open(path)).get(workload, {}).get(form, {}).get(kernel_stage)
         return None if ent is None else float(ent["bytes_per_update"]) * updates_per_launch
     except Exception:
         return None
@@ -209,9 +223,8 @@ def traffic_from_profiles(kernel_stage, workload, updates_per_launch):
 
 def stage_algorithmic_flops(info, nb, kinds_of_update):
     """Algorithmic FP64 flops per stage for one multiply, from the per-update records."""
-    ra, rb, rc = info[:, 1].astype(float), info[:, 2].astype(float), info[:, 3].astype(float)
+    ra, rb = info[:, 1].astype(float), info[:, 2].astype(float)
     k, r, sw = info[:, 4].astype(float), info[:, 5].astype(float), info[:, 6].astype(float)
-    side = info[:, 7]
     rk = info[:, 8].astype(float)
     comp = k > 0
     m = float(nb)
@@ -242,6 +255,249 @@ def stage_algorithmic_flops(info, nb, kinds_of_update):
     return out
 
 
+class Workbench:
+    """The device-resident inputs of one workload and the multiply steps run on them."""
+
+    def __init__(self, args, local):
+        import torch
+        from hcorepp_gb300 import _lib as L
+        from hcorepp_gb300 import tiles as T
+        self.torch, self.L, self.T = torch, L, T
+        self.args, self.local = args, local
+        self.w, self.a_t, self.b_t, self.c_t = workload_inputs(args.workload, None)
+        w = self.w
+        self.nb = w["nb"]
+        self.nt = w["n"] // self.nb
+        self.maxr = max(self.nb // 3, 1)
+        self.n_updates = self.nt ** 3
+        self.ctx = T.run_context(local)
+        nt, nb, maxr = self.nt, self.nb, self.maxr
+        self.A, self.a_host, self.a_ranks = load_tiles(T, L, self.a_t, nt, nb, maxr)
+        self.C0, self.c_host, self.c_ranks = load_tiles(T, L, self.c_t, nt, nb, maxr)
+        self.A.arena.copy_(torch.from_numpy(self.a_host))
+        self.A.ranks.copy_(torch.from_numpy(self.a_ranks))
+        self.C0.arena.copy_(torch.from_numpy(self.c_host))
+        self.C0.ranks.copy_(torch.from_numpy(self.c_ranks))
+        self.Cw = T.TileMatrix(nt, nt, nb, self.C0.kinds, maxr)
+        self.info = T.info_buffer(self.n_updates)
+        self.kinds_u = []
+        for kk in range(nt):
+            for j in range(nt):
+                for i in range(nt):
+                    self.kinds_u.append((self.a_t[(i, kk)][0] == "C", self.b_t[(kk, j)][0] == "C",
+                                         self.c_t[(i, j)][0] == "C"))
+        self._e2e = None
+
+    def params(self, mode, accuracy=None):
+        return self.T.CompressionParameters(accuracy or self.w["accuracy"], truncated_svd=True, mode=mode)
+
+    def step(self, params, record_info=False):
+        """One multiply from the same C: C <- A B + C (B = A: one device copy serves both operands)."""
+        self.Cw.arena.copy_(self.C0.arena)
+        self.Cw.ranks.copy_(self.C0.ranks)
+        self.T.tlr_gemm(1.0, self.A, self.A, 1.0, self.Cw, params, self.info if record_info else None,
+                        ctx=self.T.run_context(self.local))
+
+    # ---- end to end through the public API: host (pinned) inputs in, result back to the host.
+    #      Tiles travel in the rank-trimmed transfer format (hcgb_pack_tiles): the host holds A and
+    #      C packed (only the columns their ranks use); every step copies them in, unpacks them on
+    #      the device, multiplies (B = A, as in the device-resident run: one copy serves both
+    #      operands), packs C, reads the packed size and copies C and its ranks out.
+    def _e2e_buffers(self):
+        if self._e2e is None:
+            torch, T = self.torch, self.T
+            nt, nb, maxr = self.nt, self.nb, self.maxr
+            e = {}
+            e["Ae"] = T.TileMatrix(nt, nt, nb, self.A.kinds, maxr)
+            e["Ce"] = T.TileMatrix(nt, nt, nb, self.C0.kinds, maxr)
+            e["a_pk"] = torch.from_numpy(e["Ae"].host_pack(self.a_host, self.a_ranks)).pin_memory()
+            e["c_pk"] = torch.from_numpy(e["Ce"].host_pack(self.c_host, self.c_ranks)).pin_memory()
+            e["ar_pin"] = torch.from_numpy(self.a_ranks).pin_memory()
+            e["cr_pin"] = torch.from_numpy(self.c_ranks).pin_memory()
+            e["a_dev"] = torch.empty(e["a_pk"].numel(), dtype=torch.float64, device="cuda")
+            e["c_dev"] = torch.empty(e["c_pk"].numel(), dtype=torch.float64, device="cuda")
+            e["out_dev"] = torch.empty(e["Ce"].arena.numel(), dtype=torch.float64, device="cuda")
+            e["offs"] = [torch.empty(nt * nt + 1, dtype=torch.int64, device="cuda") for _ in range(3)]
+            e["out_pin"] = torch.empty(e["Ce"].arena.numel(), dtype=torch.float64).pin_memory()
+            e["outr_pin"] = torch.empty_like(e["cr_pin"]).pin_memory()
+            e["total_pin"] = torch.empty(1, dtype=torch.int64).pin_memory()
+            self._e2e = e
+        return self._e2e
+
+    def e2e_step(self, params, moved):
+        e = self._e2e_buffers()
+        Ae, Ce = e["Ae"], e["Ce"]
+        Ae.ranks.copy_(e["ar_pin"], non_blocking=True)
+        e["a_dev"].copy_(e["a_pk"], non_blocking=True)
+        Ae.unpack(e["a_dev"], e["offs"][0])
+        Ce.ranks.copy_(e["cr_pin"], non_blocking=True)
+        e["c_dev"].copy_(e["c_pk"], non_blocking=True)
+        Ce.unpack(e["c_dev"], e["offs"][1])
+        self.T.tlr_gemm(1.0, Ae, Ae, 1.0, Ce, params, ctx=self.T.run_context(self.local))
+        Ce.pack(e["out_dev"], e["offs"][2])
+        e["outr_pin"].copy_(Ce.ranks, non_blocking=True)
+        e["total_pin"].copy_(e["offs"][2][-1:], non_blocking=True)
+        self.torch.cuda.current_stream().synchronize()  # the packed size of the result
+        total = int(e["total_pin"][0])
+        e["out_pin"][:total].copy_(e["out_dev"][:total], non_blocking=True)
+        moved["h2d"] = e["a_pk"].numel() * 8 + e["c_pk"].numel() * 8 + 4 * (e["ar_pin"].numel() + e["cr_pin"].numel())
+        moved["d2h"] = total * 8 + 4 * e["outr_pin"].numel() + 8
+        moved["total"] = total
+
+    def e2e_matches_device_run(self, moved):
+        """The host copy of the e2e result against the device-resident run's result (same multiply)."""
+        e = self._e2e_buffers()
+        want = self.Cw.host_pack(self.Cw.arena.cpu().numpy(), self.Cw.ranks.cpu().numpy())
+        return bool(np.array_equal(e["out_pin"][:moved["total"]].numpy(), want))
+
+
+def timed(torch, stream, steps, fn, world, sampler=None):
+    """CUDA-event time (ms per step) of `steps` calls of fn, barrier + synchronize on both sides."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    return e0.elapsed_time(e1) / steps
+
+
+def measure_form(wb, form, mode, args, world, with_e2e=True):
+    """Device-resident and end-to-end throughput of one form, its serialised stage times and its
+    per-update records."""
+    torch, L = wb.torch, wb.L
+    params = wb.params(mode)
+    ctx = wb.ctx
+    ctx.set_concurrency(args.groups)
+    ctx.set_k_order(args.k_order)
+    for _ in range(max(args.warmup, 1)):
+        wb.step(params, record_info=True)
+    torch.cuda.synchronize()
+    info_h = wb.info.cpu().numpy()
+    stream = torch.cuda.current_stream()
+    out = {"form": form, "note": FORM_NOTES.get(form, "")}
+    l0 = L.kernel_launches()
+    with ClockSampler(wb.local) as clk:
+        ms = timed(torch, stream, args.steps, lambda: wb.step(params), world)
+    launches = (L.kernel_launches() - l0) / args.steps
+    value, ms = job_throughput(ms, wb.n_updates, device="cuda")
+    out.update(value=value, ms_per_step=ms, gpu_launches_per_step=launches, clocks=clk.summary())
+    # One more multiply, serialised on one stream with CUDA events around every stage: the
+    # per-kernel durations behind the roofline (not part of the timed region).
+    ctx.set_concurrency(1)
+    ctx.profile_reset()
+    ctx.profile(True)
+    wb.step(params)
+    ctx.profile(False)
+    out["stages"] = ctx.profile_read()
+    ctx.set_concurrency(args.groups)
+    # the result of this form (same multiply as the timed steps) for the accuracy check
+    if not args.no_check:
+        out["result_dense"] = wb.Cw.to_dense_device()
+    out["ranks_final"] = wb.Cw.rank_grid()
+    if with_e2e:
+        moved = {}
+        wb.e2e_step(params, moved)
+        torch.cuda.synchronize()
+        e2e_ms = timed(torch, stream, args.steps, lambda: wb.e2e_step(params, moved), world)
+        e2e_value, e2e_ms = job_throughput(e2e_ms, wb.n_updates, device="cuda")
+        out["e2e"] = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(moved["h2d"]),
+                      "d2h_bytes_per_step": int(moved["d2h"]), "ms_per_step": e2e_ms,
+                      "transfer": "rank-trimmed packed tiles (hcgb_pack_tiles / hcgb_unpack_tiles), pinned host "
+                                  "buffers",
+                      "result_matches_device_run": wb.e2e_matches_device_run(moved)}
+    out["info"] = info_h
+    return out
+
+
+def roofline_of(wb, res, form, dmma_peak, dfma_peak, args):
+    stages = res["stages"]
+    info_h = res["info"]
+    st_flops = stage_algorithmic_flops(info_h, wb.nb, wb.kinds_u)
+    dom = max(stages, key=lambda s: stages[s][0])
+    dom_ms_per_launch = stages[dom][0] / max(stages[dom][1], 1)
+    dom_flops_per_launch = st_flops.get(dom, 0.0) / max(stages[dom][1], 1)
+    tensor_stages = {"gemm"}
+    peak = dmma_peak if dom in tensor_stages else dfma_peak
+    achieved = dom_flops_per_launch / (dom_ms_per_launch * 1e-3) / 1e12
+    comp_updates = int(np.count_nonzero(info_h[:, 4] > 0))
+    traffic = traffic_from_profiles(dom, args.workload, form, comp_updates / max(stages[dom][1], 1))
+    ff = form == "mixed_ff48" and dom in ("core_svd", "qr", "apply_q")
+    roof = {"bound": "fp64_equivalent" if ff else ("tensor" if dom in tensor_stages else "fp64"), "kernel": dom,
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": traffic,
+            "peak_source": "measured in this run by hcgb_fp64_peak (FP64 DMMA / DFMA probe kernels); "
+                           "MEASURED_PEAKS.json has no FP64 figure",
+            "note": ("algorithmic FP64-equivalent flops of the stage; it runs in float-float arithmetic on the "
+                     "FP32 pipe and is compared with the FP64 peak it replaces" if ff else
+                     "algorithmic FP64 flops of the stage (operation counts of the reference's algorithm) per "
+                     "launch / the launch's CUDA-event duration")}
+    total_ms = sum(v[0] for v in stages.values())
+    extra = {
+        "stages_ms_serial_step": {s: stages[s][0] for s in stages},
+        "stage_launches_serial_step": {s: stages[s][1] for s in stages},
+        "serial_step_ms": total_ms,
+        "stage_share": {s: stages[s][0] / total_ms for s in stages},
+        "stage_algorithmic_tflops": {s: st_flops[s] / (stages[s][0] * 1e-3) / 1e12 for s in st_flops
+                                     if s in stages and stages[s][0] > 0},
+    }
+    return roof, extra
+
+
+def parity_block(wb, cpu_results, args, exact):
+    """The plain form in the reference driver's k order against the CPU sample's oracle chains.
+    `exact`: the FP64 dense product of the compressed inputs (device tensor)."""
+    torch, L = wb.torch, wb.L
+    ctx = wb.ctx
+    ctx.set_k_order(0)
+    wb.step(wb.params(L.PLAIN_FP64), record_info=True)
+    torch.cuda.synchronize()
+    ctx.set_k_order(args.k_order)
+    info = wb.info.cpu().numpy()
+    nt, nb = wb.nt, wb.nb
+    n = nt * nt
+    acc = wb.w["accuracy"]
+    Cres = wb.Cw
+    ranks_bad, updates, worst_dr = 0, 0, 0
+    tiles_checked, tiles_bad = 0, 0
+    max_ratio = 0.0
+    dev_res = Cres.to_dense_device()
+    for (i, j), res in cpu_results.items():
+        idx = i + j * nt
+        for k, r_o in enumerate(res["ranks"]):
+            updates += 1
+            rec = info[k * n + idx]
+            if rec[0] != 0:
+                ranks_bad += 1
+                continue
+            if r_o is None:
+                continue
+            d = abs(int(rec[5]) - int(r_o))
+            worst_dr = max(worst_dr, d)
+            ranks_bad += d > 1
+        sl = (slice(i * nb, (i + 1) * nb), slice(j * nb, (j + 1) * nb))
+        ex = exact[sl]
+        fo = res["final"]
+        o_dense = torch.from_numpy(np.ascontiguousarray(fo[1] if fo[0] == "D" else fo[1] @ fo[2])).to(ex.device)
+        nrm = float(torch.linalg.norm(ex))
+        e_o = float(torch.linalg.norm(o_dense - ex)) / nrm
+        e_g = float(torch.linalg.norm(dev_res[sl] - ex)) / nrm
+        tiles_checked += 1
+        bound = 2 * max(e_o, acc)
+        tiles_bad += e_g > bound
+        max_ratio = max(max_ratio, e_g / bound)
+    return {"form": "plain_fp64", "k_order": "ascending (reference driver)", "c_tiles": tiles_checked,
+            "updates_compared": updates, "rank_violations": int(ranks_bad), "max_abs_rank_diff": int(worst_dr),
+            "tiles_over_error_bound": int(tiles_bad), "max_error_over_bound": float(max_ratio),
+            "bar": "rank within +-1 of the oracle after every update; tile rel. Frobenius error vs the exact "
+                   "product <= 2 x max(oracle's error, accuracy)"}
+
+
 def gpu_arm(args, rank, world, local):
     import torch
     if world > 1:
@@ -249,203 +505,92 @@ def gpu_arm(args, rank, world, local):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     from hcorepp_gb300 import _lib as L
-    from hcorepp_gb300 import tiles as T
 
-    w, a_t, b_t, c_t = workload_inputs(args.workload, None)
-    nb = w["nb"]
-    nt = w["n"] // nb
-    maxr = max(nb // 3, 1)
-    n_updates = nt ** 3
-
-    ctx = T.run_context(local)
-    A, a_host, a_ranks = load_tiles(T, L, a_t, nt, nb, maxr)
-    B = A  # B = A (same seed and tiles): one device copy serves both operands
-    C0, c_host, c_ranks = load_tiles(T, L, c_t, nt, nb, maxr)
-    A.arena.copy_(torch.from_numpy(a_host))
-    A.ranks.copy_(torch.from_numpy(a_ranks))
-    C0.arena.copy_(torch.from_numpy(c_host))
-    C0.ranks.copy_(torch.from_numpy(c_ranks))
-    Cw = T.TileMatrix(nt, nt, nb, C0.kinds, maxr)
-    params = T.CompressionParameters(w["accuracy"], truncated_svd=True,
-                                     mode=L.MIXED if args.mode == "mixed" else L.PLAIN_FP64)
-    info = T.info_buffer(n_updates)
-    dmma_peak, dfma_peak = ctx.fp64_peak()
-    ctx.set_concurrency(args.groups)
-    ctx.set_k_order(args.k_order)
-
-    def step(record_info=False):
-        Cw.arena.copy_(C0.arena)
-        Cw.ranks.copy_(C0.ranks)
-        T.tlr_gemm(1.0, A, B, 1.0, Cw, params, info if record_info else None, ctx=T.run_context(local))
-
-    for _ in range(max(args.warmup, 1)):
-        step(record_info=True)
-    torch.cuda.synchronize()
-    info_h = info.cpu().numpy()
-    bad = int(np.count_nonzero((info_h[:, 0] != 0) & (info_h[:, 0] != L.HCGB_NOT_CONVERGED)))
-
-    # ---- timed region (device-resident inputs)
-    stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ctx.profile(False)
-    ctx.profile_reset()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            step()
-        e1.record(stream)
-        torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    launches = int(sum(v[1] for v in ctx.profile_read().values()))
-    value, ms = job_throughput(ms, n_updates, device="cuda")
-
-    # ---- one more multiply, serialised on one stream with CUDA events around every stage:
-    #      the per-kernel durations behind the roofline (not part of the timed region).
-    ctx.set_concurrency(1)
-    ctx.profile_reset()
-    ctx.profile(True)
-    step()
-    ctx.profile(False)
-    stages = ctx.profile_read()
-    ctx.set_concurrency(args.groups)
-    serial_ms = sum(v[0] for v in stages.values())
-
-    # ---- end to end through the public API: host (pinned) inputs in, result back to the host.
-    #      Tiles travel in the rank-trimmed transfer format (hcgb_pack_tiles): the host holds A and
-    #      C packed (only the columns their ranks use); every step copies them in, unpacks them on
-    #      the device, multiplies (B = A, as in the device-resident run: one copy serves both
-    #      operands), packs C, reads the packed size and copies C and its ranks out.
-    Ae = T.TileMatrix(nt, nt, nb, A.kinds, maxr)
-    Ce = T.TileMatrix(nt, nt, nb, C0.kinds, maxr)
-    a_pk = torch.from_numpy(Ae.host_pack(a_host, a_ranks)).pin_memory()
-    c_pk = torch.from_numpy(Ce.host_pack(c_host, c_ranks)).pin_memory()
-    ar_pin = torch.from_numpy(a_ranks).pin_memory()
-    cr_pin = torch.from_numpy(c_ranks).pin_memory()
-    a_dev = torch.empty(a_pk.numel(), dtype=torch.float64, device="cuda")
-    c_dev = torch.empty(c_pk.numel(), dtype=torch.float64, device="cuda")
-    out_dev = torch.empty(Ce.arena.numel(), dtype=torch.float64, device="cuda")
-    offs = [torch.empty(nt * nt + 1, dtype=torch.int64, device="cuda") for _ in range(3)]
-    out_pin = torch.empty(Ce.arena.numel(), dtype=torch.float64).pin_memory()
-    outr_pin = torch.empty_like(cr_pin).pin_memory()
-    total_pin = torch.empty(1, dtype=torch.int64).pin_memory()
-    moved = {}
-
-    def e2e_step():
-        Ae.ranks.copy_(ar_pin, non_blocking=True)
-        a_dev.copy_(a_pk, non_blocking=True)
-        Ae.unpack(a_dev, offs[0])
-        Ce.ranks.copy_(cr_pin, non_blocking=True)
-        c_dev.copy_(c_pk, non_blocking=True)
-        Ce.unpack(c_dev, offs[1])
-        T.tlr_gemm(1.0, Ae, Ae, 1.0, Ce, params, ctx=T.run_context(local))
-        Ce.pack(out_dev, offs[2])
-        outr_pin.copy_(Ce.ranks, non_blocking=True)
-        total_pin.copy_(offs[2][-1:], non_blocking=True)
-        torch.cuda.current_stream().synchronize()  # the packed size of the result
-        total = int(total_pin[0])
-        out_pin[:total].copy_(out_dev[:total], non_blocking=True)
-        moved["h2d"] = a_pk.numel() * 8 + c_pk.numel() * 8 + 4 * (ar_pin.numel() + cr_pin.numel())
-        moved["d2h"] = total * 8 + 4 * outr_pin.numel() + 8
-        moved["total"] = total
-
-    e2e_step()
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    e2 = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    e2[0].record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    e2[1].record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e2[0].elapsed_time(e2[1]) / args.steps
-    e2e_value, e2e_ms = job_throughput(e2e_ms, n_updates, device="cuda")
-    h2d, d2h = moved["h2d"], moved["d2h"]
-    # the host copy of the result against the device-resident run's result (same multiply)
-    e2e_matches = bool(np.array_equal(out_pin[:moved["total"]].numpy(),
-                                      Cw.host_pack(Cw.arena.cpu().numpy(), Cw.ranks.cpu().numpy())))
-
+    forms = [f for f in args.forms.split(",") if f]
+    forms = [HEADLINE_FORM] + [f for f in forms if f != HEADLINE_FORM]
+    modes = {"plain_fp64": L.PLAIN_FP64, "mixed_ff48": L.MIXED}
+    for f in forms:
+        if f not in modes:
+            raise SystemExit(f"unknown form {f}")
+    wb = Workbench(args, local)
+    dmma_peak, dfma_peak = wb.ctx.fp64_peak()
+    results = {f: measure_form(wb, f, modes[f], args, world) for f in forms}
     if rank != 0:
         return 0
-
-    # ---- accounting: flops, roofline of the dominant stage
-    kinds_u = []
-    for kk in range(nt):
-        for j in range(nt):
-            for i in range(nt):
-                kinds_u.append((a_t[(i, kk)][0] == "C", b_t[(kk, j)][0] == "C", c_t[(i, j)][0] == "C"))
-    pasc = float(np.sum(pasc_flops(info_h[:, 1], info_h[:, 2], info_h[:, 3], nb)[info_h[:, 4] > 0]))
-    st_flops = stage_algorithmic_flops(info_h, nb, kinds_u)
-    total_stage_ms = sum(v[0] for v in stages.values())
-    dom = max(stages, key=lambda s: stages[s][0])
-    dom_ms_per_launch = stages[dom][0] / max(stages[dom][1], 1)
-    dom_flops_per_launch = st_flops.get(dom, 0.0) / max(stages[dom][1], 1)
-    tensor_stages = {"gemm", "qr", "apply_q"}
-    peak = dmma_peak if dom in tensor_stages else dfma_peak
-    achieved = dom_flops_per_launch / (dom_ms_per_launch * 1e-3) / 1e12
-    comp_updates = int(np.count_nonzero(info_h[:, 4] > 0))
-    traffic = traffic_from_profiles(dom, args.workload, comp_updates / max(stages[dom][1], 1))
+    head = results[HEADLINE_FORM]
+    nb, nt, maxr = wb.nb, wb.nt, wb.maxr
+    info_h = head["info"]
 
     # ---- accuracy against the FP64 dense product of the TLR inputs (cuBLAS, outside the timing)
-    check = {}
+    exact = None
     if not args.no_check:
-        import torch as th
-        Ad = th.from_numpy(A.to_dense()).cuda()
-        Cd0 = th.from_numpy(C0.to_dense()).cuda()
+        Ad = wb.A.to_dense_device()
+        Cd0 = wb.C0.to_dense_device()
         exact = Ad @ Ad + Cd0
-        Cres = th.from_numpy(Cw.to_dense()).cuda()
-        check["rel_fro_err_vs_fp64_dense_product"] = float(th.linalg.norm(Cres - exact) / th.linalg.norm(exact))
-        del Ad, Cd0, exact, Cres
-        th.cuda.empty_cache()
-    rk = Cw.rank_grid()
-    comp_mask = np.array([[c_t[(i, j)][0] == "C" for j in range(nt)] for i in range(nt)])
-    clamped = int(np.count_nonzero(info_h[:, 5] >= maxr))
+        del Ad, Cd0
+        nrm = torch.linalg.norm(exact)
+        for f in forms:
+            res = results[f]
+            res["rel_fro_err_vs_fp64_dense_product"] = float(torch.linalg.norm(res.pop("result_dense") - exact) / nrm)
+        torch.cuda.empty_cache()
 
-    # ---- CPU baseline (oracle port) on a bounded sample, host cores
-    cpu = None
+    roof, extra = roofline_of(wb, head, HEADLINE_FORM, dmma_peak, dfma_peak, args)
+    comp_mask = np.array([[wb.c_t[(i, j)][0] == "C" for j in range(nt)] for i in range(nt)])
+    rk = head["ranks_final"]
+    clamped = int(np.count_nonzero(info_h[:, 5] >= maxr))
+    bad = int(np.count_nonzero((info_h[:, 0] != 0) & (info_h[:, 0] != L.HCGB_NOT_CONVERGED)))
+    pasc = float(np.sum(pasc_flops(info_h[:, 1], info_h[:, 2], info_h[:, 3], nb)[info_h[:, 4] > 0]))
+
+    # ---- CPU baseline (oracle port) on a bounded sample, host cores; its oracle results feed the
+    #      per-update parity check of the plain form
+    cpu, parity = None, None
     if not args.no_cpu_baseline:
         procs = os.cpu_count() or 1
         n_tiles = args.cpu_tiles or procs
-        upd, wall, sample = cpu_measure(w, a_t, b_t, c_t, n_tiles, procs)
+        cpu_results = {}
+        upd, wall, sample = cpu_measure(wb.w, wb.a_t, wb.b_t, wb.c_t, n_tiles, procs, cpu_results)
         cpu = {"value": upd / wall, "unit": UNIT, "cores": procs, "kind": "port",
                "sample": f"{n_tiles} seeded C tiles x {nt} k-updates = {upd} updates, {wall:.1f} s wall"}
+        if not args.no_parity and exact is not None:
+            parity = parity_block(wb, cpu_results, args, exact)
+    exact = None
+    torch.cuda.empty_cache()
 
-    clocks = clk.summary()
+    form_blocks = {}
+    for f in forms:
+        res = results[f]
+        blk = {"value": res["value"], "unit": UNIT, "ms_per_step": res["ms_per_step"], "note": res["note"],
+               "speedup_over_plain_fp64": res["value"] / head["value"],
+               "gpu_launches_per_step": res["gpu_launches_per_step"], "clocks": res["clocks"],
+               "rel_fro_err_vs_fp64_dense_product": res.get("rel_fro_err_vs_fp64_dense_product"),
+               "mean_final_rank": float(res["ranks_final"][comp_mask].mean())}
+        if "e2e" in res:
+            blk["e2e"] = res["e2e"]
+        if f != HEADLINE_FORM:
+            r2, x2 = roofline_of(wb, res, f, dmma_peak, dfma_peak, args)
+            blk["roofline"] = r2
+            blk["stage_share"] = x2["stage_share"]
+            blk["serial_step_ms"] = x2["serial_step_ms"]
+        form_blocks[f] = blk
+
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (Morton-sorted exponential kernel, seeded)",
-        "config": {"workload": args.workload, "n": w["n"], "nb": w["nb"], "tiles": f"{nt}x{nt}",
-                   "updates_per_step": n_updates, "accuracy": w["accuracy"], "threshold": "relative",
-                   "dense_diagonal": w["dense_diagonal"], "max_rank": maxr,
-                   "form": "plain_fp64" if args.mode == "plain" else "mixed (float-float QR, pivoted QR, Jacobi, Q application)",
-                   "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups, "k_order": "ascending" if args.k_order == 0 else "cost-descending",
+        "config": {"workload": args.workload, "n": wb.w["n"], "nb": nb, "tiles": f"{nt}x{nt}",
+                   "updates_per_step": wb.n_updates, "accuracy": wb.w["accuracy"], "threshold": "relative",
+                   "dense_diagonal": wb.w["dense_diagonal"], "max_rank": maxr, "form": HEADLINE_FORM,
+                   "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups,
+                   "k_order": "ascending" if args.k_order == 0 else "cost-descending",
                    "l2": "inputs larger than L2 (A, C arenas 1.4 GB each), no flush"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "transfer": "rank-trimmed packed tiles (hcgb_pack_tiles / hcgb_unpack_tiles), pinned host buffers",
-                "result_matches_device_run": e2e_matches},
-        "roofline": {"bound": ("fp64_equivalent" if args.mode == "mixed" and dom in ("core_svd", "qr", "apply_q")
-                               else ("tensor" if dom in tensor_stages else "fp64_simt")), "kernel": dom,
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": traffic,
-                     "peak_source": "measured in this run by hcgb_fp64_peak (FP64 DMMA / DFMA probe); "
-                                    "MEASURED_PEAKS.json has no FP64 figure",
-                     "note": ("algorithmic FP64-equivalent flops of the stage; in the mixed form it runs in "
-                              "float-float arithmetic on the FP32 pipe, so its rate is compared with the FP64 "
-                              "peak it replaces" if args.mode == "mixed" else "algorithmic FP64 flops of the stage")},
-        "fp64": {"pasc_gflops": pasc / (ms * 1e-3) / 1e9, "pasc_frac_of_dmma_peak": pasc / (ms * 1e-3) / 1e12 / dmma_peak,
-                 "dmma_peak_tflops": dmma_peak, "dfma_peak_tflops": dfma_peak},
-        "stages_ms_serial_step": {s: stages[s][0] for s in stages},
-        "serial_step_ms": serial_ms,
-        "stage_share": {s: stages[s][0] / total_stage_ms for s in stages},
-        "stage_algorithmic_tflops": {s: st_flops[s] / (stages[s][0] * 1e-3) / 1e12 for s in st_flops
-                                     if s in stages and stages[s][0] > 0},
-        "gpu_launches": launches,
+        "e2e": {k: v for k, v in head["e2e"].items() if k != "ms_per_step"},
+        "roofline": roof,
+        "fp64": {"dmma_peak_tflops": dmma_peak, "dfma_peak_tflops": dfma_peak,
+                 "reference_formula_gflops": pasc / (head["ms_per_step"] * 1e-3) / 1e9,
+                 "reference_formula_note": "36 nb r^2 + 157 r^3 with r = max(rA, rB, rC) "
+                                           "(tests/api/AdvancedGemmTest.cpp:160-166): overcounts mixed ranks"},
+        **extra,
+        "gpu_launches": int(round(head["gpu_launches_per_step"] * args.steps)),
         "ranks": {"mean_final": float(rk[comp_mask].mean()), "max_final": int(rk[comp_mask].max()),
                   "updates_at_capacity": clamped, "bad_status": bad,
                   "mean_k": float(info_h[info_h[:, 4] > 0, 4].mean()),
@@ -454,9 +599,11 @@ def gpu_arm(args, rank, world, local):
                   "mean_core_cols": float(info_h[info_h[:, 4] > 0, 8].mean())},
         "core_kcycles_mean": {nm: float(info_h[info_h[:, 4] > 0, 9 + q].mean())
                               for q, nm in enumerate(["product", "qrcp", "jacobi", "factors"])},
-        "check": check,
+        "check": {"rel_fro_err_vs_fp64_dense_product": head.get("rel_fro_err_vs_fp64_dense_product")},
+        "parity": parity,
+        "forms": form_blocks,
         "cpu_baseline": cpu,
-        "clocks": clocks,
+        "clocks": head["clocks"],
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -60,7 +60,7 @@ _LIB = None
 def header_functions():
     """Names of the functions declared in include/hcgb.h."""
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char \*)\s*(hcgb_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|long long|const char \*)\s*(hcgb_\w+)\s*\(", text, re.M)))
 
 
 def lib():
@@ -105,6 +105,8 @@ def lib():
         L.hcgb_tile_gemm_noalloc.argtypes = [C.c_double, C.POINTER(Tile), C.POINTER(Tile), C.c_double,
                                              C.POINTER(Tile), C.POINTER(Params), vp, vp]
         L.hcgb_tile_gemm_noalloc.restype = C.c_int
+        L.hcgb_kernel_launches.argtypes = []
+        L.hcgb_kernel_launches.restype = C.c_longlong
         for nm in ("hcgb_pack_tiles", "hcgb_unpack_tiles"):
             getattr(L, nm).argtypes = [vp, ip, C.POINTER(Tile), vp, vp]
             getattr(L, nm).restype = C.c_int
@@ -182,6 +184,11 @@ class Context:
 
 
 PLAIN_FP64, MIXED = 0, 1
+
+
+def kernel_launches() -> int:
+    """Kernels libhcgb has launched in this process so far."""
+    return int(lib().hcgb_kernel_launches())
 
 
 def make_params(accuracy=1e-4, truncated_svd=False, fixed_rank=0, use_trmm=False, use_ungqr=True, op_type=1,

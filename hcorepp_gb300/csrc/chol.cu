@@ -147,27 +147,27 @@ __global__ void __launch_bounds__(256) trsm_panel_kernel(const double *L, int nb
 }  // namespace
 
 void launch_trsm_panel(const double *L, int nb, int ldl, const DevTile *tiles, int count, cudaStream_t st) {
-    if (count > 0) trsm_panel_kernel<<<count, 256, 0, st>>>(L, nb, ldl, tiles);
+    if (count > 0) { trsm_panel_kernel<<<count, 256, 0, st>>>(L, nb, ldl, tiles); note_launch(); }
 }
 
 void launch_fill_triangle(int uplo, int n, double *A, int lda, double value, cudaStream_t st) {
     dim3 blk(32, 8), grid((n + 31) / 32, (n + 7) / 8);
-    fill_triangle_kernel<<<grid, blk, 0, st>>>(uplo, n, A, lda, value);
+    { fill_triangle_kernel<<<grid, blk, 0, st>>>(uplo, n, A, lda, value); note_launch(); }
 }
 
 void launch_potrf(double *A, int n, int lda, int uplo, int *info_dev, cudaStream_t st) {
-    potrf_kernel<<<1, CT, 0, st>>>(A, n, lda, uplo, info_dev);
+    { potrf_kernel<<<1, CT, 0, st>>>(A, n, lda, uplo, info_dev); note_launch(); }
 }
 
 void launch_trsm(int side, int uplo, int trans, int diag, int m, int n, double alpha, const double *A, int lda,
                  double *B, int ldb, cudaStream_t st) {
-    trsm_kernel<<<1, CT, 0, st>>>(side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb);
+    { trsm_kernel<<<1, CT, 0, st>>>(side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb); note_launch(); }
 }
 
 void launch_syrk(int uplo, int trans, int n, int k, double alpha, const double *A, int lda, double beta, double *C,
                  int ldc, cudaStream_t st) {
     dim3 blk(16, 16), grid((n + 15) / 16, (n + 15) / 16);
-    syrk_kernel<<<grid, blk, 0, st>>>(uplo, trans, n, k, alpha, A, lda, beta, C, ldc);
+    { syrk_kernel<<<grid, blk, 0, st>>>(uplo, trans, n, k, alpha, A, lda, beta, C, ldc); note_launch(); }
 }
 
 }  // namespace hcgb

@@ -3,6 +3,7 @@
 // building blocks and driver, and rank-trimmed tile packing.  Host code only; the kernels live in
 // tlr_plan.cu, oz_gemm.cu, tlr_qr.cu, tlr_svd.cu, chol.cu, pack.cu and noalloc.cu.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -11,6 +12,13 @@
 #include "internal.cuh"
 
 using namespace hcgb;
+
+namespace hcgb {
+static std::atomic<long long> g_kernel_launches{0};
+void note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace hcgb
+
+extern "C" long long hcgb_kernel_launches(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
 
 struct hcgb_context {
     int device = 0;
@@ -37,6 +45,7 @@ struct hcgb_context {
     std::vector<cudaEvent_t> group_events;  // [0] fork, [1..] joins
     void *pack_desc = nullptr;  // DevTile[] of hcgb_pack_tiles / hcgb_unpack_tiles
     size_t pack_desc_bytes = 0;
+    hcgb_update_info *tile_info = nullptr;  // the one record hcgb_tile_gemm reads back (allocated once)
 };
 
 namespace {
@@ -307,6 +316,7 @@ int hcgb_context_destroy(hcgb_context *ctx) {
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->desc) cudaFree(ctx->desc);
     if (ctx->pack_desc) cudaFree(ctx->pack_desc);
+    if (ctx->tile_info) cudaFree(ctx->tile_info);
     if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
     for (auto &g : ctx->ev_pending)
@@ -710,8 +720,8 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
         out_rank = r;
     } else {
         hcgb_update u{A, B, *c};
-        hcgb_update_info *dinfo = nullptr;
-        HCGB_CUDA(ctx, cudaMalloc(&dinfo, sizeof(hcgb_update_info)));
+        if (!ctx->tile_info) HCGB_CUDA(ctx, cudaMalloc(&ctx->tile_info, sizeof(hcgb_update_info)));
+        hcgb_update_info *dinfo = ctx->tile_info;
         rc = hcgb_gemm_batch(ctx, alpha, beta, 1, &u, params, dinfo);
         int hstatus = HCGB_OK;
         if (rc == HCGB_OK) {
@@ -719,7 +729,6 @@ extern "C" int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *
             if (ck) HCGB_CUDA(ctx, cudaMemcpyAsync(&out_rank, c->rank, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
             HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
-        cudaFree(dinfo);
         if (rc) {
             cleanup();
             return rc;
@@ -814,8 +823,8 @@ extern "C" int hcgb_compress_tile(hcgb_context *ctx, const double *dense, int ro
     const size_t n = (size_t) cols;
     HCGB_CUDA(ctx, cudaMalloc(&ibuf, sizeof(double) * 2 * n * n));
     HCGB_CUDA(ctx, cudaMalloc(&irank, sizeof(int)));
-    identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf, cols, cols);
-    identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf + n * n, cols, cols);
+    { identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf, cols, cols); note_launch(); }
+    { identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf + n * n, cols, cols); note_launch(); }
     const int ncols = cols;
     HCGB_CUDA(ctx, cudaMemcpyAsync(irank, &ncols, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     HCGB_CUDA(ctx, cudaMemsetAsync(out->rank, 0, sizeof(int), ctx->stream));

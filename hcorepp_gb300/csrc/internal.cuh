@@ -204,6 +204,9 @@ void launch_syrk(int uplo, int trans, int n, int k, double alpha, const double *
 // Rank-trimmed packing of a tile list (pack.cu): offsets (n + 1) and the packed copy, or back.
 void launch_pack(const DevTile *tiles, int n, long long *offsets, double *packed, bool unpack, cudaStream_t st);
 
+// Every kernel launch of the library is counted (hcgb_kernel_launches reads the total).
+void note_launch();
+
 size_t qr_smem_bytes(int ld, int kmax);
 size_t svd_smem_bytes(int kmax);
 

@@ -18,7 +18,9 @@
 // Host code never dereferences `g_noalloc_scratch`: on the host that name is a stand-in, not a
 // device address.  The device address is obtained once per device with cudaGetSymbolAddress,
 // with that device current, on the first call made on that device; make that first call
-// before any stream capture begins.
+// before any stream capture begins.  The address is kept for the life of the process, so a
+// device reset (cudaDeviceReset, which unloads the module) after the first call is not
+// supported: the kept address would then be stale.
 #include <cstring>
 #include <mutex>
 
@@ -96,6 +98,11 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     const size_t sched_bytes = round_up_bytes(sizeof(int) * 4);
     if (slot_bytes + meta_bytes + desc_bytes + job_bytes + sched_bytes > sizeof(double) * HCGB_NOALLOC_SCRATCH_DOUBLES)
         return HCGB_POOL_TOO_SMALL;
+    // The QR panels and the core's bookkeeping live in shared memory: the same per-CTA limit as the
+    // allocating entry points, checked before anything is launched so that C stays untouched.
+    const size_t smem_limit = 227 * 1024;
+    if (ck && (qr_smem_bytes(ld, kmax) > smem_limit || svd_smem_bytes(kmax) > smem_limit))
+        return HCGB_POOL_TOO_SMALL;
 
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return HCGB_CUDA_ERROR;
@@ -154,7 +161,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     }
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    noalloc_set_update<<<1, 32, 0, st>>>(dup, u);
+    { noalloc_set_update<<<1, 32, 0, st>>>(dup, u); note_launch(); }
     launch_plan(dup, 1, alpha, beta, ws, prm, jobs, st);
     if (ck) launch_stack(dup, 1, alpha, beta, ws, st);
     for (int ph = 0; ph < 3; ph++)

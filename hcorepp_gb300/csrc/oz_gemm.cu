@@ -240,7 +240,7 @@ void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int s
     if (njobs <= 0) return;
     const int smem = (int) (sizeof(__half) * OZ_S * (OZ_TM + OZ_TN) * OZ_LDS);
     cudaFuncSetAttribute(oz_gemm_jobs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    oz_gemm_jobs_kernel<<<sms, OZ_THREADS, smem, st>>>(jobs, njobs, sched);
+    { oz_gemm_jobs_kernel<<<sms, OZ_THREADS, smem, st>>>(jobs, njobs, sched); note_launch(); }
 }
 
 }  // namespace hcgb

@@ -78,8 +78,8 @@ __global__ void __launch_bounds__(256) pack_kernel(const DevTile *tiles, int n, 
 }  // namespace
 
 void launch_pack(const DevTile *tiles, int n, long long *offsets, double *packed, bool unpack, cudaStream_t st) {
-    pack_offsets_kernel<<<1, 1024, 0, st>>>(tiles, n, offsets);
-    pack_kernel<<<n, 256, 0, st>>>(tiles, n, offsets, packed, unpack ? 1 : 0);
+    { pack_offsets_kernel<<<1, 1024, 0, st>>>(tiles, n, offsets); note_launch(); }
+    { pack_kernel<<<n, 256, 0, st>>>(tiles, n, offsets, packed, unpack ? 1 : 0); note_launch(); }
 }
 
 }  // namespace hcgb

@@ -52,17 +52,17 @@ int measure_fp64_peak(cudaStream_t st, double *dmma_tflops, double *dfma_tflops)
     const int blocks = sms * 4, threads = 256;
     float ms = 0.f;
     // DMMA: each warp-level m8n8k4 is 8*8*4 FMAs.
-    dmma_probe_kernel<<<blocks, threads, 0, st>>>(sink, 1e-3);
+    { dmma_probe_kernel<<<blocks, threads, 0, st>>>(sink, 1e-3); note_launch(); }
     cudaEventRecord(e0, st);
-    dmma_probe_kernel<<<blocks, threads, 0, st>>>(sink, 1e-3);
+    { dmma_probe_kernel<<<blocks, threads, 0, st>>>(sink, 1e-3); note_launch(); }
     cudaEventRecord(e1, st);
     cudaEventSynchronize(e1);
     cudaEventElapsedTime(&ms, e0, e1);
     const double dmma_flops = 2.0 * 256.0 * 8 * PROBE_ITERS * (double) blocks * (threads / 32);
     if (dmma_tflops) *dmma_tflops = dmma_flops / (ms * 1e-3) / 1e12;
-    dfma_probe_kernel<<<blocks, threads, 0, st>>>(sink, 0.999999, 1e-7);
+    { dfma_probe_kernel<<<blocks, threads, 0, st>>>(sink, 0.999999, 1e-7); note_launch(); }
     cudaEventRecord(e0, st);
-    dfma_probe_kernel<<<blocks, threads, 0, st>>>(sink, 0.999999, 1e-7);
+    { dfma_probe_kernel<<<blocks, threads, 0, st>>>(sink, 0.999999, 1e-7); note_launch(); }
     cudaEventRecord(e1, st);
     cudaEventSynchronize(e1);
     cudaEventElapsedTime(&ms, e0, e1);

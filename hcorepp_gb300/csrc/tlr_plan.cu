@@ -545,20 +545,20 @@ __global__ void __launch_bounds__(256) wy_solve_kernel(Workspace ws) {
 }  // namespace
 
 void launch_plan_wy(const DevUpdate *ups, int n, Workspace ws, Params p, GemmJob *jobs, cudaStream_t st) {
-    plan_wy_kernel<<<(n + 127) / 128, 128, 0, st>>>(ups, n, ws, p, jobs);
+    { plan_wy_kernel<<<(n + 127) / 128, 128, 0, st>>>(ups, n, ws, p, jobs); note_launch(); }
 }
 
 void launch_wy_solve(int n, Workspace ws, cudaStream_t st) {
-    wy_solve_kernel<<<2 * n, 256, 0, st>>>(ws);
+    { wy_solve_kernel<<<2 * n, 256, 0, st>>>(ws); note_launch(); }
 }
 
 void launch_transpose(const double *src, int lds, int rows, int cols, double *dst, int ldd, cudaStream_t st) {
-    transpose_kernel<<<1, 256, 0, st>>>(src, lds, rows, cols, dst, ldd);
+    { transpose_kernel<<<1, 256, 0, st>>>(src, lds, rows, cols, dst, ldd); note_launch(); }
 }
 
 void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p, GemmJob *jobs,
                  cudaStream_t st) {
-    plan_kernel<<<(n + 127) / 128, 128, 0, st>>>(ups, n, alpha, beta, ws, p, jobs);
+    { plan_kernel<<<(n + 127) / 128, 128, 0, st>>>(ups, n, alpha, beta, ws, p, jobs); note_launch(); }
 }
 
 __global__ void __launch_bounds__(256) gather_ranks_kernel(const int *const *ptrs, int n, int *out) {
@@ -567,15 +567,15 @@ __global__ void __launch_bounds__(256) gather_ranks_kernel(const int *const *ptr
 }
 
 void launch_gather_ranks(const int *const *ptrs, int n, int *out, cudaStream_t st) {
-    if (n > 0) gather_ranks_kernel<<<(n + 255) / 256, 256, 0, st>>>(ptrs, n, out);
+    if (n > 0) { gather_ranks_kernel<<<(n + 255) / 256, 256, 0, st>>>(ptrs, n, out); note_launch(); }
 }
 
 void launch_order(int n, Workspace ws, cudaStream_t st) {
-    order_kernel<<<1, 1024, 0, st>>>(n, ws);
+    { order_kernel<<<1, 1024, 0, st>>>(n, ws); note_launch(); }
 }
 
 void launch_stack(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, cudaStream_t st) {
-    stack_kernel<<<n, 256, 0, st>>>(ups, alpha, beta, ws);
+    { stack_kernel<<<n, 256, 0, st>>>(ups, alpha, beta, ws); note_launch(); }
 }
 
 static int device_sms() {
@@ -591,18 +591,18 @@ void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t s
     const int sms = device_sms();
     for (int off = 0; off < njobs; off += MAX_JOBS_PER_LAUNCH) {
         const int nj = njobs - off < MAX_JOBS_PER_LAUNCH ? njobs - off : MAX_JOBS_PER_LAUNCH;
-        schedule_kernel<<<1, 1024, 0, st>>>(jobs + off, nj, sched);
-        gemm_jobs_kernel<<<4 * sms, 128, 0, st>>>(jobs + off, nj, sched);
+        { schedule_kernel<<<1, 1024, 0, st>>>(jobs + off, nj, sched); note_launch(); }
+        { gemm_jobs_kernel<<<4 * sms, 128, 0, st>>>(jobs + off, nj, sched); note_launch(); }
         launch_oz_gemm_jobs(jobs + off, nj, sched + nj + 1, sms, st);
     }
 }
 
 void launch_finalize(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st) {
-    finalize_kernel<<<n, 256, 0, st>>>(ups, ws, info);
+    { finalize_kernel<<<n, 256, 0, st>>>(ups, ws, info); note_launch(); }
 }
 
 void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t st) {
-    ddc_finalize_kernel<<<n, 256, 0, st>>>(ups, ws);
+    { ddc_finalize_kernel<<<n, 256, 0, st>>>(ups, ws); note_launch(); }
 }
 
 Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch, bool wy) {

@@ -723,10 +723,10 @@ void launch_qr(Workspace ws, int n, bool mixed, cudaStream_t st) {
         const int pair = qr_pair_fits(smem) ? 1 : 0;
         const size_t cta = pair ? 2 * smem : smem;
         cudaFuncSetAttribute(qr_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) cta);
-        qr_kernel_df<<<2 * n, QRD_THREADS, cta, st>>>(ws, n, (int) (smem / sizeof(double)), pair);
+        { qr_kernel_df<<<2 * n, QRD_THREADS, cta, st>>>(ws, n, (int) (smem / sizeof(double)), pair); note_launch(); }
     } else {
         cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-        qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws);
+        { qr_kernel<<<2 * n, QR_THREADS, smem, st>>>(ws); note_launch(); }
     }
 }
 
@@ -736,12 +736,12 @@ void launch_apply_q(const DevUpdate *ups, int n, Workspace ws, bool mixed, cudaS
         const int pair = qr_pair_fits(smem) ? 1 : 0;
         const size_t cta = pair ? 2 * smem : smem;
         cudaFuncSetAttribute(apply_q_kernel_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) cta);
-        apply_q_kernel_df<<<2 * n, QRD_THREADS, cta, st>>>(ups, ws, n, (int) (smem / sizeof(double)), pair);
+        { apply_q_kernel_df<<<2 * n, QRD_THREADS, cta, st>>>(ups, ws, n, (int) (smem / sizeof(double)), pair); note_launch(); }
         return;
     }
     const size_t smem = qr_smem_bytes(ws.ld, ws.kmax);
     cudaFuncSetAttribute(apply_q_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    apply_q_kernel<<<2 * n, QR_THREADS, smem, st>>>(ups, ws);
+    { apply_q_kernel<<<2 * n, QR_THREADS, smem, st>>>(ups, ws); note_launch(); }
 }
 
 }  // namespace hcgb

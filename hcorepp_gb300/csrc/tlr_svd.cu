@@ -1013,7 +1013,7 @@ static void launch_core_svd_t(const DevUpdate *ups, int n, Workspace ws, Params 
     int kthr = 0;
     while ((long) (kthr + 1) * (kthr + 1) <= pool) kthr++;
     cudaFuncSetAttribute(core_svd_kernel<RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    core_svd_kernel<RPL><<<n, SVD_THREADS, smem, st>>>(ups, n, ws, p, team, kthr);
+    { core_svd_kernel<RPL><<<n, SVD_THREADS, smem, st>>>(ups, n, ws, p, team, kthr); note_launch(); }
 }
 
 // Rows of M are at most min(ld, kmax); the register tile of a rotation covers 32 * RPL rows.

@@ -474,6 +474,30 @@ class TileMatrix:
                 out[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb] = blk
         return out
 
+    def to_dense_device(self) -> torch.Tensor:
+        """The whole matrix as one dense device tensor (U V of every compressed tile), for accuracy
+        checks of large grids without a host round trip of the dense matrix."""
+        nb = self.nb
+        out = torch.zeros((self.mt * nb, self.nt * nb), dtype=torch.float64, device=self.arena.device)
+        ranks = self.ranks.cpu().numpy()
+        for j in range(self.nt):
+            for i in range(self.mt):
+                idx = self.index(i, j)
+                o = int(self.offsets[idx])
+                dst = out[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb]
+                if self.kinds[i][j] == L.DENSE:
+                    dst.copy_(self.arena[o:o + nb * nb].view(nb, nb).t())
+                    continue
+                r = int(ranks[idx])
+                if r == 0:
+                    continue
+                u = self.arena[o:o + nb * r].view(r, nb).t()
+                vo = o + nb * self.max_rank
+                vreg = self.arena[vo:vo + r * nb]
+                v = vreg.view(r, nb) if self.vt else vreg.view(nb, r).t()
+                dst.copy_(u @ v)
+        return out
+
     def rank_grid(self) -> np.ndarray:
         return self.ranks.cpu().numpy().reshape((self.nt, self.mt)).T.copy()
 

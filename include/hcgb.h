@@ -242,6 +242,10 @@ int hcgb_profile_enable(hcgb_context *ctx, int enable);
 int hcgb_profile_reset(hcgb_context *ctx);
 int hcgb_profile_read(hcgb_context *ctx, double *ms_per_stage, long long *launches_per_stage, int nstages);
 
+/* Number of kernels this library has launched in this process so far (all devices, all
+ * contexts).  The difference across a region counts the library's launches in it. */
+long long hcgb_kernel_launches(void);
+
 /* Measures this device's FP64 throughput with two probe kernels (~0.1 s): the FP64 tensor-core
  * MMA (DMMA) rate and the FP64 FMA rate of the SIMT pipes, in TFLOP/s.  These are the roofline
  * denominators of the FP64 path. */
@@ -260,7 +264,8 @@ int hcgb_fp64_peak(hcgb_context *ctx, double *dmma_tflops, double *dfma_tflops);
  * HCGB_POOL_TOO_SMALL (tiles up to 512 x 512 with capacities max_rank <= 170 fit).  All calls on a
  * device share the array: calls that overlap on the GPU race, so order them.  The first call on
  * each device looks up the array's device address (with that device current); make it before any
- * stream capture begins. */
+ * stream capture begins.  The address is kept for the life of the process: a device reset
+ * (cudaDeviceReset) after that first call is not supported. */
 int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hcgb_tile *b, double beta, hcgb_tile *c,
                            const hcgb_params *params, void *stream, hcgb_update_info *info_dev);
 

@@ -3,6 +3,8 @@ from its sources where they lie, against the BLAS++/LAPACK++ shim in oracle/shim
 and SciPy's bundled OpenBLAS.  Test infrastructure only.
 
 Usage: python oracle/build_ref.py [REFERENCE_ROOT]
+The reference root is the argument, else the environment variable HCOREPP_REFERENCE_ROOT, else
+the read-only checkout this recipe was written against (DEFAULT_REFERENCE_ROOT).
 Outputs go to oracle/_ref/ only.  Nothing is copied out of the reference tree.
 The reference's own build system (CMake + network fetches) is not used.
 """
@@ -16,6 +18,15 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root(argv=None) -> str:
+    """Where the reference sources are read from: argv[1], $HCOREPP_REFERENCE_ROOT, or the default."""
+    argv = sys.argv if argv is None else argv
+    if len(argv) > 1:
+        return argv[1]
+    return os.environ.get("HCOREPP_REFERENCE_ROOT", DEFAULT_REFERENCE_ROOT)
 
 # The CPU backend of the TLR GEMM path (and what it links against).
 SOURCES = [
@@ -75,5 +86,4 @@ def build(ref_root: str, verbose: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    print(build(root, verbose=True))
+    print(build(reference_root(), verbose=True))

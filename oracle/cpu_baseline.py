@@ -29,15 +29,22 @@ def _to_oracle(t):
 
 
 def _run_chain(ij):
+    """One C tile's k-chain in ascending k.  Returns the update count, the chain's time, the rank
+    after every update and the final tile (U, V; or the dense tile), the last two for the parity
+    check of the GPU result (gathered after the chain, outside its time)."""
     from oracle import hcore_oracle as O
     i, j = ij
     a, b, c, p = _STATE["a"], _STATE["b"], _STATE["c"], _STATE["params"]
     nt = int(round(len(b) ** 0.5))
     ct = _to_oracle(c[(i, j)])
-    t0 = time.perf_counter()
+    ranks = []
+    t0 = time.monotonic()  # system-wide clock: comparable across the pool's processes
     for k in range(nt):
-        O.hcore_gemm(1.0, _to_oracle(a[(i, k)]), _to_oracle(b[(k, j)]), 1.0, ct, p)
-    return nt, time.perf_counter() - t0
+        info = O.hcore_gemm(1.0, _to_oracle(a[(i, k)]), _to_oracle(b[(k, j)]), 1.0, ct, p)
+        ranks.append(info.get("rank"))
+    t1 = time.monotonic()
+    final = ("D", ct.data) if ct.kind == "dense" else ("C", ct.u, ct.v)
+    return nt, (t0, t1), ranks, final
 
 
 def _ping(_):
@@ -52,8 +59,10 @@ def sample_tiles(nt: int, count: int, seed: int = 1234):
     return [(int(x) % nt, int(x) // nt) for x in idx]
 
 
-def run(a_tiles, b_tiles, c_tiles, params, sample, processes: int):
-    """Returns (updates, wall seconds).  Tiles: dict (i, j) -> ("D", dense) | ("C", u, v, max_rank)."""
+def run(a_tiles, b_tiles, c_tiles, params, sample, processes: int, results: dict | None = None):
+    """Returns (updates, wall seconds).  Tiles: dict (i, j) -> ("D", dense) | ("C", u, v, max_rank).
+    If `results` is given it receives, per sampled C tile (i, j), the oracle's rank after every
+    update (k ascending) and its final tile."""
     # Only ship the tiles the sample touches.
     nt = int(round(len(b_tiles) ** 0.5))
     rows = sorted({i for i, _ in sample})
@@ -71,7 +80,11 @@ def run(a_tiles, b_tiles, c_tiles, params, sample, processes: int):
     with single_threaded_blas_env(), ctx.Pool(processes=processes, initializer=_worker_init,
                                               initargs=(a_sub, b_full, c_sub, params)) as pool:
         pool.map(_ping, range(processes * 2), chunksize=1)
-        t0 = time.perf_counter()
         out = pool.map(_run_chain, sample, chunksize=1)
-        wall = time.perf_counter() - t0
+    # Wall time of the sample: first chain start to last chain end (the results' transfer back to
+    # this process is not part of it).
+    wall = max(o[1][1] for o in out) - min(o[1][0] for o in out)
+    if results is not None:
+        for ij, o in zip(sample, out):
+            results[ij] = {"ranks": o[2], "final": o[3]}
     return sum(o[0] for o in out), wall

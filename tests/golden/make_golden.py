@@ -74,4 +74,6 @@ def main(root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, str(Path(__file__).resolve().parents[2]))
+    from oracle.build_ref import reference_root
+    main(reference_root())
