@@ -183,7 +183,7 @@ class Context:
             pass
 
 
-PLAIN_FP64, MIXED = 0, 1
+PLAIN_FP64, MIXED, TF32, BF16 = 0, 1, 2, 3
 
 
 def kernel_launches() -> int:

@@ -215,7 +215,7 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     mark(HCGB_STAGE_GEMM);
     for (int ph = 0; ph < 3; ph++)
         if (sh.p_m[ph] > 0 && sh.p_n[ph] > 0) {
-            launch_gemm_jobs(djobs + (size_t) ph * n, n, sched, st);
+            launch_gemm_jobs(djobs + (size_t) ph * n, n, sched, st, lowp_prec(p.mode) != 0);
             cnt[HCGB_STAGE_GEMM]++;
         }
     mark(HCGB_STAGE_QR);
@@ -233,14 +233,17 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     }
     mark(HCGB_STAGE_APPLY_Q);
     if (sh.any_compressed_c) {
-        if (p.oz && p.mode != 1 && ws.off_w) {  // the mixed form's float-float panels are faster
+        // WY form: the plain form with the tensor-core products (sides >= WY_MIN_REFLECTORS), and every
+        // side in the low-precision forms; the mixed form's float-float panels are faster than either.
+        const bool lowp = lowp_prec(p.mode) != 0;
+        if (((p.oz && p.mode == HCGB_PLAIN_FP64) || lowp) && ws.off_w) {
             // Sides with >= WY_MIN_REFLECTORS reflectors in full WY form: the Grams, Y = V^T X and
             // X -= V W are products (tensor-core eligible), only the small triangular solve stays on
             // the FP64 pipe.  The others keep the panel-wise kernel.
             launch_plan_wy(dups, n, ws, p, djobs, st);
-            launch_gemm_jobs(djobs, 4 * n, sched, st);  // Grams and Y = V^T X (independent)
+            launch_gemm_jobs(djobs, 4 * n, sched, st, lowp);  // Grams and Y = V^T X (independent)
             launch_wy_solve(n, ws, st);
-            launch_gemm_jobs(djobs + 4 * (size_t) n, 2 * n, sched, st);
+            launch_gemm_jobs(djobs + 4 * (size_t) n, 2 * n, sched, st, lowp);
         }
         launch_apply_q(dups, n, ws, p.mode == 1, st);  // the sides not applied in WY form (plan_kernel zeroes META_WY)
         cnt[HCGB_STAGE_APPLY_Q]++;
@@ -252,12 +255,12 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     if (ctx->prof) ctx->ev_pending.push_back(ev);
 }
 
-int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, Workspace *out) {
+int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, Workspace *out, int mode = 0) {
     // The QR panels and the core's bookkeeping live in shared memory: refuse shapes beyond it.
     const size_t smem_limit = 227 * 1024;
     if (sh.any_compressed_c && (qr_smem_bytes(sh.ld, sh.kmax) > smem_limit || svd_smem_bytes(sh.kmax) > smem_limit))
         return fail(ctx, HCGB_POOL_TOO_SMALL, "tile too large: the QR panel or core bookkeeping exceeds shared memory");
-    Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, ddc, ctx->oz != 0);
+    Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, ddc, ctx->oz != 0 || lowp_prec(mode) != 0);
     size_t need = workspace_bytes_for(w, n);
     int rc = ensure_device(ctx, &ctx->ws, &ctx->ws_bytes, need);
     if (rc) return rc;
@@ -369,7 +372,7 @@ int hcgb_gemm_batch(hcgb_context *ctx, double alpha, double beta, int n, const h
     }
     BatchShape sh = shape_of(updates, n);
     Workspace ws;
-    int rc = prepare_workspace(ctx, sh, n, false, &ws);
+    int rc = prepare_workspace(ctx, sh, n, false, &ws, params ? params->mode : 0);
     if (rc) return rc;
     DevUpdate *dups;
     GemmJob *djobs;
@@ -485,7 +488,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     }
     BatchShape sh = shape_of(all.data(), (int) all.size());
     Workspace ws;
-    int rc = prepare_workspace(ctx, sh, n, false, &ws);
+    int rc = prepare_workspace(ctx, sh, n, false, &ws, params ? params->mode : 0);
     if (rc) return rc;
     const size_t ub = sizeof(DevUpdate) * dv.size(), ub_al = (ub + 255) / 256 * 256;
     const size_t jb = sizeof(GemmJob) * JOBS_PER_UPDATE * (size_t) n, jb_al = (jb + 255) / 256 * 256;
@@ -1018,7 +1021,7 @@ extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *gr
             std::vector<DevUpdate> part(dv.begin() + off, dv.begin() + off + n);
             BatchShape sh = shape_of(hu.data() + off, n);
             Workspace ws;
-            int rc = prepare_workspace(ctx, sh, n, false, &ws);
+            int rc = prepare_workspace(ctx, sh, n, false, &ws, p.mode);
             if (rc) return done(rc);
             DevUpdate *dups;
             GemmJob *djobs;

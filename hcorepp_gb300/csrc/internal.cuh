@@ -70,6 +70,7 @@ struct GemmJob {
     double alpha, beta;
     int oz;          // 1: computed on the 16-bit tensor cores by error-free splitting (oz_gemm.cu)
     int triA, triB;  // 1: the stored operand is read as unit lower trapezoidal (Householder vectors)
+    int prec;        // 0: FP64-accurate (DMMA or oz); 1: TF32, 2: BF16 on tcgen05 (tc_gemm.cu)
 };
 
 constexpr int JOBS_PER_UPDATE = 6;  // job slots per update: 3 factor-product phases, 6 for the WY application
@@ -85,6 +86,9 @@ __device__ __forceinline__ double job_b(const GemmJob &jb, int k, int j) {
     if (jb.triB && r <= c) return r == c ? 1.0 : 0.0;
     return jb.B[r + (size_t) c * jb.ldb];
 }
+
+// Precision of the factor products and of the WY Q-application products in arithmetic form `mode`.
+__host__ __device__ inline int lowp_prec(int mode) { return mode == HCGB_TF32 ? 1 : (mode == HCGB_BF16 ? 2 : 0); }
 
 // Products worth the split (enough k to amortise the 4 FP64 instructions per output, enough outputs
 // for a tile).
@@ -155,7 +159,8 @@ struct Params {
     int truncated;
     int fixed_rank;
     int side_mode;   // 0: always the reference's [Cu | alpha Au]; 1: pick the smaller stack
-    int mode;        // 0: plain FP64; 1: mixed (single-precision Jacobi preconditioning of the core)
+    int mode;        // hcgb_mode: 0 plain FP64; 1 float-float QR / core / Q application; 2 / 3 TF32 / BF16
+                     // factor products and Q-application products (QR, core, truncation in FP64)
     int oz;          // 1: large factor products on the 16-bit tensor cores (FP64-accurate splitting)
 };
 
@@ -169,10 +174,14 @@ void launch_order(int n, Workspace ws, cudaStream_t st);
 // out[i] = *ptrs[i] (device rank ints gathered for one host read).
 void launch_gather_ranks(const int *const *ptrs, int n, int *out, cudaStream_t st);
 // Batched products: sched = device scratch of 2 * njobs + 2 ints (tile prefix sums), njobs <= 4096.
-void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t st);
+// has_lowp: the list may hold TF32 / BF16 jobs (launches the tcgen05 kernel too).
+void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t st, bool has_lowp = false);
 void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int sms, cudaStream_t st);
+void launch_tc_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int sms, cudaStream_t st);
+// Bounded mbarrier waits of the tcgen05 kernels that gave up (0 unless something else failed).
+unsigned int tc_wait_timeouts();
 constexpr int MAX_JOBS_PER_LAUNCH = 4096;
-constexpr int SCHED_INTS_PER_UPDATE = 10;  // >= (2 * 4n + 2) / n: one WY launch schedules 4n jobs
+constexpr int SCHED_INTS_PER_UPDATE = 16;  // >= (3 * 4n + 3) / n: one WY launch schedules 4n jobs, 3 tile lists
 // Q application in full WY form (Q = I - V T V^T, T^-1 = striu(V^T V) + diag(1/tau)): jobs for
 // the Grams, Y = V^T X and X -= V W, then the triangular solve T^-1 W = Y.  Used for the sides
 // with at least WY_MIN_REFLECTORS reflectors (their products run on the tensor cores); the

@@ -77,6 +77,8 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     if (a->cols != b->rows || a->rows != c->rows || b->cols != c->cols) return HCGB_BAD_ARG;
     const bool ak = a->kind == HCGB_COMPRESSED, bk = b->kind == HCGB_COMPRESSED, ck = c->kind == HCGB_COMPRESSED;
     if (!ak && !bk && ck) return HCGB_UNSUPPORTED;  // DDC re-shapes the tile: hcgb_tile_gemm only
+    if (params && params->mode != HCGB_PLAIN_FP64 && params->mode != HCGB_MIXED)
+        return HCGB_UNSUPPORTED;  // the low-precision forms apply Q in WY form: hcgb_tile_gemm only
 
     // Scratch layout for this update, same as one slot of the batched path.
     const int ra = ak ? a->max_rank : 0, rb = bk ? b->max_rank : 0, rc = ck ? c->max_rank : 0;
@@ -95,7 +97,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     const size_t meta_bytes = round_up_bytes(sizeof(int) * META_INTS);
     const size_t desc_bytes = round_up_bytes(sizeof(DevUpdate));
     const size_t job_bytes = round_up_bytes(sizeof(GemmJob) * 3);
-    const size_t sched_bytes = round_up_bytes(sizeof(int) * 4);
+    const size_t sched_bytes = round_up_bytes(sizeof(int) * 8);  // three tile lists of one job
     if (slot_bytes + meta_bytes + desc_bytes + job_bytes + sched_bytes > sizeof(double) * HCGB_NOALLOC_SCRATCH_DOUBLES)
         return HCGB_POOL_TOO_SMALL;
     // The QR panels and the core's bookkeeping live in shared memory: the same per-CTA limit as the

@@ -26,6 +26,7 @@ __device__ __forceinline__ GemmJob make_job(const double *A, int lda, int opA, c
     j.beta = beta;
     j.oz = 0;
     j.triA = j.triB = 0;
+    j.prec = 0;
     return j;
 }
 
@@ -39,10 +40,13 @@ __global__ void plan_kernel(const DevUpdate *ups, int n, double alpha, double be
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     plan_update(ups, n, alpha, beta, ws, p, jobs, s);
-    // Large products go to the tensor-core path.
+    // Low-precision forms: every product on tcgen05 in TF32 / BF16; otherwise the large products go
+    // to the FP64-accurate tensor-core path.
+    const int lp = lowp_prec(p.mode);
     for (int ph = 0; ph < 3; ph++) {
         GemmJob &j = jobs[(size_t) ph * n + s];
-        j.oz = (p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K)) ? 1 : 0;
+        j.prec = (lp && j.M > 0 && j.N > 0) ? lp : 0;
+        j.oz = (!j.prec && p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K)) ? 1 : 0;
     }
 }
 
@@ -314,52 +318,48 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs, int
     }
 }
 
-// Tile counts of every job for the two GEMM kernels and their exclusive prefix sums:
-// sched[0 .. njobs] (FP64 DMMA, 64 x 64 tiles) and sched[njobs + 1 .. 2 njobs + 1] (tensor-core
-// path, 64 x 32 tiles).  One CTA; njobs up to 4 * 1024.
+// Tile counts of every job for the three GEMM kernels and their exclusive prefix sums:
+// sched[0 .. njobs] (FP64 DMMA, 64 x 64 tiles), sched[njobs + 1 .. 2 njobs + 1] (FP64-accurate
+// tensor-core path, 64 x 32 tiles) and sched[2 njobs + 2 .. 3 njobs + 2] (TF32 / BF16 on tcgen05,
+// 128 x 64 tiles).  One CTA; njobs up to 4 * 1024.
 __global__ void __launch_bounds__(1024) schedule_kernel(const GemmJob *jobs, int njobs, int *sched) {
-    __shared__ int part[2][1024];
+    constexpr int NL = 3;
+    __shared__ int part[NL][1024];
     constexpr int PER = 4;
-    int cd[PER], co[PER], sd = 0, so = 0;
+    int cnt[NL][PER], sum[NL] = {0, 0, 0};
     for (int q = 0; q < PER; q++) {
         const int j = threadIdx.x * PER + q;
-        cd[q] = co[q] = 0;
+        for (int l = 0; l < NL; l++) cnt[l][q] = 0;
         if (j < njobs) {
             const GemmJob &jb = jobs[j];
             if (jb.M > 0 && jb.N > 0 && jb.K >= 0) {
-                if (jb.oz) co[q] = ((jb.M + 63) / 64) * ((jb.N + 31) / 32);
-                else cd[q] = ((jb.M + GT - 1) / GT) * ((jb.N + GT - 1) / GT);
+                if (jb.prec) cnt[2][q] = ((jb.M + 127) / 128) * ((jb.N + 63) / 64);
+                else if (jb.oz) cnt[1][q] = ((jb.M + 63) / 64) * ((jb.N + 31) / 32);
+                else cnt[0][q] = ((jb.M + GT - 1) / GT) * ((jb.N + GT - 1) / GT);
             }
         }
-        sd += cd[q];
-        so += co[q];
+        for (int l = 0; l < NL; l++) sum[l] += cnt[l][q];
     }
-    part[0][threadIdx.x] = sd;
-    part[1][threadIdx.x] = so;
+    for (int l = 0; l < NL; l++) part[l][threadIdx.x] = sum[l];
     __syncthreads();
     // inclusive scan of the per-thread sums (Hillis-Steele over 1024 entries)
     for (int off = 1; off < 1024; off <<= 1) {
-        const int a = threadIdx.x >= off ? part[0][threadIdx.x - off] : 0;
-        const int b = threadIdx.x >= off ? part[1][threadIdx.x - off] : 0;
+        int add[NL];
+        for (int l = 0; l < NL; l++) add[l] = threadIdx.x >= off ? part[l][threadIdx.x - off] : 0;
         __syncthreads();
-        part[0][threadIdx.x] += a;
-        part[1][threadIdx.x] += b;
+        for (int l = 0; l < NL; l++) part[l][threadIdx.x] += add[l];
         __syncthreads();
     }
-    int rd = part[0][threadIdx.x] - sd, ro = part[1][threadIdx.x] - so;  // exclusive starts
+    int run[NL];
+    for (int l = 0; l < NL; l++) run[l] = part[l][threadIdx.x] - sum[l];  // exclusive starts
     for (int q = 0; q < PER; q++) {
         const int j = threadIdx.x * PER + q;
-        if (j < njobs) {
-            sched[j] = rd;
-            sched[njobs + 1 + j] = ro;
-        }
-        rd += cd[q];
-        ro += co[q];
+        if (j < njobs)
+            for (int l = 0; l < NL; l++) sched[l * (njobs + 1) + j] = run[l];
+        for (int l = 0; l < NL; l++) run[l] += cnt[l][q];
     }
-    if (threadIdx.x == 1023) {
-        sched[njobs] = part[0][1023];
-        sched[2 * njobs + 1] = part[1][1023];
-    }
+    if (threadIdx.x == 1023)
+        for (int l = 0; l < NL; l++) sched[l * (njobs + 1) + njobs] = part[l][1023];
 }
 
 // One CTA per update: V (r x n, ld r) = XV^T into the tile buffer, publish rank and record.
@@ -440,7 +440,7 @@ __global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params
     if (s >= n) return;
     GemmJob none;
     none.M = none.N = none.K = 0;
-    none.oz = none.triA = none.triB = 0;
+    none.oz = none.triA = none.triB = none.prec = 0;
     for (int q = 0; q < 6; q++) jobs[(size_t) q * n + s] = none;
     int *meta = ws.meta + (size_t) s * META_INTS;
     meta[META_WY] = 0;
@@ -451,7 +451,9 @@ __global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params
     const int ld = ws.ld, lk = ws.kmax;
     for (int side = 0; side < 2; side++) {
         const int rows = side ? nn : m, kk = rows < k ? rows : k;
-        if (!p.oz || kk < WY_MIN_REFLECTORS) continue;  // panel-wise apply_q_kernel
+        const int lp = lowp_prec(p.mode);  // low-precision forms: every side in WY form
+        if (!lp && (!p.oz || kk < WY_MIN_REFLECTORS)) continue;  // panel-wise apply_q_kernel
+        if (kk < 1) continue;
         meta[META_WY] |= 1 << side;
         double *Vst = base + (side ? ws.off_vstack : ws.off_ustack);
         double *G = base + (side ? ws.off_mcopy : ws.off_m);
@@ -464,10 +466,13 @@ __global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params
         y.triA = 1;
         GemmJob u = make_job(Vst, ld, 0, W, lk, 0, X, ldx, rows, r, kk, -1.0, 1.0);
         u.triA = 1;
+        // The Grams define the T factor of the QR and stay FP64-accurate; Y = V^T X and X - V W take
+        // the form's product precision.
+        y.prec = u.prec = lp;
         GemmJob *out[3] = {&g, &y, &u};
         for (int q = 0; q < 3; q++) {
             GemmJob &j = *out[q];
-            j.oz = (p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K)) ? 1 : 0;
+            j.oz = (!j.prec && p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K)) ? 1 : 0;
             jobs[(size_t) (2 * q + side) * n + s] = j;
         }
     }
@@ -587,13 +592,14 @@ static int device_sms() {
     return sms[dev] > 0 ? sms[dev] : 152;
 }
 
-void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t st) {
+void launch_gemm_jobs(const GemmJob *jobs, int njobs, int *sched, cudaStream_t st, bool has_lowp) {
     const int sms = device_sms();
     for (int off = 0; off < njobs; off += MAX_JOBS_PER_LAUNCH) {
         const int nj = njobs - off < MAX_JOBS_PER_LAUNCH ? njobs - off : MAX_JOBS_PER_LAUNCH;
         { schedule_kernel<<<1, 1024, 0, st>>>(jobs + off, nj, sched); note_launch(); }
         { gemm_jobs_kernel<<<4 * sms, 128, 0, st>>>(jobs + off, nj, sched); note_launch(); }
         launch_oz_gemm_jobs(jobs + off, nj, sched + nj + 1, sms, st);
+        if (has_lowp) launch_tc_gemm_jobs(jobs + off, nj, sched + 2 * (nj + 1), sms, st);
     }
 }
 

@@ -32,7 +32,7 @@ class CompressionParameters:
     truncated_svd: bool = False
     fixed_rank: int = 0
     op_type: int = GESDD
-    mode: int = L.PLAIN_FP64  # GB300 addition: HCGB_PLAIN_FP64 or HCGB_MIXED
+    mode: int = L.PLAIN_FP64  # GB300 addition: HCGB_PLAIN_FP64, HCGB_MIXED, HCGB_TF32 or HCGB_BF16
 
     def c(self) -> L.Params:
         return L.make_params(self.accuracy, self.truncated_svd, self.fixed_rank, self.use_trmm, self.use_ungqr,

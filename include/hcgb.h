@@ -77,7 +77,15 @@ typedef struct {
  * plain form at the accuracies this path is used at (>= 1e-12 relative), about 1.7x as fast.
  * In both forms the larger factor products run on the 16-bit tensor cores by FP64-accurate
  * error-free splitting unless hcgb_set_tensor_products(ctx, 0). */
-typedef enum { HCGB_PLAIN_FP64 = 0, HCGB_MIXED = 1 } hcgb_mode;
+typedef enum { HCGB_PLAIN_FP64 = 0, HCGB_MIXED = 1, HCGB_TF32 = 2, HCGB_BF16 = 3 } hcgb_mode;
+/* HCGB_TF32 / HCGB_BF16: the low-precision forms.  Every factor product and the two large products of
+ * the Q application (Y = V^T X and X - V W of the compact-WY form, used on every side) run on the
+ * fifth-generation tensor cores (tcgen05.mma kind::tf32 / kind::f16 with BF16 operands, FP32
+ * accumulation in tensor memory) after per-row / per-column power-of-two scaling of the operands.
+ * The Householder QR of the stacks (and its T factor), the core SVD and the truncation test stay in
+ * FP64.  The product error is that of TF32 (2^-11) / BF16 (2^-8) operand rounding: these forms do
+ * not reach accuracies below ~1e-3 relative; callers read the error and the rank growth off the
+ * result. */
 
 /* One tile update C <- alpha * A * B + beta * C (NoTrans operands). */
 typedef struct {
