@@ -76,6 +76,9 @@ def parse():
     ap.add_argument("--groups", type=int, default=8, help="independent C-tile groups (streams)")
     ap.add_argument("--k-order", type=int, default=1, choices=[0, 1],
                     help="0: ascending k per C tile (reference order); 1: costliest updates first")
+    ap.add_argument("--lowp", default="1e-4,1e-6,1e-8",
+                    help="accuracies of the TF32 / BF16 low-precision sweep ('' to skip)")
+    ap.add_argument("--lowp-steps", type=int, default=2, help="timed steps per low-precision run")
     return ap.parse_args()
 
 
@@ -150,12 +153,25 @@ class ClockSampler:
         self.dev = device_index
         self.proc = None
         self.out = None
+        self.lines = []
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line)
 
     def __enter__(self):
+        import threading
+        import time
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+            # the sampler is running (first sample read) before the timed region starts
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 15 and self.proc.poll() is None:
+                time.sleep(0.05)
         except Exception:
             self.proc = None
         return self
@@ -164,10 +180,11 @@ class ClockSampler:
         if self.proc is not None:
             self.proc.terminate()
             try:
-                self.out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
-                self.out = ""
+            self.reader.join(timeout=5)
+            self.out = "".join(self.lines)
         return False
 
     def summary(self):
@@ -367,15 +384,17 @@ def timed(torch, stream, steps, fn, world, sampler=None):
     return e0.elapsed_time(e1) / steps
 
 
-def measure_form(wb, form, mode, args, world, with_e2e=True):
+def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, steps=None, warmup=None):
     """Device-resident and end-to-end throughput of one form, its serialised stage times and its
     per-update records."""
     torch, L = wb.torch, wb.L
-    params = wb.params(mode)
+    params = wb.params(mode, accuracy)
+    steps = steps or args.steps
+    warmup = args.warmup if warmup is None else warmup
     ctx = wb.ctx
     ctx.set_concurrency(args.groups)
     ctx.set_k_order(args.k_order)
-    for _ in range(max(args.warmup, 1)):
+    for _ in range(max(warmup, 1)):
         wb.step(params, record_info=True)
     torch.cuda.synchronize()
     info_h = wb.info.cpu().numpy()
@@ -383,8 +402,8 @@ def measure_form(wb, form, mode, args, world, with_e2e=True):
     out = {"form": form, "note": FORM_NOTES.get(form, "")}
     l0 = L.kernel_launches()
     with ClockSampler(wb.local) as clk:
-        ms = timed(torch, stream, args.steps, lambda: wb.step(params), world)
-    launches = (L.kernel_launches() - l0) / args.steps
+        ms = timed(torch, stream, steps, lambda: wb.step(params), world)
+    launches = (L.kernel_launches() - l0) / steps
     value, ms = job_throughput(ms, wb.n_updates, device="cuda")
     out.update(value=value, ms_per_step=ms, gpu_launches_per_step=launches, clocks=clk.summary())
     # One more multiply, serialised on one stream with CUDA events around every stage: the
@@ -404,7 +423,7 @@ def measure_form(wb, form, mode, args, world, with_e2e=True):
         moved = {}
         wb.e2e_step(params, moved)
         torch.cuda.synchronize()
-        e2e_ms = timed(torch, stream, args.steps, lambda: wb.e2e_step(params, moved), world)
+        e2e_ms = timed(torch, stream, steps, lambda: wb.e2e_step(params, moved), world)
         e2e_value, e2e_ms = job_throughput(e2e_ms, wb.n_updates, device="cuda")
         out["e2e"] = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(moved["h2d"]),
                       "d2h_bytes_per_step": int(moved["d2h"]), "ms_per_step": e2e_ms,
@@ -515,6 +534,20 @@ def gpu_arm(args, rank, world, local):
     wb = Workbench(args, local)
     dmma_peak, dfma_peak = wb.ctx.fp64_peak()
     results = {f: measure_form(wb, f, modes[f], args, world) for f in forms}
+    # Low-precision forms (TF32 / BF16 products and Q-application products; QR, core SVD and the
+    # truncation test in FP64) at several accuracies, each beside the plain FP64 form at the same
+    # accuracy: throughput, error against the FP64 dense product, rank growth.
+    lowp = {}
+    for acc_s in [a for a in args.lowp.split(",") if a]:
+        acc = float(acc_s)
+        runs = {}
+        for name, mode in (("plain_fp64", L.PLAIN_FP64), ("tf32", L.TF32), ("bf16", L.BF16)):
+            if name == "plain_fp64" and acc == wb.w["accuracy"]:
+                runs[name] = results[HEADLINE_FORM]
+                continue
+            runs[name] = measure_form(wb, name, mode, args, world, with_e2e=False, accuracy=acc,
+                                      steps=args.lowp_steps, warmup=1)
+        lowp[acc_s] = runs
     if rank != 0:
         return 0
     head = results[HEADLINE_FORM]
@@ -529,9 +562,9 @@ def gpu_arm(args, rank, world, local):
         exact = Ad @ Ad + Cd0
         del Ad, Cd0
         nrm = torch.linalg.norm(exact)
-        for f in forms:
-            res = results[f]
-            res["rel_fro_err_vs_fp64_dense_product"] = float(torch.linalg.norm(res.pop("result_dense") - exact) / nrm)
+        for res in list(results.values()) + [r for runs in lowp.values() for r in runs.values()]:
+            if "result_dense" in res:
+                res["rel_fro_err_vs_fp64_dense_product"] = float(torch.linalg.norm(res.pop("result_dense") - exact) / nrm)
         torch.cuda.empty_cache()
 
     roof, extra = roofline_of(wb, head, HEADLINE_FORM, dmma_peak, dfma_peak, args)
@@ -573,6 +606,24 @@ def gpu_arm(args, rank, world, local):
             blk["serial_step_ms"] = x2["serial_step_ms"]
         form_blocks[f] = blk
 
+    lowp_block = {}
+    for acc_s, runs in lowp.items():
+        base = runs["plain_fp64"]
+        ent = {}
+        for name, res in runs.items():
+            ri = res["info"]
+            comp = ri[:, 4] > 0
+            ent[name] = {"value": res["value"], "unit": UNIT, "ms_per_step": res["ms_per_step"],
+                         "rel_fro_err_vs_fp64_dense_product": res.get("rel_fro_err_vs_fp64_dense_product"),
+                         "mean_final_rank": float(res["ranks_final"][comp_mask].mean()),
+                         "rank_growth_vs_plain_fp64": float(res["ranks_final"][comp_mask].mean() /
+                                                            max(base["ranks_final"][comp_mask].mean(), 1e-9)),
+                         "mean_k": float(ri[comp, 4].mean()) if comp.any() else 0.0,
+                         "updates_at_capacity": int(np.count_nonzero(ri[:, 5] >= maxr)),
+                         "speedup_over_plain_fp64_same_accuracy": res["value"] / base["value"],
+                         "gpu_launches_per_step": res["gpu_launches_per_step"]}
+        lowp_block[acc_s] = ent
+
     line = {
         "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -602,6 +653,11 @@ def gpu_arm(args, rank, world, local):
         "check": {"rel_fro_err_vs_fp64_dense_product": head.get("rel_fro_err_vs_fp64_dense_product")},
         "parity": parity,
         "forms": form_blocks,
+        "lowp_forms": {"note": "TF32 / BF16: factor products and the WY Q-application products on tcgen05 "
+                               "(FP32 accumulation in tensor memory, per-row / per-column power-of-two scaling); "
+                               "stack QR with its T factor, core SVD and truncation test in FP64. Each accuracy "
+                               "beside the plain FP64 form at that accuracy; errors against the FP64 dense "
+                               "product of the inputs.", "steps": args.lowp_steps, "by_accuracy": lowp_block},
         "cpu_baseline": cpu,
         "clocks": head["clocks"],
     }
