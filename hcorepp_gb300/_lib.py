@@ -48,11 +48,11 @@ class UpdateInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("rank_a", C.c_int), ("rank_b", C.c_int), ("rank_c", C.c_int),
                 ("k", C.c_int), ("new_rank", C.c_int), ("sweeps", C.c_int), ("side", C.c_int),
                 ("core_cols", C.c_int), ("kc_product", C.c_int), ("kc_qrcp", C.c_int), ("kc_jacobi", C.c_int),
-                ("kc_factors", C.c_int)]
+                ("kc_factors", C.c_int), ("sketch_cols", C.c_int), ("sketch_accepted", C.c_int)]
 
 
 INFO_FIELDS = [f[0] for f in UpdateInfo._fields_]
-STAGES = ["plan", "stack", "gemm", "qr", "core_svd", "apply_q", "finalize"]
+STAGES = ["plan", "stack", "gemm", "qr", "core_svd", "apply_q", "finalize", "sketch"]
 
 _LIB = None
 
@@ -107,6 +107,19 @@ def lib():
         L.hcgb_tile_gemm_noalloc.restype = C.c_int
         L.hcgb_kernel_launches.argtypes = []
         L.hcgb_kernel_launches.restype = C.c_longlong
+        L.hcgb_rank_model_create.argtypes = [vp, C.c_ulonglong, C.POINTER(vp)]
+        L.hcgb_rank_model_destroy.argtypes = [vp]
+        L.hcgb_rank_model_params.argtypes = [vp, vp, vp]
+        L.hcgb_rank_model_predict.argtypes = [vp, vp, ip, vp, vp]
+        L.hcgb_rank_model_gradient.argtypes = [vp, vp, ip, vp, vp, vp, C.POINTER(C.c_double)]
+        L.hcgb_rank_model_train.argtypes = [vp, vp, ip, vp, vp, ip, ip, C.c_float, C.c_ulonglong,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        L.hcgb_set_rank_model.argtypes = [vp, vp, ip]
+        L.hcgb_set_feature_sink.argtypes = [vp, vp]
+        for nm in ("hcgb_rank_model_create", "hcgb_rank_model_destroy", "hcgb_rank_model_params",
+                   "hcgb_rank_model_predict", "hcgb_rank_model_gradient", "hcgb_rank_model_train",
+                   "hcgb_set_rank_model", "hcgb_set_feature_sink"):
+            getattr(L, nm).restype = C.c_int
         for nm in ("hcgb_pack_tiles", "hcgb_unpack_tiles"):
             getattr(L, nm).argtypes = [vp, ip, C.POINTER(Tile), vp, vp]
             getattr(L, nm).restype = C.c_int

@@ -34,7 +34,8 @@ struct hcgb_context {
     // stage profiling
     bool prof = false;
     std::vector<cudaEvent_t> ev_free;
-    std::vector<std::vector<cudaEvent_t>> ev_pending;  // one group of HCGB_NUM_STAGES + 1 per pipeline
+    // one list of (stage, event) marks per pipeline; the time to the next mark belongs to the stage
+    std::vector<std::vector<std::pair<int, cudaEvent_t>>> ev_pending;
     double stage_ms[HCGB_NUM_STAGES] = {0};
     long long stage_launches[HCGB_NUM_STAGES] = {0};
     // independent C-tile groups of hcgb_tlr_gemm, one stream each
@@ -46,6 +47,16 @@ struct hcgb_context {
     void *pack_desc = nullptr;  // DevTile[] of hcgb_pack_tiles / hcgb_unpack_tiles
     size_t pack_desc_bytes = 0;
     hcgb_update_info *tile_info = nullptr;  // the one record hcgb_tile_gemm reads back (allocated once)
+    // learned form
+    bool learned = false;                     // the learned form is on
+    struct hcgb_rank_model *model = nullptr;  // rank predictor (policy 0)
+    int sk_policy = 0;                        // 0: sketch width from the predictor; 1: from the input ranks
+    unsigned long long sk_seed = 0x5eedULL;   // seed of the Gaussian test matrices
+    float *feature_sink = nullptr;            // device: per-update predictor features, indexed like info
+};
+
+struct hcgb_rank_model {
+    hcgb::RankModel m;
 };
 
 namespace {
@@ -163,8 +174,10 @@ BatchShape shape_of(const hcgb_update *ups, int n) {
     return s;
 }
 
-size_t workspace_bytes_for(const Workspace &w, int n) {
-    return sizeof(double) * w.slot_doubles * (size_t) n + sizeof(int) * (META_INTS + 1) * (size_t) n + 256;
+size_t workspace_bytes_for(const Workspace &w, int n, bool features = false) {
+    size_t b = sizeof(double) * w.slot_doubles * (size_t) n + sizeof(int) * (META_INTS + 1) * (size_t) n + 256;
+    if (features) b += sizeof(float) * (MLP_IN + 1) * (size_t) n + 256;
+    return b;
 }
 
 Params to_params(const hcgb_params *p, const hcgb_context *ctx) {
@@ -178,19 +191,15 @@ Params to_params(const hcgb_params *p, const hcgb_context *ctx) {
     return q;
 }
 
-std::vector<cudaEvent_t> take_events(hcgb_context *ctx, int count) {
-    std::vector<cudaEvent_t> ev;
-    for (int i = 0; i < count; i++) {
-        cudaEvent_t e;
-        if (!ctx->ev_free.empty()) {
-            e = ctx->ev_free.back();
-            ctx->ev_free.pop_back();
-        } else {
-            cudaEventCreate(&e);
-        }
-        ev.push_back(e);
+cudaEvent_t take_event(hcgb_context *ctx) {
+    cudaEvent_t e;
+    if (!ctx->ev_free.empty()) {
+        e = ctx->ev_free.back();
+        ctx->ev_free.pop_back();
+    } else {
+        cudaEventCreate(&e);
     }
-    return ev;
+    return e;
 }
 
 // Launch the full pipeline for n updates whose descriptors are already on the device.
@@ -198,12 +207,15 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
                      double alpha,
                      double beta, const Workspace &ws, const BatchShape &sh, const Params &p,
                      hcgb_update_info *info) {
-    std::vector<cudaEvent_t> ev;
-    if (ctx->prof) ev = take_events(ctx, HCGB_NUM_STAGES + 1);
-    auto mark = [&](int i) {
-        if (ctx->prof) cudaEventRecord(ev[i], st);
+    std::vector<std::pair<int, cudaEvent_t>> ev;
+    auto mark = [&](int stage) {
+        if (!ctx->prof) return;
+        cudaEvent_t e = take_event(ctx);
+        cudaEventRecord(e, st);
+        ev.push_back({stage, e});
     };
     long long *cnt = ctx->stage_launches;
+    const bool lowp = lowp_prec(p.mode) != 0;
     mark(HCGB_STAGE_PLAN);
     launch_plan(dups, n, alpha, beta, ws, p, djobs, st);
     cnt[HCGB_STAGE_PLAN]++;
@@ -215,43 +227,78 @@ void launch_pipeline(hcgb_context *ctx, cudaStream_t st, const DevUpdate *dups, 
     mark(HCGB_STAGE_GEMM);
     for (int ph = 0; ph < 3; ph++)
         if (sh.p_m[ph] > 0 && sh.p_n[ph] > 0) {
-            launch_gemm_jobs(djobs + (size_t) ph * n, n, sched, st, lowp_prec(p.mode) != 0);
+            launch_gemm_jobs(djobs + (size_t) ph * n, n, sched, st, lowp);
             cnt[HCGB_STAGE_GEMM]++;
         }
-    mark(HCGB_STAGE_QR);
-    // The heavy stages index updates through ws.order: it must be written for every launch
-    // that carries it (a single update included).
-    if (sh.any_compressed_c && ws.order) launch_order(n, ws, st);
-    if (sh.any_compressed_c) {
-        launch_qr(ws, n, p.mode == 1, st);
+    // Stack QR, core SVD, Q application and write-back of every update whose meta marks a compressed
+    // C, on the stacks of w.
+    auto recompress = [&](const Workspace &w, hcgb_update_info *inf) {
+        mark(HCGB_STAGE_QR);
+        // The heavy stages index updates through w.order: it must be written for every launch
+        // that carries it (a single update included).
+        if (w.order) launch_order(n, w, st);
+        launch_qr(w, n, p.mode == 1, st);
         cnt[HCGB_STAGE_QR]++;
-    }
-    mark(HCGB_STAGE_CORE_SVD);
-    if (sh.any_compressed_c) {
-        launch_core_svd(dups, n, ws, p, st);
+        mark(HCGB_STAGE_CORE_SVD);
+        launch_core_svd(dups, n, w, p, st);
         cnt[HCGB_STAGE_CORE_SVD]++;
-    }
-    mark(HCGB_STAGE_APPLY_Q);
-    if (sh.any_compressed_c) {
+        mark(HCGB_STAGE_APPLY_Q);
         // WY form: the plain form with the tensor-core products (sides >= WY_MIN_REFLECTORS), and every
         // side in the low-precision forms; the mixed form's float-float panels are faster than either.
-        const bool lowp = lowp_prec(p.mode) != 0;
-        if (((p.oz && p.mode == HCGB_PLAIN_FP64) || lowp) && ws.off_w) {
-            // Sides with >= WY_MIN_REFLECTORS reflectors in full WY form: the Grams, Y = V^T X and
-            // X -= V W are products (tensor-core eligible), only the small triangular solve stays on
-            // the FP64 pipe.  The others keep the panel-wise kernel.
-            launch_plan_wy(dups, n, ws, p, djobs, st);
+        if (((p.oz && p.mode == HCGB_PLAIN_FP64) || lowp) && w.off_w) {
+            // Sides in full WY form: the Grams, Y = V^T X and X -= V W are products (tensor-core
+            // eligible), only the small triangular solve stays on the FP64 pipe.  The others keep the
+            // panel-wise kernel.
+            launch_plan_wy(dups, n, w, p, djobs, st);
             launch_gemm_jobs(djobs, 4 * n, sched, st, lowp);  // Grams and Y = V^T X (independent)
-            launch_wy_solve(n, ws, st);
+            launch_wy_solve(n, w, st);
             launch_gemm_jobs(djobs + 4 * (size_t) n, 2 * n, sched, st, lowp);
         }
-        launch_apply_q(dups, n, ws, p.mode == 1, st);  // the sides not applied in WY form (plan_kernel zeroes META_WY)
+        launch_apply_q(dups, n, w, p.mode == 1, st);  // the sides not applied in WY form (plan_kernel zeroes META_WY)
         cnt[HCGB_STAGE_APPLY_Q]++;
+        mark(HCGB_STAGE_FINALIZE);
+        launch_finalize(dups, n, w, inf, st);
+        cnt[HCGB_STAGE_FINALIZE]++;
+    };
+    const bool features = sh.any_compressed_c && ws.feat && (ctx->feature_sink || ctx->learned);
+    const bool learned = ctx->learned && sh.any_compressed_c && p.fixed_rank == 0 && ws.off_sk1 && ws.pred;
+    if (features) {
+        mark(HCGB_STAGE_SKETCH);
+        launch_features(dups, n, ws, p.accuracy, ctx->feature_sink, st);
     }
-    mark(HCGB_STAGE_FINALIZE);
-    launch_finalize(dups, n, ws, info, st);
-    cnt[HCGB_STAGE_FINALIZE]++;
-    mark(HCGB_NUM_STAGES);
+    if (learned) {
+        // Randomized sketch sized by the predictor, then the plain recompression on the sketch
+        // (pass A) and, for every update not sketched or whose residual test failed, on the
+        // original stacks (pass B).
+        mark(HCGB_STAGE_SKETCH);
+        if (ctx->sk_policy == 0) launch_mlp_forward(ctx->model->m, ws.feat, n, ws.pred, st);  // y = log2(1 + r)
+        launch_sketch_plan(dups, n, ws, p, ctx->sk_policy, ctx->sk_seed, djobs, st);
+        launch_gemm_jobs(djobs, n, sched, st, lowp);                 // Z = V_s^T Omega
+        launch_gemm_jobs(djobs + (size_t) n, n, sched, st, lowp);    // Y = U_s Z
+        launch_sketch_qr(n, ws, st);
+        launch_sketch_plan2(n, ws, p, djobs, st);
+        launch_gemm_jobs(djobs, n, sched, st, lowp);                 // W = U_s^T Q_Y
+        launch_gemm_jobs(djobs + (size_t) n, n, sched, st, lowp);    // V' = V_s W
+        launch_sketch_pass(n, ws, p, 0, st);
+        cnt[HCGB_STAGE_SKETCH]++;
+        Workspace wsk = ws;
+        wsk.off_ustack = ws.off_sk1;
+        wsk.off_vstack = ws.off_sk2;
+        recompress(wsk, nullptr);
+        mark(HCGB_STAGE_SKETCH);
+        launch_sketch_pass(n, ws, p, 1, st);
+        recompress(ws, nullptr);
+        mark(HCGB_STAGE_SKETCH);
+        launch_sketch_pass(n, ws, p, 2, st);
+        launch_learned_records(dups, n, ws, info, st);
+    } else if (sh.any_compressed_c) {
+        recompress(ws, info);
+    } else {
+        mark(HCGB_STAGE_FINALIZE);
+        launch_finalize(dups, n, ws, info, st);
+        cnt[HCGB_STAGE_FINALIZE]++;
+    }
+    mark(-1);
     if (ctx->prof) ctx->ev_pending.push_back(ev);
 }
 
@@ -260,13 +307,20 @@ int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, 
     const size_t smem_limit = 227 * 1024;
     if (sh.any_compressed_c && (qr_smem_bytes(sh.ld, sh.kmax) > smem_limit || svd_smem_bytes(sh.kmax) > smem_limit))
         return fail(ctx, HCGB_POOL_TOO_SMALL, "tile too large: the QR panel or core bookkeeping exceeds shared memory");
-    Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, ddc, ctx->oz != 0 || lowp_prec(mode) != 0);
-    size_t need = workspace_bytes_for(w, n);
+    const bool learned = ctx->learned, features = learned || ctx->feature_sink;
+    Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, ddc, ctx->oz != 0 || lowp_prec(mode) != 0, learned);
+    size_t need = workspace_bytes_for(w, n, features);
     int rc = ensure_device(ctx, &ctx->ws, &ctx->ws_bytes, need);
     if (rc) return rc;
     w.base = static_cast<double *>(ctx->ws);
     w.meta = reinterpret_cast<int *>(static_cast<char *>(ctx->ws) + sizeof(double) * w.slot_doubles * (size_t) n);
     w.order = w.meta + (size_t) META_INTS * n;
+    if (features) {
+        const size_t fo = (sizeof(double) * w.slot_doubles * (size_t) n + sizeof(int) * (META_INTS + 1) * (size_t) n +
+                           255) / 256 * 256;
+        w.feat = reinterpret_cast<float *>(static_cast<char *>(ctx->ws) + fo);
+        w.pred = w.feat + (size_t) MLP_IN * n;
+    }
     *out = w;
     return HCGB_OK;
 }
@@ -323,7 +377,7 @@ int hcgb_context_destroy(hcgb_context *ctx) {
     if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
     for (auto &g : ctx->ev_pending)
-        for (auto e : g) cudaEventDestroy(e);
+        for (auto &e : g) cudaEventDestroy(e.second);
     for (auto e : ctx->ev_free) cudaEventDestroy(e);
     for (auto st : ctx->group_streams) cudaStreamDestroy(st);
     for (auto e : ctx->group_events) cudaEventDestroy(e);
@@ -483,7 +537,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
                 if (u.a.kind == HCGB_DENSE && u.b.kind == HCGB_DENSE && compressed(u.c.kind))
                     return fail(ctx, HCGB_UNSUPPORTED, "hcgb_tlr_gemm: DDC updates are not batched");
                 all[w] = u;
-                dv[w] = DevUpdate{to_dev(u.a), to_dev(u.b), to_dev(u.c), kx * n + idx};
+                dv[w] = DevUpdate{to_dev(u.a), to_dev(u.b), to_dev(u.c), kx * n + idx, i > j ? i - j : j - i};
             }
     }
     BatchShape sh = shape_of(all.data(), (int) all.size());
@@ -524,6 +578,10 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         wg.base = ws.base + ws.slot_doubles * (size_t) first[g];
         wg.meta = ws.meta + (size_t) META_INTS * first[g];
         wg.order = ws.order + first[g];
+        if (ws.feat) {
+            wg.feat = ws.feat + (size_t) MLP_IN * first[g];
+            wg.pred = ws.pred + first[g];
+        }
     }
     // Waves are issued round-robin over the groups, so every group starts at once instead of
     // waiting for the host to enqueue the earlier groups' whole chains.
@@ -766,7 +824,7 @@ extern "C" int hcgb_profile_reset(hcgb_context *ctx) {
     if (!ctx) return HCGB_BAD_ARG;
     HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (auto &g : ctx->ev_pending)
-        for (auto e : g) ctx->ev_free.push_back(e);
+        for (auto &e : g) ctx->ev_free.push_back(e.second);
     ctx->ev_pending.clear();
     for (int i = 0; i < HCGB_NUM_STAGES; i++) {
         ctx->stage_ms[i] = 0.0;
@@ -780,12 +838,12 @@ extern "C" int hcgb_profile_read(hcgb_context *ctx, double *ms_per_stage, long l
     if (!ctx || nstages < 0) return HCGB_BAD_ARG;
     HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (auto &g : ctx->ev_pending) {
-        for (int i = 0; i < HCGB_NUM_STAGES; i++) {
+        for (size_t i = 0; i + 1 < g.size(); i++) {
             float ms = 0.f;
-            HCGB_CUDA(ctx, cudaEventElapsedTime(&ms, g[i], g[i + 1]));
-            ctx->stage_ms[i] += ms;
+            HCGB_CUDA(ctx, cudaEventElapsedTime(&ms, g[i].second, g[i + 1].second));
+            if (g[i].first >= 0 && g[i].first < HCGB_NUM_STAGES) ctx->stage_ms[g[i].first] += ms;
         }
-        for (auto e : g) ctx->ev_free.push_back(e);
+        for (auto &e : g) ctx->ev_free.push_back(e.second);
     }
     ctx->ev_pending.clear();
     for (int i = 0; i < nstages && i < HCGB_NUM_STAGES; i++) {
@@ -1032,4 +1090,146 @@ extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *gr
         }
     }
     return done(HCGB_OK);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Rank predictor of the learned form (no counterpart in the reference).
+// ---------------------------------------------------------------------------------------------
+extern "C" int hcgb_rank_model_create(hcgb_context *ctx, unsigned long long seed, hcgb_rank_model **out) {
+    if (!ctx || !out) return HCGB_BAD_ARG;
+    *out = nullptr;
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    auto *m = new hcgb_rank_model();
+    m->m.device = ctx->device;
+    const int rc = m->m.init(seed);
+    if (rc) {
+        m->m.release();
+        delete m;
+        return fail(ctx, rc, "hcgb_rank_model_create: device allocation failed");
+    }
+    *out = m;
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_rank_model_destroy(hcgb_rank_model *m) {
+    if (!m) return HCGB_BAD_ARG;
+    cudaSetDevice(m->m.device);
+    cudaDeviceSynchronize();
+    m->m.release();
+    delete m;
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_rank_model_params(hcgb_rank_model *m, float *host_out, const float *host_in) {
+    if (!m) return HCGB_BAD_ARG;
+    if (cudaSetDevice(m->m.device) != cudaSuccess) return HCGB_CUDA_ERROR;
+    int rc = HCGB_OK;
+    if (host_in) rc = m->m.set_params(host_in);
+    if (!rc && host_out) rc = m->m.get_params(host_out);
+    return rc;
+}
+
+extern "C" int hcgb_rank_model_predict(hcgb_context *ctx, hcgb_rank_model *m, int n, const float *features_dev,
+                                       float *out_dev) {
+    if (!ctx || !m || n < 0 || (n > 0 && (!features_dev || !out_dev)))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_rank_model_predict: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    launch_mlp_forward(m->m, features_dev, n, out_dev, ctx->stream);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_rank_model_gradient(hcgb_context *ctx, hcgb_rank_model *m, int n, const float *features_dev,
+                                        const float *targets_dev, float *grad_host, double *loss) {
+    if (!ctx || !m || n <= 0 || !features_dev || !targets_dev || !grad_host)
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_rank_model_gradient: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    double *dloss = nullptr;
+    HCGB_CUDA(ctx, cudaMalloc(&dloss, sizeof(double)));
+    cudaMemsetAsync(dloss, 0, sizeof(double), ctx->stream);
+    cudaMemsetAsync(m->m.grad, 0, sizeof(float) * MLP_PARAMS, ctx->stream);
+    launch_mlp_grad(m->m, features_dev, targets_dev, nullptr, 0, n, 1.0f / (float) n, dloss, ctx->stream);
+    double h = 0.0;
+    cudaError_t e = cudaMemcpyAsync(grad_host, m->m.grad, sizeof(float) * MLP_PARAMS, cudaMemcpyDeviceToHost,
+                                    ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, dloss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->m.grad, 0, sizeof(float) * MLP_PARAMS, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dloss);
+    if (e != cudaSuccess) return fail(ctx, HCGB_CUDA_ERROR, std::string("hcgb_rank_model_gradient: ") + cudaGetErrorString(e));
+    if (loss) *loss = h / n;
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_rank_model_train(hcgb_context *ctx, hcgb_rank_model *m, int n, const float *features_dev,
+                                     const hcgb_update_info *records_dev, int epochs, int batch, float lr,
+                                     unsigned long long seed, double *final_loss, int *samples) {
+    if (!ctx || !m || n <= 0 || !features_dev || !records_dev || epochs < 0 || batch <= 0 || !(lr > 0.f))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_rank_model_train: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    float *T = nullptr;
+    int *keep = nullptr, *idx = nullptr;
+    double *dloss = nullptr;
+    auto done = [&](int rc) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(T);
+        cudaFree(keep);
+        cudaFree(idx);
+        cudaFree(dloss);
+        return rc;
+    };
+    if (cudaMalloc(&T, sizeof(float) * n) != cudaSuccess || cudaMalloc(&keep, sizeof(int) * n) != cudaSuccess ||
+        cudaMalloc(&idx, sizeof(int) * n) != cudaSuccess || cudaMalloc(&dloss, sizeof(double)) != cudaSuccess)
+        return done(fail(ctx, HCGB_CUDA_ERROR, "hcgb_rank_model_train: cudaMalloc failed"));
+    launch_targets_from_records(records_dev, n, T, keep, ctx->stream);
+    std::vector<int> hk((size_t) n);
+    if (cudaMemcpyAsync(hk.data(), keep, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        return done(fail(ctx, HCGB_CUDA_ERROR, "hcgb_rank_model_train: record read failed"));
+    std::vector<int> rows;
+    for (int i = 0; i < n; i++)
+        if (hk[i]) rows.push_back(i);
+    const int cnt = (int) rows.size();
+    if (samples) *samples = cnt;
+    if (cnt == 0) return done(fail(ctx, HCGB_BAD_ARG, "hcgb_rank_model_train: no recompressed update in the records"));
+    unsigned long long st = seed * 2862933555777941757ULL + 3037000493ULL;
+    double last = 0.0;
+    for (int ep = 0; ep < epochs; ep++) {
+        // Fisher-Yates shuffle of the rows (64-bit LCG), then minibatches in that order.
+        for (int i = cnt - 1; i > 0; i--) {
+            st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+            const int j = (int) ((st >> 33) % (unsigned long long) (i + 1));
+            std::swap(rows[i], rows[j]);
+        }
+        if (cudaMemcpyAsync(idx, rows.data(), sizeof(int) * cnt, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+            return done(fail(ctx, HCGB_CUDA_ERROR, "hcgb_rank_model_train: upload failed"));
+        cudaMemsetAsync(dloss, 0, sizeof(double), ctx->stream);
+        for (int off = 0; off < cnt; off += batch) {
+            const int bs = cnt - off < batch ? cnt - off : batch;
+            launch_mlp_grad(m->m, features_dev, T, idx, off, bs, 1.0f / (float) bs, dloss, ctx->stream);
+            launch_adam(m->m, lr, ctx->stream);
+        }
+        double h = 0.0;
+        if (cudaMemcpyAsync(&h, dloss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+            cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+            return done(fail(ctx, HCGB_CUDA_ERROR, "hcgb_rank_model_train: training step failed"));
+        last = h / cnt;
+    }
+    if (final_loss) *final_loss = last;
+    return done(HCGB_OK);
+}
+
+extern "C" int hcgb_set_rank_model(hcgb_context *ctx, hcgb_rank_model *m, int policy) {
+    if (!ctx || policy < 0 || policy > 1) return HCGB_BAD_ARG;
+    if (m && m->m.device != ctx->device) return fail(ctx, HCGB_BAD_ARG, "hcgb_set_rank_model: model on another device");
+    ctx->model = m;
+    ctx->sk_policy = policy;
+    ctx->learned = policy == 1 || m != nullptr;
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_set_feature_sink(hcgb_context *ctx, float *features_dev) {
+    if (!ctx) return HCGB_BAD_ARG;
+    ctx->feature_sink = features_dev;
+    return HCGB_OK;
 }

@@ -19,6 +19,7 @@
 //   finalize  : transpose V into the tile buffer, publish the new rank
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
@@ -106,7 +107,8 @@ struct DevTile {
 
 struct DevUpdate {
     DevTile a, b, c;
-    int uid;  // index of this update's record in the caller's hcgb_update_info array
+    int uid;   // index of this update's record in the caller's hcgb_update_info array
+    int dist;  // |i - j| of the C tile in a tile-matrix multiply (a feature of the rank predictor)
 };
 
 // Per-update bookkeeping written by the plan kernel and read by the later stages.
@@ -128,7 +130,12 @@ enum MetaField {
     META_KC_JACOBI,
     META_KC_FACTORS,
     META_WY,         // bit 0 / bit 1: the U / V factor's Q is applied in WY form (else apply_q_kernel)
-    META_INTS = 17
+    META_LSK,        // learned form: sketch width l (0: this update takes the plain recompression)
+    META_SK_CK,      // learned form: CKIND, K and STATUS saved while the sketch / fallback passes run
+    META_SK_K,
+    META_SK_ST,
+    META_SK_ACC,     // learned form: 1 when the sketch result passed the residual test
+    META_INTS = 22
 };
 
 // Device workspace: n slots of `slot_doubles` doubles plus an int meta block.
@@ -143,6 +150,9 @@ struct Workspace {
     size_t off_ustack, off_vstack, off_tmp1, off_tmp2, off_tauu, off_tauv, off_tu, off_tv;
     size_t off_m, off_mcopy, off_xv, off_sigma, off_mixed;
     size_t off_w;  // WY application: W_U, W_V (kmax x kmax each), present when built with wy
+    size_t off_sk1, off_sk2, off_skaux;  // learned form: sketch stacks (ld x kmax each), residual estimate
+    float *feat;   // learned form / feature sink: MLP_IN features per update (n x MLP_IN), or null
+    float *pred;   // learned form: predicted log2(1 + rank) per update (n), or null
 
     __host__ __device__ double *slot(int s) const { return base + slot_doubles * (size_t) s; }
     // Update processed by CTA `b` of the QR / core / Q-application launches: largest first, so the
@@ -152,7 +162,7 @@ struct Workspace {
 
 // Layout of one workspace slot for stacks of up to `ld` rows and `kmax` columns; factor ranks
 // up to `rmax`.  ddc_scratch reserves an ld x ld product for the DDC combination.
-Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch, bool wy = false);
+Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch, bool wy = false, bool learned = false);
 
 struct Params {
     double accuracy;
@@ -215,6 +225,43 @@ void launch_pack(const DevTile *tiles, int n, long long *offsets, double *packed
 
 // Every kernel launch of the library is counted (hcgb_kernel_launches reads the total).
 void note_launch();
+
+// ---- learned form (learned.cu): features, sketch recompression and its fallback ----
+// Per-update features (ws.feat, and sink[uid * MLP_IN ..] when sink != null); needs ws.feat.
+void launch_features(const DevUpdate *ups, int n, Workspace ws, double accuracy, float *sink, cudaStream_t st);
+// Sketch width per update from ws.pred (policy 0) or from the input ranks (policy 1), the jobs
+// Z = V_s^T Omega (jobs[0 .. n)) and Y = U_s Z (jobs[n .. 2n)), and Omega itself.
+void launch_sketch_plan(const DevUpdate *ups, int n, Workspace ws, Params p, int policy, unsigned long long seed,
+                        GemmJob *jobs, cudaStream_t st);
+// Householder QR of Y's first l columns, residual probe, explicit Q_Y; then the jobs W = U_s^T Q_Y
+// (jobs[0 .. n)) and V' = V_s W (jobs[n .. 2n)).
+void launch_sketch_qr(int n, Workspace ws, cudaStream_t st);
+void launch_sketch_plan2(int n, Workspace ws, Params p, GemmJob *jobs, cudaStream_t st);
+// stage 0: before the sketch pass; 1: residual test, before the fallback pass; 2: restore.
+void launch_sketch_pass(int n, Workspace ws, Params p, int stage, cudaStream_t st);
+void launch_learned_records(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st);
+
+// ---- rank predictor of the learned form (mlp.cu) ----
+constexpr int MLP_IN = 12, MLP_HIDDEN = 64;
+constexpr int MLP_PARAMS = MLP_HIDDEN * MLP_IN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1;
+struct RankModel {
+    float *master = nullptr;  // FP32 master parameters, then grad, Adam m1, m2 (4 x MLP_PARAMS floats)
+    float *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
+    __nv_bfloat16 *w = nullptr;  // BF16 weights read by the forward / backward kernels
+    int adam_t = 0;
+    int device = 0;
+    int init(unsigned long long seed);
+    int set_params(const float *host);
+    int get_params(float *host) const;
+    void release();
+};
+void launch_mlp_forward(const RankModel &m, const float *X, int n, float *Y, cudaStream_t st);
+// grad += dL/dparams of L = inv_total * sum over samples (y - t)^2, *loss += sum (y - t)^2, for the
+// samples idx[off .. off + n) (or rows off .. off + n when idx is null).
+void launch_mlp_grad(const RankModel &m, const float *X, const float *T, const int *idx, int off, int n,
+                     float inv_total, double *loss, cudaStream_t st);
+void launch_adam(RankModel &m, float lr, cudaStream_t st);
+void launch_targets_from_records(const hcgb_update_info *info, int n, float *T, int *keep, cudaStream_t st);
 
 size_t qr_smem_bytes(int ld, int kmax);
 size_t svd_smem_bytes(int kmax);

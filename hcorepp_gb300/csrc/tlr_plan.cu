@@ -381,6 +381,8 @@ __global__ void __launch_bounds__(256) finalize_kernel(const DevUpdate *ups, Wor
         r.side = meta[META_SIDE];
         r.core_cols = meta[META_CORE_COLS];
         for (int q = 0; q < 4; q++) r.core_kcycles[q] = meta[META_KC_PRODUCT + q];
+        r.sketch_cols = meta[META_LSK];
+        r.sketch_accepted = meta[META_SK_ACC];
         info[ups[s].uid] = r;
     }
     if (!ok) return;
@@ -611,7 +613,7 @@ void launch_ddc_finalize(const DevUpdate *ups, int n, Workspace ws, cudaStream_t
     { ddc_finalize_kernel<<<n, 256, 0, st>>>(ups, ws); note_launch(); }
 }
 
-Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch, bool wy) {
+Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch, bool wy, bool learned) {
     Workspace w{};
     w.ld = ld;
     w.kmax = kmax;
@@ -634,6 +636,14 @@ Workspace make_workspace_layout(int ld, int kmax, int rmax, bool ddc_scratch, bo
     w.off_mixed = off;  off += round(((size_t) kmax * (size_t) (kmax + ld) + 1) / 2);  // float X32 + J32
     w.off_w = wy ? off : 0;  // 0: absent (no region starts at 0 but the U stack)
     off += wy ? round(2 * (size_t) kmax * kmax) : 0;
+    w.off_sk1 = learned ? off : 0;
+    off += learned ? round((size_t) ld * kmax) : 0;
+    w.off_sk2 = learned ? off : 0;
+    off += learned ? round((size_t) ld * kmax) : 0;
+    w.off_skaux = learned ? off : 0;
+    off += learned ? round(8) : 0;
+    w.feat = nullptr;
+    w.pred = nullptr;
     w.slot_doubles = off;
     return w;
 }

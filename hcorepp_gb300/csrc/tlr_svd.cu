@@ -929,6 +929,7 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
         if (r > maxr) r = maxr;
         if (r > rk) r = rk;
         s_rank = r;
+        base[ws.off_sigma] = sig[0];  // the largest singular value (the learned form's residual test)
         meta[META_NEWRANK] = r;
         meta[META_SWEEPS] = sweeps;
         meta[META_CORE_COLS] = rk;

@@ -107,12 +107,15 @@ typedef struct {
     int core_cols;  /* rows of R the rank-revealing QR of the core kept (columns Jacobi rotated) */
     int core_kcycles[4]; /* core SVD phases in units of 1024 SM cycles: core product, pivoted QR,
                             Jacobi, new factors (diagnostics) */
+    int sketch_cols;     /* learned form: columns of the randomized sketch (0: plain recompression) */
+    int sketch_accepted; /* learned form: 1 if the sketch passed its residual test, 0 if the plain
+                            recompression ran as the fallback */
 } hcgb_update_info;
 
 /* Pipeline stages, for hcgb_profile_read. */
 typedef enum {
     HCGB_STAGE_PLAN = 0, HCGB_STAGE_STACK, HCGB_STAGE_GEMM, HCGB_STAGE_QR, HCGB_STAGE_CORE_SVD,
-    HCGB_STAGE_APPLY_Q, HCGB_STAGE_FINALIZE, HCGB_NUM_STAGES
+    HCGB_STAGE_APPLY_Q, HCGB_STAGE_FINALIZE, HCGB_STAGE_SKETCH, HCGB_NUM_STAGES
 } hcgb_stage;
 
 typedef struct hcgb_context hcgb_context;
@@ -258,6 +261,60 @@ long long hcgb_kernel_launches(void);
  * MMA (DMMA) rate and the FP64 FMA rate of the SIMT pipes, in TFLOP/s.  These are the roofline
  * denominators of the FP64 path. */
 int hcgb_fp64_peak(hcgb_context *ctx, double *dmma_tflops, double *dfma_tflops);
+
+/* ---- The learned form (no counterpart in the reference) ----
+ * A rank predictor sizes a randomized sketch of each update's product P = U_s V_s^T (the stacked
+ * bases of the plain recompression): l = predicted rank + 8 columns of seeded Gaussian test vectors,
+ * Y = P Omega, Q_Y from a Householder QR of Y, and the plain recompression (stack QR, core SVD,
+ * truncation by the reference's rule, Q application) run on the l-column stacks [Q_Y], [V_s U_s^T Q_Y].
+ * Four more Gaussian probe vectors w_p give the a-posteriori estimate
+ * e = 10 sqrt(2/pi) max_p ||(I - Q_Y Q_Y^T) P w_p|| of ||(I - Q_Y Q_Y^T) P||_2 (Halko, Martinsson and
+ * Tropp 2011, 4.3; wrong with probability below 1e-4).  The sketch result is kept when e is below the
+ * truncation threshold (accuracy * sigma_0, or accuracy) and the new rank is below l; otherwise the
+ * plain recompression runs on the original stacks (the fallback), in the same call.  Updates whose
+ * stacks are not wider than l + 4 columns, and fixed-rank truncations, take the plain recompression.
+ * Every batched entry point of the context (hcgb_gemm_batch, hcgb_tlr_gemm, hcgb_tile_cholesky) uses
+ * the form while it is set; the per-update records report sketch_cols and sketch_accepted.
+ *
+ * The predictor: an MLP with 12 inputs, two hidden layers of 64 (GELU) and one output, BF16 weights,
+ * FP32 accumulation; y = predicted log2(1 + rank).  Inputs per update (HCGB_RANK_FEATURES floats):
+ * ranks of A, B, C / rows of C (dense operands count as full rank); log10(sigma_1 / sigma_0) and
+ * log10(sigma_2 / sigma_0) of A, B and C, each / 8 (a compressed tile's singular values taken as the
+ * row norms of its V factor); log10(||A||_F ||B||_F / ||C||_F) / 8; |i - j| / 32 of the C tile;
+ * log10(accuracy) / 8.  Trained by the library's own kernels (forward, backward, Adam on an FP32
+ * master copy) with mean squared error on log2(1 + rank). */
+#define HCGB_RANK_FEATURES 12
+#define HCGB_RANK_MODEL_PARAMS 5057
+typedef struct hcgb_rank_model hcgb_rank_model;
+
+/* Device-resident predictor, Glorot-initialised from `seed`, on the context's device. */
+int hcgb_rank_model_create(hcgb_context *ctx, unsigned long long seed, hcgb_rank_model **out);
+int hcgb_rank_model_destroy(hcgb_rank_model *m);
+/* Parameters as HCGB_RANK_MODEL_PARAMS floats (W1 64x12 row-major, b1, W2 64x64 row-major, b2, w3,
+ * b3): host_in (if not NULL) replaces them (the BF16 weights are rounded from it), then host_out (if not
+ * NULL) receives the FP32 master copy.  Synchronous. */
+int hcgb_rank_model_params(hcgb_rank_model *m, float *host_out, const float *host_in);
+/* out_dev[i] = predicted log2(1 + rank) for the features of row i (device, n x HCGB_RANK_FEATURES). */
+int hcgb_rank_model_predict(hcgb_context *ctx, hcgb_rank_model *m, int n, const float *features_dev, float *out_dev);
+/* Gradient of (1/n) sum_i (y_i - t_i)^2 with respect to the parameters (host, HCGB_RANK_MODEL_PARAMS
+ * floats) and that loss.  Synchronous. */
+int hcgb_rank_model_gradient(hcgb_context *ctx, hcgb_rank_model *m, int n, const float *features_dev,
+                             const float *targets_dev, float *grad_host, double *loss);
+/* Trains on the (features, records) pairs of n updates -- features as recorded by
+ * hcgb_set_feature_sink, records the hcgb_update_info of the same updates -- with targets
+ * log2(1 + new_rank) of every recompressed update (k > 0, status OK or NOT_CONVERGED): `epochs`
+ * passes over a seeded shuffle, minibatches of `batch`, Adam with step `lr`.  *final_loss receives
+ * the last epoch's mean squared error, *samples the number of pairs used.  Synchronous. */
+int hcgb_rank_model_train(hcgb_context *ctx, hcgb_rank_model *m, int n, const float *features_dev,
+                          const hcgb_update_info *records_dev, int epochs, int batch, float lr,
+                          unsigned long long seed, double *final_loss, int *samples);
+/* Turns the learned form on for this context: policy 0 sizes the sketch by the predictor m; policy 1
+ * (m may be NULL) sizes it without a network, from the input ranks (max(rank C, the rank the product
+ * adds)).  m = NULL with policy 0 turns the form off. */
+int hcgb_set_rank_model(hcgb_context *ctx, hcgb_rank_model *m, int policy);
+/* While set, every batched call records each recompressed update's predictor features at
+ * features_dev[record index * HCGB_RANK_FEATURES] (the record index of info_dev); NULL stops it. */
+int hcgb_set_feature_sink(hcgb_context *ctx, float *features_dev);
 
 /* One tile update that allocates nothing (no counterpart in the reference; an addition of this
  * library).  For callers that may not allocate device memory themselves: task-runtime workers whose

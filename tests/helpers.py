@@ -29,3 +29,29 @@ def random_lowrank(m, n, r, rng, decay=0.5):
     q2, _ = np.linalg.qr(rng.standard_normal((n, r)))
     s = decay ** np.arange(r)
     return (q1 * s) @ q2.T
+
+
+def oracle_tile_grid(km, nt, acc, dense_diagonal):
+    """Oracle tiles of a kernel matrix: dense on the diagonal (if asked), else compressed at `acc`
+    relative by the reference's dense constructor rule."""
+    grid = [[None] * nt for _ in range(nt)]
+    for i in range(nt):
+        for j in range(nt):
+            d = km.tile(i, j)
+            grid[i][j] = O.DenseTile(d) if (dense_diagonal and i == j) else compressed_from_dense(d, acc)
+    return grid
+
+
+def load_tile_matrix(T, L, grid, nb, max_rank):
+    """A device TileMatrix holding the oracle tiles of `grid`."""
+    mt, nt = len(grid), len(grid[0])
+    kinds = [[L.DENSE if grid[i][j].kind == "dense" else L.COMPRESSED for j in range(nt)] for i in range(mt)]
+    tm = T.TileMatrix(mt, nt, nb, kinds, max_rank)
+    for i in range(mt):
+        for j in range(nt):
+            t = grid[i][j]
+            if t.kind == "dense":
+                tm.set_tile(i, j, dense=t.data)
+            else:
+                tm.set_tile(i, j, u=t.u, v=t.v)
+    return tm
