@@ -20,7 +20,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhcgb.so")
 
 CU_SOURCES = ["hcgb_abi.cu", "tlr_plan.cu", "tlr_qr.cu", "tlr_svd.cu", "probe.cu", "noalloc.cu", "chol.cu",
-              "oz_gemm.cu", "pack.cu", "tc_gemm.cu", "mlp.cu", "learned.cu"]
+              "oz_gemm.cu", "pack.cu", "tc_gemm.cu", "mlp.cu", "learned.cu", "backend.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

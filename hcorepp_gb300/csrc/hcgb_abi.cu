@@ -53,6 +53,9 @@ struct hcgb_context {
     int sk_policy = 0;                        // 0: sketch width from the predictor; 1: from the input ranks
     unsigned long long sk_seed = 0x5eedULL;   // seed of the Gaussian test matrices
     float *feature_sink = nullptr;            // device: per-update predictor features, indexed like info
+    // per-matrix operations (hcgb_d*)
+    void *be_scratch = nullptr;
+    size_t be_scratch_bytes = 0;
 };
 
 struct hcgb_rank_model {
@@ -374,6 +377,7 @@ int hcgb_context_destroy(hcgb_context *ctx) {
     if (ctx->desc) cudaFree(ctx->desc);
     if (ctx->pack_desc) cudaFree(ctx->pack_desc);
     if (ctx->tile_info) cudaFree(ctx->tile_info);
+    if (ctx->be_scratch) cudaFree(ctx->be_scratch);
     if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
     for (auto &g : ctx->ev_pending)
@@ -1231,5 +1235,196 @@ extern "C" int hcgb_set_rank_model(hcgb_context *ctx, hcgb_rank_model *m, int po
 extern "C" int hcgb_set_feature_sink(hcgb_context *ctx, float *features_dev) {
     if (!ctx) return HCGB_BAD_ARG;
     ctx->feature_sink = features_dev;
+    return HCGB_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Per-matrix operations behind the HCoreKernels<double> backend (hcorepp_gb300/backend).
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+bool bad_ld(int ld, int rows) { return ld < (rows > 1 ? rows : 1); }
+
+}  // namespace
+
+extern "C" int hcgb_dgemm(hcgb_context *ctx, int transa, int transb, int m, int n, int k, double alpha,
+                          const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (m < 0 || n < 0 || k < 0 || (transa != 0 && transa != 1) || (transb != 0 && transb != 1) ||
+        (m > 0 && n > 0 && (!C || bad_ld(ldc, m))) ||
+        (m > 0 && n > 0 && k > 0 && (!A || !B || bad_ld(lda, transa ? k : m) || bad_ld(ldb, transb ? n : k))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dgemm: bad arguments");
+    if (m == 0 || n == 0) return HCGB_OK;
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    GemmJob j{};
+    j.A = A;
+    j.B = B;
+    j.C = C;
+    j.M = m;
+    j.N = n;
+    j.K = k;
+    j.lda = lda > 0 ? lda : 1;
+    j.ldb = ldb > 0 ? ldb : 1;
+    j.ldc = ldc;
+    j.opA = transa;
+    j.opB = transb;
+    j.alpha = alpha;
+    j.beta = beta;
+    j.oz = (ctx->oz && oz_shape(m, n, k)) ? 1 : 0;
+    const size_t jb = (sizeof(GemmJob) + 255) / 256 * 256;
+    int rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, jb + sizeof(int) * 16);
+    if (rc) return rc;
+    if ((rc = ensure_stage(ctx, sizeof(GemmJob)))) return rc;
+    std::memcpy(ctx->stage, &j, sizeof(GemmJob));
+    auto *dj = static_cast<GemmJob *>(ctx->desc);
+    HCGB_CUDA(ctx, cudaMemcpyAsync(dj, ctx->stage, sizeof(GemmJob), cudaMemcpyHostToDevice, ctx->stream));
+    HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
+    launch_gemm_jobs(dj, 1, reinterpret_cast<int *>(static_cast<char *>(ctx->desc) + jb), ctx->stream);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dcopy2d(hcgb_context *ctx, int trans, int m, int n, double alpha, const double *A, int lda,
+                            double *B, int ldb) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (m < 0 || n < 0 || (m > 0 && n > 0 && (!A || !B || bad_ld(ldb, m) || bad_ld(lda, trans ? n : m))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dcopy2d: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    be_copy(ctx->stream, trans ? 1 : 0, m, n, alpha, A, lda, B, ldb);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dlacpy(hcgb_context *ctx, int part, int m, int n, const double *A, int lda, double *B, int ldb) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (part < 0 || part > 2 || m < 0 || n < 0 || (m > 0 && n > 0 && (!A || !B || bad_ld(lda, m) || bad_ld(ldb, m))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dlacpy: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    be_lacpy(ctx->stream, part, m, n, A, lda, B, ldb);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dlaset(hcgb_context *ctx, int part, int m, int n, double offdiag, double diag, double *A, int lda) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (part < 0 || part > 3 || m < 0 || n < 0 || (m > 0 && n > 0 && (!A || bad_ld(lda, m))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dlaset: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    be_laset(ctx->stream, part, m, n, offdiag, diag, A, lda);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dscale_rows(hcgb_context *ctx, int rows, int cols, const double *s, double *A, int lda) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (rows < 0 || cols < 0 || (rows > 0 && cols > 0 && (!s || !A || bad_ld(lda, rows))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dscale_rows: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    be_scale_rows(ctx->stream, rows, cols, s, A, lda);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dsymmetrize(hcgb_context *ctx, int uplo, int n, double *A, int lda) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if ((uplo != HCGB_LOWER && uplo != HCGB_UPPER) || n < 0 || (n > 0 && (!A || bad_ld(lda, n))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dsymmetrize: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    be_symmetrize(ctx->stream, uplo == HCGB_UPPER ? 1 : 2, n, A, lda);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dgeqrf(hcgb_context *ctx, int m, int n, double *A, int lda, double *tau) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (m < 0 || n < 0 || (m > 0 && n > 0 && (!A || !tau || bad_ld(lda, m))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dgeqrf: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    be_geqr2(ctx->stream, m, n, A, lda, tau);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dorgqr(hcgb_context *ctx, int m, int n, int k, double *A, int lda, const double *tau) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (m < 0 || n < 0 || n > m || k < 0 || k > n || (m > 0 && n > 0 && (!A || bad_ld(lda, m) || (k > 0 && !tau))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dorgqr: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    be_org2r(ctx->stream, m, n, k, A, lda, tau);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dormqr(hcgb_context *ctx, int side, int trans, int m, int n, int k, const double *A, int lda,
+                           const double *tau, double *C, int ldc) {
+    if (!ctx) return HCGB_BAD_ARG;
+    const int nq = side == HCGB_LEFT ? m : n;
+    if ((side != HCGB_LEFT && side != HCGB_RIGHT) || (trans != HCGB_NOTRANS && trans != HCGB_TRANS) || m < 0 ||
+        n < 0 || k < 0 || k > nq || (m > 0 && n > 0 && k > 0 && (!A || !tau || !C || bad_ld(lda, nq) || bad_ld(ldc, m))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dormqr: bad arguments");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    be_orm2r(ctx->stream, side == HCGB_LEFT, trans == HCGB_TRANS, m, n, k, A, lda, tau, C, ldc);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dtrmm(hcgb_context *ctx, int side, int uplo, int trans, int diag, int m, int n, double alpha,
+                          const double *A, int lda, double *B, int ldb) {
+    if (!ctx) return HCGB_BAD_ARG;
+    const int na = side == HCGB_LEFT ? m : n;
+    if ((side != HCGB_LEFT && side != HCGB_RIGHT) || (uplo != HCGB_LOWER && uplo != HCGB_UPPER) ||
+        (trans != HCGB_NOTRANS && trans != HCGB_TRANS) || (diag != HCGB_NONUNIT && diag != HCGB_UNIT) || m < 0 ||
+        n < 0 || (m > 0 && n > 0 && (!A || !B || bad_ld(lda, na) || bad_ld(ldb, m))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dtrmm: bad arguments");
+    if (m == 0 || n == 0) return HCGB_OK;
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    int rc = ensure_device(ctx, &ctx->be_scratch, &ctx->be_scratch_bytes, sizeof(double) * (size_t) m * n);
+    if (rc) return rc;
+    double *T = static_cast<double *>(ctx->be_scratch);
+    be_lacpy(ctx->stream, 0, m, n, B, ldb, T, m);
+    be_trmm(ctx->stream, side == HCGB_LEFT, uplo == HCGB_UPPER, trans == HCGB_TRANS, diag == HCGB_UNIT, m, n, alpha, A,
+            lda, T, B, ldb);
+    HCGB_CUDA(ctx, cudaGetLastError());
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_dgesvd(hcgb_context *ctx, int jobu, int jobvt, int m, int n, double *A, int lda, double *S,
+                           double *U, int ldu, double *VT, int ldvt, int *info) {
+    if (!ctx) return HCGB_BAD_ARG;
+    const int kk = m < n ? m : n;
+    const bool wu = jobu != HCGB_SVD_NONE, wv = jobvt != HCGB_SVD_NONE;
+    if (jobu < 0 || jobu > 2 || jobvt < 0 || jobvt > 2 || m < 0 || n < 0 || (m > 0 && n > 0 && (!A || !S || bad_ld(lda, m))) ||
+        (wu && m > 0 && (!U || bad_ld(ldu, m))) || (wv && n > 0 && (!VT || bad_ld(ldvt, jobvt == HCGB_SVD_ALL ? n : kk))))
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_dgesvd: bad arguments");
+    if ((jobu == HCGB_SVD_ALL && m > n) || (jobvt == HCGB_SVD_ALL && n > m))
+        return fail(ctx, HCGB_UNSUPPORTED, "hcgb_dgesvd: full U of a tall or full V^T of a wide matrix");
+    if (info) *info = 0;
+    if (m == 0 || n == 0) return HCGB_OK;
+    if (kk > 1024) return fail(ctx, HCGB_UNSUPPORTED, "hcgb_dgesvd: min(m, n) > 1024");
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    // Jacobi on X = A (m >= n) or X = A^T (m < n): rows >= cols = kk.
+    const bool tr = m < n;
+    const int rows = tr ? n : m;
+    const size_t need = sizeof(double) * ((size_t) kk * kk + (tr ? (size_t) rows * kk : 0)) + 256;
+    int rc = ensure_device(ctx, &ctx->be_scratch, &ctx->be_scratch_bytes, need + sizeof(int) * 4);
+    if (rc) return rc;
+    double *V = static_cast<double *>(ctx->be_scratch);
+    double *X = A;
+    int ldx = lda;
+    if (tr) {
+        X = V + (size_t) kk * kk;
+        ldx = rows;
+        be_copy(ctx->stream, 1, rows, kk, 1.0, A, lda, X, ldx);
+    }
+    int *dsw = reinterpret_cast<int *>(static_cast<char *>(ctx->be_scratch) + need);
+    be_jacobi_svd(ctx->stream, rows, kk, X, ldx, V, kk, 2.2204460492503131e-16 * std::sqrt((double) rows), dsw);
+    be_svd_finish(ctx->stream, rows, kk, X, ldx, V, kk, S, U, ldu, VT, ldvt, kk, wu ? 1 : 0, wv ? 1 : 0, tr ? 1 : 0);
+    int sw = 0;
+    HCGB_CUDA(ctx, cudaMemcpyAsync(&sw, dsw, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (sw < 0) {
+        if (info) *info = 1;
+        return fail(ctx, HCGB_NOT_CONVERGED, "hcgb_dgesvd: Jacobi sweep limit reached");
+    }
     return HCGB_OK;
 }

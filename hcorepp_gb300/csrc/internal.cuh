@@ -190,6 +190,7 @@ void launch_oz_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int s
 void launch_tc_gemm_jobs(const GemmJob *jobs, int njobs, const int *sched, int sms, cudaStream_t st);
 // Bounded mbarrier waits of the tcgen05 kernels that gave up (0 unless something else failed).
 unsigned int tc_wait_timeouts();
+unsigned int oz_wait_timeouts();
 constexpr int MAX_JOBS_PER_LAUNCH = 4096;
 constexpr int SCHED_INTS_PER_UPDATE = 16;  // >= (3 * 4n + 3) / n: one WY launch schedules 4n jobs, 3 tile lists
 // Q application in full WY form (Q = I - V T V^T, T^-1 = striu(V^T V) + diag(1/tau)): jobs for
@@ -240,6 +241,22 @@ void launch_sketch_plan2(int n, Workspace ws, Params p, GemmJob *jobs, cudaStrea
 // stage 0: before the sketch pass; 1: residual test, before the fallback pass; 2: restore.
 void launch_sketch_pass(int n, Workspace ws, Params p, int stage, cudaStream_t st);
 void launch_learned_records(const DevUpdate *ups, int n, Workspace ws, hcgb_update_info *info, cudaStream_t st);
+
+// ---- per-matrix operations of the HCoreKernels backend (backend.cu); asynchronous on st ----
+void be_copy(cudaStream_t st, int trans, int m, int n, double alpha, const double *A, int lda, double *B, int ldb);
+void be_lacpy(cudaStream_t st, int uplo, int m, int n, const double *A, int lda, double *B, int ldb);
+void be_laset(cudaStream_t st, int uplo, int m, int n, double offdiag, double diag, double *A, int lda);
+void be_scale_rows(cudaStream_t st, int rows, int cols, const double *s, double *A, int lda);
+void be_symmetrize(cudaStream_t st, int uplo, int n, double *A, int lda);
+void be_geqr2(cudaStream_t st, int m, int n, double *A, int lda, double *tau);
+void be_org2r(cudaStream_t st, int m, int n, int k, double *A, int lda, const double *tau);
+void be_orm2r(cudaStream_t st, int left, int trans, int m, int n, int k, const double *A, int lda, const double *tau,
+              double *C, int ldc);
+void be_trmm(cudaStream_t st, int left, int upper, int trans, int unit, int m, int n, double alpha, const double *A,
+             int lda, const double *T, double *B, int ldb);
+void be_jacobi_svd(cudaStream_t st, int rows, int cols, double *X, int ldx, double *V, int ldv, double tol, int *sweeps);
+void be_svd_finish(cudaStream_t st, int rows, int cols, const double *X, int ldx, const double *V, int ldv, double *S,
+                   double *U, int ldu, double *VT, int ldvt, int kk, int want_u, int want_vt, int transposed);
 
 // ---- rank predictor of the learned form (mlp.cu) ----
 constexpr int MLP_IN = 12, MLP_HIDDEN = 64;

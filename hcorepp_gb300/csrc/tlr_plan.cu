@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(128) gemm_jobs_kernel(const GemmJob *jobs, int
 
 // Tile counts of every job for the three GEMM kernels and their exclusive prefix sums:
 // sched[0 .. njobs] (FP64 DMMA, 64 x 64 tiles), sched[njobs + 1 .. 2 njobs + 1] (FP64-accurate
-// tensor-core path, 64 x 32 tiles) and sched[2 njobs + 2 .. 3 njobs + 2] (TF32 / BF16 on tcgen05,
+// tensor-core path, 128 x 64 tiles) and sched[2 njobs + 2 .. 3 njobs + 2] (TF32 / BF16 on tcgen05,
 // 128 x 64 tiles).  One CTA; njobs up to 4 * 1024.
 __global__ void __launch_bounds__(1024) schedule_kernel(const GemmJob *jobs, int njobs, int *sched) {
     constexpr int NL = 3;
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(1024) schedule_kernel(const GemmJob *jobs, int
             const GemmJob &jb = jobs[j];
             if (jb.M > 0 && jb.N > 0 && jb.K >= 0) {
                 if (jb.prec) cnt[2][q] = ((jb.M + 127) / 128) * ((jb.N + 63) / 64);
-                else if (jb.oz) cnt[1][q] = ((jb.M + 63) / 64) * ((jb.N + 31) / 32);
+                else if (jb.oz) cnt[1][q] = ((jb.M + 127) / 128) * ((jb.N + 63) / 64);
                 else cnt[0][q] = ((jb.M + GT - 1) / GT) * ((jb.N + GT - 1) / GT);
             }
         }

@@ -316,6 +316,43 @@ int hcgb_set_rank_model(hcgb_context *ctx, hcgb_rank_model *m, int policy);
  * features_dev[record index * HCGB_RANK_FEATURES] (the record index of info_dev); NULL stops it. */
 int hcgb_set_feature_sink(hcgb_context *ctx, float *features_dev);
 
+/* ---- Per-matrix operations (the HCoreKernels<double> backend, hcorepp_gb300/backend) ----
+ * The operations HCore++'s CompressedTile<T>::Gemm and its tests call one matrix at a time through
+ * HCoreKernels<T> (include/hcorepp/kernels/kernels.hpp:24-137), for a build of the reference on this
+ * library.  Column-major device matrices; asynchronous on the context stream unless stated. */
+typedef enum { HCGB_PART_GENERAL = 0, HCGB_PART_UPPER = 1, HCGB_PART_LOWER = 2, HCGB_PART_DIAGONAL = 3 } hcgb_part;
+typedef enum { HCGB_SVD_NONE = 0, HCGB_SVD_SOME = 1, HCGB_SVD_ALL = 2 } hcgb_svd_job;
+/* C = alpha op(A) op(B) + beta C (trans 0 / 1); HCoreKernels::Gemm (src/kernels/cuda/kernels.cpp:18-24). */
+int hcgb_dgemm(hcgb_context *ctx, int transa, int transb, int m, int n, int k, double alpha, const double *A, int lda,
+               const double *B, int ldb, double beta, double *C, int ldc);
+/* B (m x n) = alpha op(A): the copies and transpositions of MultiplyByAlpha, ProcessVpointer,
+ * CalculateUVptr and transpose (src/kernels/omp/kernels.cpp:22-79, :106-114). */
+int hcgb_dcopy2d(hcgb_context *ctx, int trans, int m, int n, double alpha, const double *A, int lda, double *B,
+                 int ldb);
+/* LAPACK dlacpy / dlaset (part: general, upper, lower; dlaset also HCGB_PART_DIAGONAL = only the
+ * diagonal, FillIdentityMatrix); HCoreKernels::LaCpy / Laset (omp/kernels.cpp:152-177). */
+int hcgb_dlacpy(hcgb_context *ctx, int part, int m, int n, const double *A, int lda, double *B, int ldb);
+int hcgb_dlaset(hcgb_context *ctx, int part, int m, int n, double offdiag, double diag, double *A, int lda);
+/* Row i < rows of A scaled by s[i] (device): CalculateVTnew (omp/kernels.cpp:116-130). */
+int hcgb_dscale_rows(hcgb_context *ctx, int rows, int cols, const double *s, double *A, int lda);
+/* The uplo triangle of A copied onto the other one: HCoreKernels::Symmetrize. */
+int hcgb_dsymmetrize(hcgb_context *ctx, int uplo, int n, double *A, int lda);
+/* Householder QR in LAPACK's compact form (dgeqrf semantics), its Q (dorgqr) and applying it (dormqr,
+ * side HCGB_LEFT / HCGB_RIGHT, trans HCGB_NOTRANS / HCGB_TRANS): HCoreKernels::Geqrf, ungqr, Unmqr. */
+int hcgb_dgeqrf(hcgb_context *ctx, int m, int n, double *A, int lda, double *tau);
+int hcgb_dorgqr(hcgb_context *ctx, int m, int n, int k, double *A, int lda, const double *tau);
+int hcgb_dormqr(hcgb_context *ctx, int side, int trans, int m, int n, int k, const double *A, int lda,
+                const double *tau, double *C, int ldc);
+/* B = alpha op(A) B (left) or alpha B op(A) (right), A triangular (BLAS dtrmm): HCoreKernels::Trmm. */
+int hcgb_dtrmm(hcgb_context *ctx, int side, int uplo, int trans, int diag, int m, int n, double alpha,
+               const double *A, int lda, double *B, int ldb);
+/* SVD of A (m x n, destroyed) by one-sided Jacobi in FP64: S (min(m, n), descending), U (m x min,
+ * jobu SOME; ALL only when m <= n), VT (min x n, jobvt SOME; ALL only when n <= m); min(m, n) <=
+ * 1024.  HCoreKernels::SVD (gesvd / gesdd, omp/kernels.cpp:182-192).  Synchronous; *info = 1 and
+ * HCGB_NOT_CONVERGED if the sweep limit was reached. */
+int hcgb_dgesvd(hcgb_context *ctx, int jobu, int jobvt, int m, int n, double *A, int lda, double *S, double *U,
+                int ldu, double *VT, int ldvt, int *info);
+
 /* One tile update that allocates nothing (no counterpart in the reference; an addition of this
  * library).  For callers that may not allocate device memory themselves: task-runtime workers whose
  * runtime owns the device memory and places the tile buffers, and real-time or embedded callers
