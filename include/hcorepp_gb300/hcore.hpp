@@ -82,19 +82,65 @@ private:
 }  // namespace kernels
 
 namespace dataunits {
-// The library sizes and owns its scratch per context; the unit keeps the reference's interface.
+// A device pool with the reference's bump-allocation semantics (pool/MemoryHandler.hpp:22-157,
+// src/data-units/memory-handlers/pool/MemoryHandler.cpp:20-50): Initialize allocates and zeroes it,
+// RequestAllocation hands out consecutive slices and throws when the pool is exhausted or not
+// initialised, Reset rewinds (zeroing the pool on the context stream), Free releases it.  HCore<T>'s
+// operations here take their scratch from the library's per-context workspace instead, so a unit
+// serves callers that carve their own temporaries (the reference's examples and tests do).
 template <typename T>
 class MemoryUnit {
 public:
-    explicit MemoryUnit(const kernels::RunContext &ctx) : mCtx(&ctx) {}
-    MemoryUnit() = default;
-    bool IsInitialized() const { return true; }
-    void Initialize(size_t) {}
-    void Reset() {}
-    void FreeAllocations() {}
+    explicit MemoryUnit(const kernels::RunContext &ctx, size_t aAllocationSize = 0) : mCtx(&ctx) {
+        if (aAllocationSize > 0) Initialize(aAllocationSize);
+    }
+    MemoryUnit(const MemoryUnit &) = delete;
+    MemoryUnit &operator=(const MemoryUnit &) = delete;
+    ~MemoryUnit() { Free(); }
+
+    T *RequestAllocation(size_t aSize) {
+        if (mAvailable < aSize || mpData == nullptr)
+            throw std::runtime_error("Requested Allocation Greater than MemoryUnit Size or the pool isn't initialized");
+        T *ret = mpData + mNext;
+        mNext += aSize;
+        mAvailable -= aSize;
+        return ret;
+    }
+    T *GetData() const { return mpData; }
+    size_t GetPoolSize() const { return mSize; }
+    size_t GetPoolAvailableSize() const { return mAvailable; }
+    bool IsInitialized() const { return mpData != nullptr; }
+    void Initialize(size_t aSize) {
+        if (IsInitialized()) throw std::runtime_error("MemoryUnit Is Already Allocated");
+        if (aSize == 0) return;
+        detail::cuda(cudaMalloc(reinterpret_cast<void **>(&mpData), sizeof(T) * aSize), "MemoryUnit::Initialize");
+        mSize = mAvailable = aSize;
+        mNext = 0;
+        BufferMemSet(0, aSize);
+    }
+    void BufferMemSet(char aValue, size_t aSize, size_t aOffset = 0) {
+        if (mpData)
+            detail::cuda(cudaMemsetAsync(mpData + aOffset, aValue, sizeof(T) * aSize, mCtx->GetStream()),
+                         "MemoryUnit::BufferMemSet");
+    }
+    void Free() {
+        if (!mpData) return;
+        cudaStreamSynchronize(mCtx->GetStream());
+        cudaFree(mpData);
+        mpData = nullptr;
+        mSize = mAvailable = mNext = 0;
+    }
+    void FreeAllocations() { Free(); }
+    void Reset() {
+        mAvailable = mSize;
+        mNext = 0;
+        if (mpData) BufferMemSet(0, mSize);
+    }
 
 private:
     const kernels::RunContext *mCtx = nullptr;
+    T *mpData = nullptr;
+    size_t mSize = 0, mAvailable = 0, mNext = 0;
 };
 }  // namespace dataunits
 

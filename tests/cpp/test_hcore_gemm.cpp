@@ -233,6 +233,48 @@ static int tile_packer(kernels::RunContext &ctx, dataunits::MemoryUnit<double> &
     return failures;
 }
 
+// MemoryUnit's pool semantics (pool/MemoryHandler.hpp:22-157): consecutive slices, exhaustion and
+// use before Initialize throw, Reset rewinds and zeroes, Free releases.
+static int memory_unit(kernels::RunContext &ctx) {
+    int fails = 0;
+    dataunits::MemoryUnit<double> unit(ctx);
+    bool threw = false;
+    try {
+        (void) unit.RequestAllocation(1);
+    } catch (const std::runtime_error &) {
+        threw = true;
+    }
+    fails += !threw;
+    unit.Initialize(1000);
+    double *a = unit.RequestAllocation(300), *b = unit.RequestAllocation(700);
+    fails += (b != a + 300) || unit.GetPoolAvailableSize() != 0 || unit.GetPoolSize() != 1000;
+    threw = false;
+    try {
+        (void) unit.RequestAllocation(1);
+    } catch (const std::runtime_error &) {
+        threw = true;
+    }
+    fails += !threw;
+    threw = false;
+    try {
+        unit.Initialize(10);
+    } catch (const std::runtime_error &) {
+        threw = true;
+    }
+    fails += !threw;
+    std::vector<double> ones(1000, 1.0), back(1000, -1.0);
+    cudaMemcpy(a, ones.data(), sizeof(double) * 1000, cudaMemcpyHostToDevice);
+    unit.Reset();
+    cudaMemcpyAsync(back.data(), unit.GetData(), sizeof(double) * 1000, cudaMemcpyDeviceToHost, ctx.GetStream());
+    cudaStreamSynchronize(ctx.GetStream());
+    for (double v : back) fails += v != 0.0;
+    fails += unit.GetPoolAvailableSize() != 1000 || unit.RequestAllocation(10) != a;
+    unit.Free();
+    fails += unit.IsInitialized();
+    std::printf("MemoryUnit pool: %s\n", fails ? "Fail" : "Pass");
+    return fails ? 1 : 0;
+}
+
 int main() {
     kernels::RunContext ctx(0);
     dataunits::MemoryUnit<double> mem(ctx);
@@ -278,5 +320,6 @@ int main() {
     }
     failures += cholesky_ops(ctx, mem);
     failures += tile_packer(ctx, mem);
+    failures += memory_unit(ctx);
     return failures == 0 ? 0 : 1;
 }

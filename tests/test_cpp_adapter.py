@@ -31,4 +31,4 @@ def test_adapter_all_combinations_pass_reference_rule():
     r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count("Pass") == 30
+    assert r.stdout.count("Pass") == 31
