@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--lowp", default="1e-4,1e-6,1e-8",
                     help="accuracies of the TF32 / BF16 low-precision sweep ('' to skip)")
     ap.add_argument("--lowp-steps", type=int, default=2, help="timed steps per low-precision run")
+    ap.add_argument("--no-tuning", action="store_true",
+                    help="default launch shapes instead of the autotuner's cache (hcorepp_gb300/tuning_cache.json)")
     return ap.parse_args()
 
 
@@ -384,22 +386,40 @@ def timed(torch, stream, steps, fn, world, sampler=None):
     return e0.elapsed_time(e1) / steps
 
 
+def tuned_config(wb, form, args):
+    """The autotuner's launch shapes for this workload's tile size, stack-width class and form."""
+    from hcorepp_gb300 import autotune
+    cfg = dict(autotune.DEFAULT)
+    cfg["groups"] = args.groups
+    if args.no_tuning:
+        return cfg, None
+    comp = np.array([[wb.c_t[(i, j)][0] == "C" for j in range(wb.nt)] for i in range(wb.nt)])
+    a_r = np.where(comp, wb.A.rank_grid(), wb.nb)
+    key = autotune.cache_key(wb.nb, autotune.mean_stack_width(a_r, wb.C0.rank_grid(), comp), form)
+    cache = autotune.load()
+    if key in cache:
+        cfg = autotune.lookup(key, cache)
+    return cfg, key if key in cache else None
+
+
 def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, steps=None, warmup=None):
     """Device-resident and end-to-end throughput of one form, its serialised stage times and its
     per-update records."""
     torch, L = wb.torch, wb.L
+    from hcorepp_gb300 import autotune
     params = wb.params(mode, accuracy)
     steps = steps or args.steps
     warmup = args.warmup if warmup is None else warmup
     ctx = wb.ctx
-    ctx.set_concurrency(args.groups)
+    cfg, key = tuned_config(wb, form, args)
+    autotune.apply(ctx, cfg)
     ctx.set_k_order(args.k_order)
     for _ in range(max(warmup, 1)):
         wb.step(params, record_info=True)
     torch.cuda.synchronize()
     info_h = wb.info.cpu().numpy()
     stream = torch.cuda.current_stream()
-    out = {"form": form, "note": FORM_NOTES.get(form, "")}
+    out = {"form": form, "note": FORM_NOTES.get(form, ""), "tuning": {"config": cfg, "cache_key": key}}
     l0 = L.kernel_launches()
     with ClockSampler(wb.local) as clk:
         ms = timed(torch, stream, steps, lambda: wb.step(params), world)
@@ -408,13 +428,14 @@ def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, step
     out.update(value=value, ms_per_step=ms, gpu_launches_per_step=launches, clocks=clk.summary())
     # One more multiply, serialised on one stream with CUDA events around every stage: the
     # per-kernel durations behind the roofline (not part of the timed region).
+    ctx.set_graph(False)
     ctx.set_concurrency(1)
     ctx.profile_reset()
     ctx.profile(True)
     wb.step(params)
     ctx.profile(False)
     out["stages"] = ctx.profile_read()
-    ctx.set_concurrency(args.groups)
+    autotune.apply(ctx, cfg)
     # the result of this form (same multiply as the timed steps) for the accuracy check
     if not args.no_check:
         out["result_dense"] = wb.Cw.to_dense_device()
@@ -423,6 +444,7 @@ def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, step
         moved = {}
         wb.e2e_step(params, moved)
         torch.cuda.synchronize()
+        ctx.set_graph(False)  # the e2e multiply runs on other tile matrices: no graph of its own
         e2e_ms = timed(torch, stream, steps, lambda: wb.e2e_step(params, moved), world)
         e2e_value, e2e_ms = job_throughput(e2e_ms, wb.n_updates, device="cuda")
         out["e2e"] = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(moved["h2d"]),
@@ -431,6 +453,7 @@ def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, step
                                   "buffers",
                       "result_matches_device_run": wb.e2e_matches_device_run(moved)}
     out["info"] = info_h
+    autotune.apply(ctx, autotune.DEFAULT)
     return out
 
 
@@ -595,6 +618,7 @@ def gpu_arm(args, rank, world, local):
         blk = {"value": res["value"], "unit": UNIT, "ms_per_step": res["ms_per_step"], "note": res["note"],
                "speedup_over_plain_fp64": res["value"] / head["value"],
                "gpu_launches_per_step": res["gpu_launches_per_step"], "clocks": res["clocks"],
+               "tuning": res["tuning"],
                "rel_fro_err_vs_fp64_dense_product": res.get("rel_fro_err_vs_fp64_dense_product"),
                "mean_final_rank": float(res["ranks_final"][comp_mask].mean())}
         if "e2e" in res:
@@ -631,7 +655,8 @@ def gpu_arm(args, rank, world, local):
         "config": {"workload": args.workload, "n": wb.w["n"], "nb": nb, "tiles": f"{nt}x{nt}",
                    "updates_per_step": wb.n_updates, "accuracy": wb.w["accuracy"], "threshold": "relative",
                    "dense_diagonal": wb.w["dense_diagonal"], "max_rank": maxr, "form": HEADLINE_FORM,
-                   "parallelism": "replicas" if world > 1 else "single_gpu", "c_tile_groups": args.groups,
+                   "parallelism": "replicas" if world > 1 else "single_gpu",
+                   "launch_shapes": head["tuning"],
                    "k_order": "ascending" if args.k_order == 0 else "cost-descending",
                    "l2": "inputs larger than L2 (A, C arenas 1.4 GB each), no flush"},
         "e2e": {k: v for k, v in head["e2e"].items() if k != "ms_per_step"},

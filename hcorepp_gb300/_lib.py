@@ -116,6 +116,10 @@ def lib():
                                             C.POINTER(C.c_double), C.POINTER(C.c_int)]
         L.hcgb_set_rank_model.argtypes = [vp, vp, ip]
         L.hcgb_set_feature_sink.argtypes = [vp, vp]
+        L.hcgb_set_graph.argtypes = [vp, ip]
+        L.hcgb_set_graph.restype = C.c_int
+        L.hcgb_set_tuning.argtypes = [vp, ip, ip]
+        L.hcgb_set_tuning.restype = C.c_int
         for nm in ("hcgb_rank_model_create", "hcgb_rank_model_destroy", "hcgb_rank_model_params",
                    "hcgb_rank_model_predict", "hcgb_rank_model_gradient", "hcgb_rank_model_train",
                    "hcgb_set_rank_model", "hcgb_set_feature_sink"):
@@ -175,6 +179,13 @@ class Context:
     def set_tensor_products(self, enable: bool):
         """Large factor products on the 16-bit tensor cores (FP64-accurate splitting) or on DMMA."""
         self.check(lib().hcgb_set_tensor_products(self._h, int(bool(enable))))
+
+    def set_graph(self, enable: bool):
+        """hcgb_tlr_gemm as a captured CUDA graph, replayed while the call is unchanged."""
+        self.check(lib().hcgb_set_graph(self._h, int(bool(enable))))
+
+    def set_tuning(self, oz_min_outputs: int = 2048, wy_min_reflectors: int = 48):
+        self.check(lib().hcgb_set_tuning(self._h, int(oz_min_outputs), int(wy_min_reflectors)))
 
     def set_concurrency(self, groups: int):
         self.check(lib().hcgb_set_concurrency(self._h, int(groups)))

@@ -16,6 +16,7 @@ using namespace hcgb;
 namespace hcgb {
 static std::atomic<long long> g_kernel_launches{0};
 void note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
+static void note_launches(long long n) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
 }  // namespace hcgb
 
 extern "C" long long hcgb_kernel_launches(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
@@ -42,6 +43,8 @@ struct hcgb_context {
     int groups = 8;
     int k_order = 0;  // 0: ascending k per C tile (reference order); 1: estimated cost, largest first
     int oz = 1;       // large factor products on the 16-bit tensor cores (FP64-accurate splitting)
+    int oz_min = OZ_MIN_OUTPUTS;     // tuning: outputs a product needs for the tensor cores
+    int wy_min = WY_MIN_REFLECTORS;  // tuning: reflectors a side needs for the WY Q application
     std::vector<cudaStream_t> group_streams;
     std::vector<cudaEvent_t> group_events;  // [0] fork, [1..] joins
     void *pack_desc = nullptr;  // DevTile[] of hcgb_pack_tiles / hcgb_unpack_tiles
@@ -56,6 +59,14 @@ struct hcgb_context {
     // per-matrix operations (hcgb_d*)
     void *be_scratch = nullptr;
     size_t be_scratch_bytes = 0;
+    // CUDA graph of the last hcgb_tlr_gemm (hcgb_set_graph)
+    bool graph_mode = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::string graph_key;      // the call's arguments and the context settings it was captured with
+    void *graph_desc = nullptr;  // descriptors the graph reads (its own buffer: other calls reuse desc)
+    size_t graph_desc_bytes = 0;
+    void *graph_ws = nullptr;    // workspace the graph was captured on
+    long long graph_launches = 0;
 };
 
 struct hcgb_rank_model {
@@ -186,6 +197,8 @@ size_t workspace_bytes_for(const Workspace &w, int n, bool features = false) {
 Params to_params(const hcgb_params *p, const hcgb_context *ctx) {
     Params q;
     q.oz = ctx ? ctx->oz : 1;
+    q.oz_min = ctx ? ctx->oz_min : OZ_MIN_OUTPUTS;
+    q.wy_min = ctx ? ctx->wy_min : WY_MIN_REFLECTORS;
     q.accuracy = p ? p->accuracy : 1e-9;
     q.truncated = p ? p->truncated_svd : 0;
     q.fixed_rank = p ? p->fixed_rank : 0;
@@ -378,6 +391,8 @@ int hcgb_context_destroy(hcgb_context *ctx) {
     if (ctx->pack_desc) cudaFree(ctx->pack_desc);
     if (ctx->tile_info) cudaFree(ctx->tile_info);
     if (ctx->be_scratch) cudaFree(ctx->be_scratch);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph_desc) cudaFree(ctx->graph_desc);
     if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
     for (auto &g : ctx->ev_pending)
@@ -449,6 +464,31 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         return fail(ctx, HCGB_BAD_ARG, "hcgb_tlr_gemm: bad grid");
     HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
     const int n = mt * nt;
+    // Graph mode: replay the captured multiply while its arguments and the context's settings are
+    // those it was captured with (and the workspace has not moved).
+    std::string key;
+    if (ctx->graph_mode) {
+        auto put = [&](const void *p, size_t b) { key.append(static_cast<const char *>(p), b); };
+        const int ints[] = {mt, nt, kt, ctx->groups, ctx->k_order, ctx->oz, ctx->learned ? 1 : 0, ctx->sk_policy,
+                            ctx->oz_min, ctx->wy_min};
+        put(ints, sizeof(ints));
+        put(&alpha, sizeof(alpha));
+        put(&beta, sizeof(beta));
+        hcgb_params pz{};
+        if (params) pz = *params;
+        put(&pz, sizeof(pz));
+        const void *ptrs[] = {ctx->model, ctx->feature_sink, info_dev, ctx->stream};
+        put(ptrs, sizeof(ptrs));
+        put(&ctx->sk_seed, sizeof(ctx->sk_seed));
+        put(a_grid, sizeof(hcgb_tile) * (size_t) mt * kt);
+        put(b_grid, sizeof(hcgb_tile) * (size_t) kt * nt);
+        put(c_grid, sizeof(hcgb_tile) * (size_t) n);
+        if (ctx->graph_exec && key == ctx->graph_key && ctx->graph_ws == ctx->ws) {
+            HCGB_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+            note_launches(ctx->graph_launches);
+            return HCGB_OK;
+        }
+    }
     // C tiles are split into G groups (tile index mod G); each group runs its own chain of k-waves
     // on its own stream, so one slow update delays only its group, not every C tile.
     const int G = std::max(1, std::min(ctx->groups, n));
@@ -551,14 +591,16 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     const size_t ub = sizeof(DevUpdate) * dv.size(), ub_al = (ub + 255) / 256 * 256;
     const size_t jb = sizeof(GemmJob) * JOBS_PER_UPDATE * (size_t) n, jb_al = (jb + 255) / 256 * 256;
     const size_t sb = sizeof(int) * SCHED_INTS_PER_UPDATE * (size_t) n;
-    if ((rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, ub_al + jb_al + sb))) return rc;
+    void **dbuf = ctx->graph_mode ? &ctx->graph_desc : &ctx->desc;
+    size_t *dbytes = ctx->graph_mode ? &ctx->graph_desc_bytes : &ctx->desc_bytes;
+    if ((rc = ensure_device(ctx, dbuf, dbytes, ub_al + jb_al + sb))) return rc;
     if ((rc = ensure_stage(ctx, ub))) return rc;
     std::memcpy(ctx->stage, dv.data(), ub);
-    HCGB_CUDA(ctx, cudaMemcpyAsync(ctx->desc, ctx->stage, ub, cudaMemcpyHostToDevice, ctx->stream));
+    HCGB_CUDA(ctx, cudaMemcpyAsync(*dbuf, ctx->stage, ub, cudaMemcpyHostToDevice, ctx->stream));
     HCGB_CUDA(ctx, cudaEventRecord(ctx->stage_done, ctx->stream));
-    auto *dups = static_cast<DevUpdate *>(ctx->desc);
-    auto *djobs = reinterpret_cast<GemmJob *>(static_cast<char *>(ctx->desc) + ub_al);
-    auto *dsched = reinterpret_cast<int *>(static_cast<char *>(ctx->desc) + ub_al + jb_al);
+    auto *dups = static_cast<DevUpdate *>(*dbuf);
+    auto *djobs = reinterpret_cast<GemmJob *>(static_cast<char *>(*dbuf) + ub_al);
+    auto *dsched = reinterpret_cast<int *>(static_cast<char *>(*dbuf) + ub_al + jb_al);
     const Params p = to_params(params, ctx);
     // Streams and fork/join events for the groups.
     while ((int) ctx->group_streams.size() < G) {
@@ -572,6 +614,21 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
         ctx->group_events.push_back(e);
     }
     const bool single = (G == 1);
+    // Graph mode: the descriptors are on the device before the capture; then every launch of the
+    // multiply (all groups, all waves) is recorded into one graph and the graph is launched.
+    const bool capture = ctx->graph_mode;
+    const bool prof_saved = ctx->prof;
+    long long launches0 = 0;
+    if (capture) {
+        HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->graph_exec) {
+            cudaGraphExecDestroy(ctx->graph_exec);
+            ctx->graph_exec = nullptr;
+        }
+        ctx->prof = false;  // no profiling events inside a graph
+        launches0 = hcgb_kernel_launches();
+        HCGB_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    }
     if (!single) HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[0], ctx->stream));
     std::vector<Workspace> wgs((size_t) G);
     for (int g = 0; g < G; g++) {
@@ -607,6 +664,21 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
             HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[g + 1], ctx->group_streams[g]));
             HCGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->group_events[g + 1], 0));
         }
+    if (capture) {
+        ctx->prof = prof_saved;
+        cudaGraph_t graph = nullptr;
+        HCGB_CUDA(ctx, cudaStreamEndCapture(ctx->stream, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            ctx->graph_exec = nullptr;
+            return fail(ctx, HCGB_CUDA_ERROR, std::string("hcgb_tlr_gemm: cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+        ctx->graph_key = key;
+        ctx->graph_ws = ctx->ws;
+        ctx->graph_launches = hcgb_kernel_launches() - launches0;
+        HCGB_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    }
     HCGB_CUDA(ctx, cudaGetLastError());
     return HCGB_OK;
 }
@@ -1270,7 +1342,7 @@ extern "C" int hcgb_dgemm(hcgb_context *ctx, int transa, int transb, int m, int 
     j.opB = transb;
     j.alpha = alpha;
     j.beta = beta;
-    j.oz = (ctx->oz && oz_shape(m, n, k)) ? 1 : 0;
+    j.oz = (ctx->oz && oz_shape(m, n, k, ctx->oz_min)) ? 1 : 0;
     const size_t jb = (sizeof(GemmJob) + 255) / 256 * 256;
     int rc = ensure_device(ctx, &ctx->desc, &ctx->desc_bytes, jb + sizeof(int) * 16);
     if (rc) return rc;
@@ -1426,5 +1498,24 @@ extern "C" int hcgb_dgesvd(hcgb_context *ctx, int jobu, int jobvt, int m, int n,
         if (info) *info = 1;
         return fail(ctx, HCGB_NOT_CONVERGED, "hcgb_dgesvd: Jacobi sweep limit reached");
     }
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_set_graph(hcgb_context *ctx, int enable) {
+    if (!ctx || (enable != 0 && enable != 1)) return HCGB_BAD_ARG;
+    ctx->graph_mode = enable != 0;
+    if (!enable && ctx->graph_exec) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaGraphExecDestroy(ctx->graph_exec);
+        ctx->graph_exec = nullptr;
+        ctx->graph_key.clear();
+    }
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_set_tuning(hcgb_context *ctx, int oz_min_outputs, int wy_min_reflectors) {
+    if (!ctx || oz_min_outputs < 1 || wy_min_reflectors < 1) return HCGB_BAD_ARG;
+    ctx->oz_min = oz_min_outputs;
+    ctx->wy_min = wy_min_reflectors;
     return HCGB_OK;
 }

@@ -93,8 +93,9 @@ __host__ __device__ inline int lowp_prec(int mode) { return mode == HCGB_TF32 ? 
 
 // Products worth the split (enough k to amortise the 4 FP64 instructions per output, enough outputs
 // for a tile).
-__host__ __device__ inline bool oz_shape(int M, int N, int K) {
-    return K >= 16 && M >= 16 && N >= 8 && (long long) M * N >= 2048;
+constexpr int OZ_MIN_OUTPUTS = 2048;
+__host__ __device__ inline bool oz_shape(int M, int N, int K, int min_outputs = OZ_MIN_OUTPUTS) {
+    return K >= 16 && M >= 16 && N >= 8 && (long long) M * N >= min_outputs;
 }
 
 struct DevTile {
@@ -172,6 +173,8 @@ struct Params {
     int mode;        // hcgb_mode: 0 plain FP64; 1 float-float QR / core / Q application; 2 / 3 TF32 / BF16
                      // factor products and Q-application products (QR, core, truncation in FP64)
     int oz;          // 1: large factor products on the 16-bit tensor cores (FP64-accurate splitting)
+    int oz_min;      // outputs a product needs to go to the tensor cores (OZ_MIN_OUTPUTS by default)
+    int wy_min;      // reflectors a side needs for the WY Q application (WY_MIN_REFLECTORS by default)
 };
 
 // ---- launchers (stream-ordered, asynchronous) ----

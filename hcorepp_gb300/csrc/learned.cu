@@ -154,7 +154,7 @@ __device__ __forceinline__ GemmJob sk_job(const double *A, int lda, int opA, con
     j.beta = 0.0;
     j.triA = j.triB = 0;
     j.prec = lowp_prec(p.mode);
-    j.oz = (!j.prec && p.oz && oz_shape(M, N, K)) ? 1 : 0;
+    j.oz = (!j.prec && p.oz && oz_shape(M, N, K, p.oz_min)) ? 1 : 0;
     return j;
 }
 

@@ -46,7 +46,7 @@ __global__ void plan_kernel(const DevUpdate *ups, int n, double alpha, double be
     for (int ph = 0; ph < 3; ph++) {
         GemmJob &j = jobs[(size_t) ph * n + s];
         j.prec = (lp && j.M > 0 && j.N > 0) ? lp : 0;
-        j.oz = (!j.prec && p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K)) ? 1 : 0;
+        j.oz = (!j.prec && p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K, p.oz_min)) ? 1 : 0;
     }
 }
 
@@ -454,7 +454,7 @@ __global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params
     for (int side = 0; side < 2; side++) {
         const int rows = side ? nn : m, kk = rows < k ? rows : k;
         const int lp = lowp_prec(p.mode);  // low-precision forms: every side in WY form
-        if (!lp && (!p.oz || kk < WY_MIN_REFLECTORS)) continue;  // panel-wise apply_q_kernel
+        if (!lp && (!p.oz || kk < p.wy_min)) continue;  // panel-wise apply_q_kernel
         if (kk < 1) continue;
         meta[META_WY] |= 1 << side;
         double *Vst = base + (side ? ws.off_vstack : ws.off_ustack);
@@ -474,7 +474,7 @@ __global__ void plan_wy_kernel(const DevUpdate *ups, int n, Workspace ws, Params
         GemmJob *out[3] = {&g, &y, &u};
         for (int q = 0; q < 3; q++) {
             GemmJob &j = *out[q];
-            j.oz = (!j.prec && p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K)) ? 1 : 0;
+            j.oz = (!j.prec && p.oz && j.M > 0 && j.N > 0 && oz_shape(j.M, j.N, j.K, p.oz_min)) ? 1 : 0;
             jobs[(size_t) (2 * q + side) * n + s] = j;
         }
     }

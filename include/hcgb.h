@@ -166,6 +166,22 @@ int hcgb_set_concurrency(hcgb_context *ctx, int groups);
  * within the accuracy bound).  The expensive updates of all tiles then share a few k-waves. */
 int hcgb_set_k_order(hcgb_context *ctx, int policy);
 
+/* enable = 1: hcgb_tlr_gemm records every launch of a multiply (all C-tile groups and k-waves) into
+ * one CUDA graph and launches the graph; a later call with the same arguments (grids, alpha, beta,
+ * params, info_dev) and the same context settings replays it without any per-kernel launch from
+ * the host.  The descriptors and the k order are those of the capturing call: with the cost-first
+ * k order (hcgb_set_k_order 1) a replay keeps the order computed from the ranks at capture time
+ * (the sum is the same in any order).  The workspace must not be reallocated in between (another
+ * call needing a larger one forces a new capture).  enable = 0 drops the graph.  Default 0. */
+int hcgb_set_graph(hcgb_context *ctx, int enable);
+
+/* Tuning knobs of the batched pipeline (chosen by hcorepp_gb300/autotune.py per tile size and
+ * stack-width class; results do not depend on them beyond rounding): a factor product goes to the
+ * FP64-accurate tensor-core path when it has at least oz_min_outputs outputs (default 2048, with
+ * K >= 16, M >= 16, N >= 8), and in the plain form a side's Q is applied in WY form when it has at
+ * least wy_min_reflectors reflectors (default 48). */
+int hcgb_set_tuning(hcgb_context *ctx, int oz_min_outputs, int wy_min_reflectors);
+
 /* Factor products of k >= 16 with at least 2048 outputs run on the 16-bit tensor cores by
  * error-free splitting (each FP64 operand cut into eight 7-bit integer digit planes relative to its
  * row / column maximum, plane products accumulated exactly in FP32 and combined in FP64; result

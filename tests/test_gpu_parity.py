@@ -261,6 +261,54 @@ def test_tlr_multiply_concurrency_invariant(T):
         np.testing.assert_array_equal(arena, outs[0][0])
 
 
+@pytest.mark.parametrize("k_order", [0, 1])
+def test_tlr_multiply_graph_replay_bitwise(T, k_order):
+    """hcgb_set_graph: the multiply captured as one CUDA graph and replayed gives the same bits as the
+    directly launched multiply, call after call, and its launches are counted."""
+    import torch
+    from hcorepp_gb300 import _lib as L
+    from hcorepp_gb300.problems import KernelMatrix
+    nt, nb, acc = 4, 96, 1e-8
+    km = KernelMatrix(nt * nb, nb, 2, 0.1, 1)
+    kc = KernelMatrix(nt * nb, nb, 2, 0.1, 2)
+    kinds = [[L.DENSE if i == j else L.COMPRESSED for j in range(nt)] for i in range(nt)]
+    A = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+    C0 = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+    for i in range(nt):
+        for j in range(nt):
+            if i == j:
+                A.set_tile(i, j, dense=km.tile(i, j))
+                C0.set_tile(i, j, dense=kc.tile(i, j))
+            else:
+                ta = compressed_from_dense(km.tile(i, j), acc)
+                tc = compressed_from_dense(kc.tile(i, j), acc)
+                A.set_tile(i, j, u=ta.u, v=ta.v)
+                C0.set_tile(i, j, u=tc.u, v=tc.v)
+    ctx = T.run_context()
+    ctx.set_k_order(k_order)
+    C = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+    params = T.CompressionParameters(acc, truncated_svd=True)
+    outs = []
+    try:
+        for graph in (False, True, True, True):
+            ctx.set_graph(graph)
+            C.arena.copy_(C0.arena)
+            C.ranks.copy_(C0.ranks)
+            l0 = L.kernel_launches()
+            T.tlr_gemm(1.0, A, A, 1.0, C, params)
+            torch.cuda.synchronize()
+            outs.append((C.arena.cpu().numpy().copy(), C.ranks.cpu().numpy().copy(), L.kernel_launches() - l0))
+    finally:
+        ctx.set_graph(False)
+        ctx.set_k_order(0)
+    for arena, ranks, launches in outs[1:]:
+        np.testing.assert_array_equal(ranks, outs[0][1])
+        np.testing.assert_array_equal(arena, outs[0][0])
+        # a replay launches the captured kernels; the capturing call also ran the rank gather of the
+        # cost-first order before its capture
+        assert outs[0][2] > 0 and 0 <= outs[0][2] - launches <= k_order
+
+
 @pytest.mark.parametrize("combo", ["CCC", "DCC", "CDC"])
 def test_mixed_mode_vs_oracle(T, combo):
     """HCGB_MIXED (single-precision Jacobi preconditioning of the core): same ranks (+-1) and
