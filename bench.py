@@ -444,7 +444,6 @@ def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, step
         moved = {}
         wb.e2e_step(params, moved)
         torch.cuda.synchronize()
-        ctx.set_graph(False)  # the e2e multiply runs on other tile matrices: no graph of its own
         e2e_ms = timed(torch, stream, steps, lambda: wb.e2e_step(params, moved), world)
         e2e_value, e2e_ms = job_throughput(e2e_ms, wb.n_updates, device="cuda")
         out["e2e"] = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(moved["h2d"]),
