@@ -57,6 +57,10 @@ FORM_NOTES = {
                   "FP64 pipe; factor products FP64-accurate (DMMA, or 16-bit tensor cores by error-free splitting)",
     "mixed_ff48": "stack QR, core pivoted QR + Jacobi and Q application in float-float (48-bit significand) on the "
                   "FP32 pipe; core product, new factors, truncation test and factor products as in plain_fp64",
+    "learned_ff48": "mixed_ff48 with the learned form: an MLP (trained on plain runs of other seeds, "
+                    "hcorepp_gb300/rank_model_weights.npy) sizes a Gaussian sketch of each update; the plain "
+                    "recompression runs where the a-posteriori residual test fails",
+    "learned_plain": "plain_fp64 with the learned form (sketch sized by the MLP, plain fallback)",
 }
 
 
@@ -67,7 +71,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tlr_gemm_n16384_nb512", choices=sorted(WORKLOADS))
-    ap.add_argument("--forms", default="plain_fp64,mixed_ff48",
+    ap.add_argument("--forms", default="plain_fp64,mixed_ff48,learned_ff48,learned_plain",
                     help="comma-separated forms; plain_fp64 (the headline) always runs first")
     ap.add_argument("--cpu-tiles", type=int, default=256, help="C tiles (each with its full k-chain) in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -414,6 +418,11 @@ def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, step
     cfg, key = tuned_config(wb, form, args)
     autotune.apply(ctx, cfg)
     ctx.set_k_order(args.k_order)
+    model = None
+    if form.startswith("learned"):
+        from hcorepp_gb300 import rank_model as RM
+        model = RM.RankModel.load(ctx=ctx)
+        model.enable(ctx)
     for _ in range(max(warmup, 1)):
         wb.step(params, record_info=True)
     torch.cuda.synchronize()
@@ -453,6 +462,10 @@ def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, step
                       "result_matches_device_run": wb.e2e_matches_device_run(moved)}
     out["info"] = info_h
     autotune.apply(ctx, autotune.DEFAULT)
+    if model is not None:
+        from hcorepp_gb300 import rank_model as RM
+        RM.learned_off(ctx)
+        out["model"] = model  # kept alive while the context may still reference it
     return out
 
 
@@ -549,7 +562,11 @@ def gpu_arm(args, rank, world, local):
 
     forms = [f for f in args.forms.split(",") if f]
     forms = [HEADLINE_FORM] + [f for f in forms if f != HEADLINE_FORM]
-    modes = {"plain_fp64": L.PLAIN_FP64, "mixed_ff48": L.MIXED}
+    modes = {"plain_fp64": L.PLAIN_FP64, "mixed_ff48": L.MIXED, "learned_ff48": L.MIXED,
+             "learned_plain": L.PLAIN_FP64}
+    from hcorepp_gb300 import rank_model as RM
+    if not os.path.exists(RM.WEIGHTS):
+        forms = [f for f in forms if not f.startswith("learned")]
     for f in forms:
         if f not in modes:
             raise SystemExit(f"unknown form {f}")
@@ -618,6 +635,8 @@ def gpu_arm(args, rank, world, local):
                "speedup_over_plain_fp64": res["value"] / head["value"],
                "gpu_launches_per_step": res["gpu_launches_per_step"], "clocks": res["clocks"],
                "tuning": res["tuning"],
+               "updates_sketched": int(np.count_nonzero(res["info"][:, 13] > 0)),
+               "sketches_accepted": int(np.count_nonzero(res["info"][:, 14] > 0)),
                "rel_fro_err_vs_fp64_dense_product": res.get("rel_fro_err_vs_fp64_dense_product"),
                "mean_final_rank": float(res["ranks_final"][comp_mask].mean())}
         if "e2e" in res:

@@ -67,6 +67,7 @@ struct hcgb_context {
     size_t graph_desc_bytes = 0;
     void *graph_ws = nullptr;    // workspace the graph was captured on
     long long graph_launches = 0;
+    cudaStream_t capture_stream = nullptr;  // captures run here when the context stream is the legacy one
 };
 
 struct hcgb_rank_model {
@@ -392,6 +393,7 @@ int hcgb_context_destroy(hcgb_context *ctx) {
     if (ctx->tile_info) cudaFree(ctx->tile_info);
     if (ctx->be_scratch) cudaFree(ctx->be_scratch);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     if (ctx->graph_desc) cudaFree(ctx->graph_desc);
     if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
@@ -619,20 +621,29 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     const bool capture = ctx->graph_mode;
     const bool prof_saved = ctx->prof;
     long long launches0 = 0;
+    // The stream the launches are issued on: the context's, or for a capture on the legacy default
+    // stream (which cannot be captured) a stream of the context's own; the graph then runs on the
+    // context's stream.
+    cudaStream_t main_st = ctx->stream;
     if (capture) {
         HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (ctx->graph_exec) {
             cudaGraphExecDestroy(ctx->graph_exec);
             ctx->graph_exec = nullptr;
         }
+        if (!main_st) {
+            if (!ctx->capture_stream)
+                HCGB_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking));
+            main_st = ctx->capture_stream;
+        }
         ctx->prof = false;  // no profiling events inside a graph
         launches0 = hcgb_kernel_launches();
-        HCGB_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        HCGB_CUDA(ctx, cudaStreamBeginCapture(main_st, cudaStreamCaptureModeThreadLocal));
     }
-    if (!single) HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[0], ctx->stream));
+    if (!single) HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[0], main_st));
     std::vector<Workspace> wgs((size_t) G);
     for (int g = 0; g < G; g++) {
-        cudaStream_t st = single ? ctx->stream : ctx->group_streams[g];
+        cudaStream_t st = single ? main_st : ctx->group_streams[g];
         if (!single) HCGB_CUDA(ctx, cudaStreamWaitEvent(st, ctx->group_events[0], 0));
         Workspace &wg = wgs[g];
         wg = ws;
@@ -649,7 +660,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     for (int kk = 0; kk < kt; kk++)
         for (int g = 0; g < G; g++) {
             const int ng = first[g + 1] - first[g];
-            cudaStream_t st = single ? ctx->stream : ctx->group_streams[g];
+            cudaStream_t st = single ? main_st : ctx->group_streams[g];
             const size_t off = (size_t) first[g] * kt + (size_t) kk * ng;
             BatchShape shw = shape_of(all.data() + off, ng);
             shw.ld = sh.ld;
@@ -662,12 +673,12 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     if (!single)
         for (int g = 0; g < G; g++) {
             HCGB_CUDA(ctx, cudaEventRecord(ctx->group_events[g + 1], ctx->group_streams[g]));
-            HCGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->group_events[g + 1], 0));
+            HCGB_CUDA(ctx, cudaStreamWaitEvent(main_st, ctx->group_events[g + 1], 0));
         }
     if (capture) {
         ctx->prof = prof_saved;
         cudaGraph_t graph = nullptr;
-        HCGB_CUDA(ctx, cudaStreamEndCapture(ctx->stream, &graph));
+        HCGB_CUDA(ctx, cudaStreamEndCapture(main_st, &graph));
         const cudaError_t e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
