@@ -24,6 +24,10 @@ namespace hcgb {
 namespace {
 
 constexpr int SVD_THREADS = 512;
+// Plain form: cores with at least this many Jacobi columns get the FP32 preconditioning sweeps.
+constexpr int PRECOND_MIN_COLS = 16;
+constexpr float PRECOND_TOL32 = 1e-6f;
+constexpr int PRECOND_MAX_SWEEPS = 12;
 constexpr int SVD_RED_DOUBLES = 64, SVD_REDI_INTS = 128;  // reduction area (up to 32 warps)
 constexpr int SVD_AUX_FIXED = 1 + SVD_RED_DOUBLES + SVD_REDI_INTS / 2;  // aux = 6 kmax + this
 
@@ -388,6 +392,75 @@ __device__ void jacobi_dispatch(const TM &tm, double *X, int ldx, int rows, int 
     else if (rows <= 256 && MAXRPL >= 16) jacobi<16, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 256 || MAXRPL <= 8) jacobi<32, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else jacobi<32, MAXRPL>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP32 preconditioning of the plain form's Jacobi (the FP64 pipe is the plain core's bound): one-
+// sided Jacobi in single precision on X32 = X * 2^-e (rows x ncols, ld rows) with the rotations
+// accumulated in J32 (ncols x ncols, ld ncols), one warp per column pair, until every pair is
+// orthogonal to tol32 or max_sweeps.  The caller then forms X J32 in FP64 and finishes with FP64
+// sweeps.  J32 is orthogonal only to single precision; that is a multiplicative perturbation
+// X -> X G (||G^T G - I|| ~ 1e-6), which moves the singular values by that relative amount and
+// the kept singular subspace by ~1e-6 sigma_j / sigma_i, while the FP64 sweeps make the final
+// columns orthogonal to working precision (the new factors are the projection of M onto them).
+// ---------------------------------------------------------------------------------------------
+template <class TM>
+__device__ int jacobi_precond32(const TM &tm, float *X, int rows, int ncols, float *J, float tol32, int max_sweeps,
+                                int *s_rot) {
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
+    for (int e = tm.tid; e < ncols * ncols; e += tm.nth) J[e] = (e % ncols) == (e / ncols) ? 1.f : 0.f;
+    const int n2 = ncols + (ncols & 1);
+    const float tol2 = tol32 * tol32;
+    int sweeps = 0;
+    for (; sweeps < max_sweeps; sweeps++) {
+        if (tm.tid == 0) *s_rot = 0;
+        tm.sync();
+        int rot = 0;
+        for (int t = 0; t < n2 - 1; t++) {
+            for (int pp = warp; pp < n2 / 2; pp += nw) {
+                int i, j;
+                jacobi_pair(t, pp, n2, i, j);
+                if (i >= ncols || j >= ncols) continue;
+                float *xi = X + (size_t) i * rows, *xj = X + (size_t) j * rows;
+                float a = 0.f, b = 0.f, c = 0.f;
+                for (int r = lane; r < rows; r += 32) {
+                    const float u = xi[r], w = xj[r];
+                    a = fmaf(u, u, a);
+                    b = fmaf(w, w, b);
+                    c = fmaf(u, w, c);
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    a += __shfl_xor_sync(0xffffffffu, a, o);
+                    b += __shfl_xor_sync(0xffffffffu, b, o);
+                    c += __shfl_xor_sync(0xffffffffu, c, o);
+                }
+                if (c == 0.f || c * c <= tol2 * a * b) continue;
+                const float zeta = (b - a) / (2.f * c);
+                const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
+                const float cs = rsqrtf(fmaf(tt, tt, 1.f)), sn = cs * tt;
+                for (int r = lane; r < rows; r += 32) {
+                    const float u = xi[r], w = xj[r];
+                    xi[r] = cs * u - sn * w;
+                    xj[r] = fmaf(sn, u, cs * w);
+                }
+                float *ji = J + (size_t) i * ncols, *jj = J + (size_t) j * ncols;
+                for (int r = lane; r < ncols; r += 32) {
+                    const float u = ji[r], w = jj[r];
+                    ji[r] = cs * u - sn * w;
+                    jj[r] = fmaf(sn, u, cs * w);
+                }
+                rot++;
+            }
+            tm.sync();
+        }
+        if (lane == 0 && rot) atomicAdd(s_rot, rot);
+        tm.sync();
+        const bool done = *s_rot == 0;
+        tm.sync();
+        if (done) break;
+    }
+    return sweeps;
 }
 
 // Householder QR with column pivoting of A (mrows x ncols, ld lda) in place, stopped early once
@@ -884,6 +957,46 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
         }
         tm.sync();
     } else {
+        if (rk >= PRECOND_MIN_COLS) {
+            // FP32 sweeps with accumulated rotations (FP32 pipe), then X <- X J in FP64: the FP64
+            // sweeps below start from a nearly orthogonal X and need about half as many.
+            float *X32 = reinterpret_cast<float *>(base + ws.off_mixed);
+            float *J32 = X32 + (size_t) kV * rk;
+            if (tm.tid == 0) s_emax = 0;
+            tm.sync();
+            int em = 0;
+            for (int e = tm.tid; e < kV * rk; e += tm.nth) {
+                const int ef = (int) ((__double_as_longlong(X[(e % kV) + (size_t) (e / kV) * ldx]) >> 52) & 0x7ff);
+                em = em > ef ? em : ef;
+            }
+            atomicMax(&s_emax, em);
+            tm.sync();
+            const int esc = s_emax ? s_emax - 1023 : 0;
+            const double down = __hiloint2double((1023 - esc) << 20, 0);
+            for (int e = tm.tid; e < kV * rk; e += tm.nth)
+                X32[e] = (float) (X[(e % kV) + (size_t) (e / kV) * ldx] * down);
+            tm.sync();
+            jacobi_precond32(tm, X32, kV, rk, J32, PRECOND_TOL32, PRECOND_MAX_SWEEPS, &s_rot);
+            // XV (ld ws.ld) <- X J32 in FP64, then back into X
+            for (int e = tm.tid; e < kV * rk; e += tm.nth) {
+                const int r = e % kV, c = e / kV;
+                const float *jc = J32 + (size_t) c * rk;
+                double s0 = 0.0, s1 = 0.0;
+                int l = 0;
+                for (; l + 1 < rk; l += 2) {
+                    s0 = fma(X[r + (size_t) l * ldx], (double) jc[l], s0);
+                    s1 = fma(X[r + (size_t) (l + 1) * ldx], (double) jc[l + 1], s1);
+                }
+                if (l < rk) s0 = fma(X[r + (size_t) l * ldx], (double) jc[l], s0);
+                XV[r + (size_t) c * ld] = s0 + s1;
+            }
+            tm.sync();
+            for (int e = tm.tid; e < kV * rk; e += tm.nth) {
+                const int r = e % kV, c = e / kV;
+                X[r + (size_t) c * ldx] = XV[r + (size_t) c * ld];
+            }
+            tm.sync();
+        }
         jacobi_dispatch<RPL>(tm, X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64, MAX_JACOBI_SWEEPS,
                              dsc, ws.kmax);
     }
