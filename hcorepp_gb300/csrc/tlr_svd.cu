@@ -397,18 +397,18 @@ __device__ void jacobi_dispatch(const TM &tm, double *X, int ldx, int rows, int 
 // ---------------------------------------------------------------------------------------------
 // FP32 preconditioning of the plain form's Jacobi (the FP64 pipe is the plain core's bound): one-
 // sided Jacobi in single precision on X32 = X * 2^-e (rows x ncols, ld rows) with the rotations
-// accumulated in J32 (ncols x ncols, ld ncols), one warp per column pair, until every pair is
-// orthogonal to tol32 or max_sweeps.  The caller then forms X J32 in FP64 and finishes with FP64
-// sweeps.  J32 is orthogonal only to single precision; that is a multiplicative perturbation
-// X -> X G (||G^T G - I|| ~ 1e-6), which moves the singular values by that relative amount and
-// the kept singular subspace by ~1e-6 sigma_j / sigma_i, while the FP64 sweeps make the final
-// columns orthogonal to working precision (the new factors are the projection of M onto them).
+// accumulated in J (ncols x ncols, ld ncols, float-float), one warp per column pair, until every
+// pair is orthogonal to tol32 or max_sweeps.  The caller then forms X J in FP64 and finishes with
+// FP64 sweeps.  Each rotation is the rotation of a float tangent normalised to float-float accuracy,
+// and J accumulates them in float-float, so J is orthogonal to ~1e-13: X -> X J moves singular values
+// and subspaces only at that level (a truncation at a fixed rank inside a slowly decaying spectrum
+// included), and the FP64 sweeps make the final columns orthogonal to working precision.
 // ---------------------------------------------------------------------------------------------
 template <class TM>
-__device__ int jacobi_precond32(const TM &tm, float *X, int rows, int ncols, float *J, float tol32, int max_sweeps,
+__device__ int jacobi_precond32(const TM &tm, float *X, int rows, int ncols, df *J, float tol32, int max_sweeps,
                                 int *s_rot) {
     const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
-    for (int e = tm.tid; e < ncols * ncols; e += tm.nth) J[e] = (e % ncols) == (e / ncols) ? 1.f : 0.f;
+    for (int e = tm.tid; e < ncols * ncols; e += tm.nth) J[e] = df_f((e % ncols) == (e / ncols) ? 1.f : 0.f);
     const int n2 = ncols + (ncols & 1);
     const float tol2 = tol32 * tol32;
     int sweeps = 0;
@@ -438,17 +438,22 @@ __device__ int jacobi_precond32(const TM &tm, float *X, int rows, int ncols, flo
                 if (c == 0.f || c * c <= tol2 * a * b) continue;
                 const float zeta = (b - a) / (2.f * c);
                 const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
-                const float cs = rsqrtf(fmaf(tt, tt, 1.f)), sn = cs * tt;
+                // The rotation of the float tangent, normalised to float-float accuracy
+                // (cs = 1 / sqrt(1 + t^2), sn = cs t): orthogonal to ~2^-46, so the accumulated J is
+                // orthogonal to working precision of the FP64 phase's purposes.
+                const df tdf = df_f(tt);
+                const df cs = df_rsqrt(df_fma(tdf, tdf, df_f(1.f))), sn = df_mul(cs, tdf);
+                const float cs32 = cs.h, sn32 = sn.h;
                 for (int r = lane; r < rows; r += 32) {
                     const float u = xi[r], w = xj[r];
-                    xi[r] = cs * u - sn * w;
-                    xj[r] = fmaf(sn, u, cs * w);
+                    xi[r] = cs32 * u - sn32 * w;
+                    xj[r] = fmaf(sn32, u, cs32 * w);
                 }
-                float *ji = J + (size_t) i * ncols, *jj = J + (size_t) j * ncols;
+                df *ji = J + (size_t) i * ncols, *jj = J + (size_t) j * ncols;
                 for (int r = lane; r < ncols; r += 32) {
-                    const float u = ji[r], w = jj[r];
-                    ji[r] = cs * u - sn * w;
-                    jj[r] = fmaf(sn, u, cs * w);
+                    const df u = ji[r], w = jj[r];
+                    ji[r] = df_fma(-sn, w, df_mul(cs, u));
+                    jj[r] = df_fma(sn, u, df_mul(cs, w));
                 }
                 rot++;
             }
@@ -957,11 +962,14 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
         }
         tm.sync();
     } else {
-        if (rk >= PRECOND_MIN_COLS) {
+        // X32 (kV x rk floats) and J (rk x rk float-float) in the float region of the slot
+        const size_t x32_floats = ((size_t) kV * rk + 1) & ~size_t(1);
+        const bool fits = x32_floats + 2 * (size_t) rk * rk <= (size_t) ws.kmax * (ws.kmax + ws.ld);
+        if (rk >= PRECOND_MIN_COLS && fits) {
             // FP32 sweeps with accumulated rotations (FP32 pipe), then X <- X J in FP64: the FP64
             // sweeps below start from a nearly orthogonal X and need about half as many.
             float *X32 = reinterpret_cast<float *>(base + ws.off_mixed);
-            float *J32 = X32 + (size_t) kV * rk;
+            df *J32 = reinterpret_cast<df *>(X32 + x32_floats);
             if (tm.tid == 0) s_emax = 0;
             tm.sync();
             int em = 0;
@@ -980,7 +988,7 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
             // XV (ld ws.ld) <- X J32 in FP64, then back into X
             for (int e = tm.tid; e < kV * rk; e += tm.nth) {
                 const int r = e % kV, c = e / kV;
-                const float *jc = J32 + (size_t) c * rk;
+                const df *jc = J32 + (size_t) c * rk;
                 double s0 = 0.0, s1 = 0.0;
                 int l = 0;
                 for (; l + 1 < rk; l += 2) {
