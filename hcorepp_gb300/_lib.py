@@ -102,6 +102,9 @@ def lib():
         L.hcgb_set_k_order.restype = C.c_int
         L.hcgb_compress_tile.argtypes = [vp, vp, ip, ip, C.POINTER(Tile), C.POINTER(Params), C.POINTER(C.c_int)]
         L.hcgb_compress_tile.restype = C.c_int
+        L.hcgb_compress_tiles.argtypes = [vp, ip, C.POINTER(vp), ip, ip, C.POINTER(Tile), C.POINTER(Params),
+                                          C.POINTER(C.c_int)]
+        L.hcgb_compress_tiles.restype = C.c_int
         L.hcgb_tile_gemm_noalloc.argtypes = [C.c_double, C.POINTER(Tile), C.POINTER(Tile), C.c_double,
                                              C.POINTER(Tile), C.POINTER(Params), vp, vp]
         L.hcgb_tile_gemm_noalloc.restype = C.c_int

@@ -342,6 +342,20 @@ int prepare_workspace(hcgb_context *ctx, const BatchShape &sh, int n, bool ddc, 
     return HCGB_OK;
 }
 
+// Updates per pipeline launch for a batch of shape `sh`: at most `limit`, and few enough that the
+// workspace stays within half of the device memory that is free or already held by the context.
+int updates_per_launch(hcgb_context *ctx, const BatchShape &sh, int mode, int limit) {
+    const bool features = ctx->learned || ctx->feature_sink;
+    const Workspace w = make_workspace_layout(sh.ld, sh.kmax, sh.rmax, false, ctx->oz != 0 || lowp_prec(mode) != 0,
+                                              ctx->learned);
+    const size_t per = workspace_bytes_for(w, 1, features);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return limit;
+    const size_t budget = (free_b + ctx->ws_bytes) / 2;
+    const size_t fit = per ? budget / (per + per / 8) : (size_t) limit;
+    return (int) std::max<size_t>(1, std::min<size_t>((size_t) limit, fit));
+}
+
 // Upload `n` device update descriptors and make room for 3n jobs; returns device pointers.
 int upload_updates(hcgb_context *ctx, const std::vector<DevUpdate> &dv, DevUpdate **dups, GemmJob **djobs,
                    int **sched) {
@@ -987,6 +1001,67 @@ extern "C" int hcgb_compress_tile(hcgb_context *ctx, const double *dense, int ro
     return rc;
 }
 
+extern "C" int hcgb_compress_tiles(hcgb_context *ctx, int count, const double *const *dense, int rows, int cols,
+                                   hcgb_tile *out, const hcgb_params *params, int *ranks) {
+    if (!ctx) return HCGB_BAD_ARG;
+    if (count < 0 || (count > 0 && (!dense || !out)) || rows <= 0 || cols <= 0)
+        return fail(ctx, HCGB_BAD_ARG, "hcgb_compress_tiles: bad arguments");
+    for (int i = 0; i < count; i++)
+        if (!dense[i] || !compressed(out[i].kind) || out[i].rows != rows || out[i].cols != cols || !out[i].rank ||
+            out[i].max_rank <= 0)
+            return fail(ctx, HCGB_BAD_ARG, "hcgb_compress_tiles: bad tile " + std::to_string(i));
+    if (count == 0) return HCGB_OK;
+    HCGB_CUDA(ctx, cudaSetDevice(ctx->device));
+    // Every tile is the update C_i = D_i * I with C_i at rank 0 (as in hcgb_compress_tile); the
+    // identity factors are shared by the whole batch.
+    double *ibuf = nullptr;
+    int *irank = nullptr;
+    hcgb_update_info *dinfo = nullptr;
+    const size_t n = (size_t) cols;
+    auto done = [&](int rc) {
+        cudaStreamSynchronize(ctx->stream);
+        if (ibuf) cudaFree(ibuf);
+        if (irank) cudaFree(irank);
+        if (dinfo) cudaFree(dinfo);
+        return rc;
+    };
+    if (cudaMalloc(&ibuf, sizeof(double) * 2 * n * n) != cudaSuccess || cudaMalloc(&irank, sizeof(int)) != cudaSuccess)
+        return done(fail(ctx, HCGB_CUDA_ERROR, "hcgb_compress_tiles: cudaMalloc failed"));
+    { identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf, cols, cols); note_launch(); }
+    { identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf + n * n, cols, cols); note_launch(); }
+    const int ncols = cols;
+    HCGB_CUDA(ctx, cudaMemcpyAsync(irank, &ncols, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    const hcgb_tile ident{ibuf, irank, cols, cols, cols, HCGB_COMPRESSED};
+    std::vector<hcgb_update> ups(count);
+    for (int i = 0; i < count; i++) {
+        HCGB_CUDA(ctx, cudaMemsetAsync(out[i].rank, 0, sizeof(int), ctx->stream));
+        ups[i] = hcgb_update{hcgb_tile{const_cast<double *>(dense[i]), nullptr, rows, cols, 0, HCGB_DENSE}, ident,
+                             out[i]};
+    }
+    const int mode = params ? params->mode : 0;
+    const int chunk = updates_per_launch(ctx, shape_of(ups.data(), 1), mode, count);
+    if (cudaMalloc(&dinfo, sizeof(hcgb_update_info) * (size_t) chunk) != cudaSuccess)
+        return done(fail(ctx, HCGB_CUDA_ERROR, "hcgb_compress_tiles: cudaMalloc failed"));
+    std::vector<hcgb_update_info> hinfo(chunk);
+    bool not_converged = false;
+    for (int off = 0; off < count; off += chunk) {
+        const int nb = std::min(chunk, count - off);
+        int rc = hcgb_gemm_batch(ctx, 1.0, 0.0, nb, ups.data() + off, params, dinfo);
+        if (rc) return done(rc);
+        HCGB_CUDA(ctx, cudaMemcpyAsync(hinfo.data(), dinfo, sizeof(hcgb_update_info) * (size_t) nb,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int i = 0; i < nb; i++) {
+            const int st = hinfo[i].status;
+            if (st == HCGB_NOT_CONVERGED) not_converged = true;
+            else if (st != HCGB_OK)
+                return done(fail(ctx, st, "hcgb_compress_tiles: tile " + std::to_string(off + i) + " failed"));
+            if (ranks) ranks[off + i] = hinfo[i].new_rank;
+        }
+    }
+    return done(not_converged ? HCGB_NOT_CONVERGED : HCGB_OK);
+}
+
 extern "C" int hcgb_potrf(hcgb_context *ctx, int uplo, int n, double *A, int lda, int *info) {
     if (!ctx) return HCGB_BAD_ARG;
     if (!A || n < 0 || lda < (n > 1 ? n : 1) || (uplo != HCGB_LOWER && uplo != HCGB_UPPER))
@@ -1121,7 +1196,7 @@ extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *gr
         return rc;
     };
     const Params p = to_params(params, ctx);
-    const int chunk = 1024;  // updates per pipeline launch (bounds the workspace)
+    const int max_chunk = 1024;  // updates per pipeline launch (bounds the workspace)
     int uid = 0;
     auto tile = [&](int i, int j) -> const hcgb_tile & { return grid[i + (size_t) j * nt]; };
     for (int k = 0; k < nt; k++) {
@@ -1161,6 +1236,7 @@ extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *gr
                 std::swap(db.rows, db.cols);
                 dv.push_back(DevUpdate{to_dev(ta), db, to_dev(tc), uid++});
             }
+        const int chunk = updates_per_launch(ctx, shape_of(hu.data(), (int) hu.size()), p.mode, max_chunk);
         for (size_t off = 0; off < dv.size(); off += chunk) {
             const int n = (int) std::min<size_t>(chunk, dv.size() - off);
             std::vector<DevUpdate> part(dv.begin() + off, dv.begin() + off + n);

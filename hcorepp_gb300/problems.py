@@ -112,12 +112,12 @@ def compress_dense(d: np.ndarray, accuracy: float, truncated: bool = True, max_r
 
 
 def _tile_job(args):
-    n, nb, d, ell, seed, diag_shift, i, j, accuracy, dense = args
+    n, nb, d, ell, seed, diag_shift, i, j, accuracy, dense, max_rank = args
     km = _cached_matrix(n, nb, d, ell, seed, diag_shift)
     blk = km.tile(i, j)
     if dense:
         return (i, j), ("D", blk)
-    u, v, cap = compress_dense(blk, accuracy, True)
+    u, v, cap = compress_dense(blk, accuracy, True, max_rank)
     return (i, j), ("C", u, v, cap)
 
 
@@ -131,12 +131,14 @@ def _cached_matrix(n, nb, d, ell, seed, diag_shift):
     return _KM_CACHE[key]
 
 
-def build_tiles(n, nb, d, ell, seed, accuracy, dense_diagonal, processes=None, diag_shift=0.0):
-    """All tiles of one matrix: dict (i, j) -> ("D", dense) | ("C", u, v, max_rank)."""
+def build_tiles(n, nb, d, ell, seed, accuracy, dense_diagonal, processes=None, diag_shift=0.0,
+                lower_only=False, max_rank=None):
+    """All tiles of one matrix (or those with i >= j): dict (i, j) -> ("D", dense) | ("C", u, v,
+    max_rank); compressed tiles get capacity max_rank (default the reference's min(m, n) / 3)."""
     import multiprocessing as mp
     nt = n // nb
-    jobs = [(n, nb, d, ell, seed, diag_shift, i, j, accuracy, dense_diagonal and i == j)
-            for j in range(nt) for i in range(nt)]
+    jobs = [(n, nb, d, ell, seed, diag_shift, i, j, accuracy, dense_diagonal and i == j, max_rank)
+            for j in range(nt) for i in range(nt) if i >= j or not lower_only]
     processes = processes or max(1, min(len(jobs), os.cpu_count() or 1))
     if processes == 1:
         return dict(_tile_job(j) for j in jobs)

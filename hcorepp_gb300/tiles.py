@@ -127,6 +127,30 @@ class CompressedTile:
                                              C.byref(p), C.byref(r)), allow=(L.HCGB_OK, L.HCGB_NOT_CONVERGED))
         return t
 
+    @staticmethod
+    def compress_batch(dense, out, params: "CompressionParameters") -> list:
+        """Compress the dense device tiles ``dense`` (float64 tensors of rows x cols values in
+        column-major order) into the compressed tiles ``out`` (same shape, their own capacities) with
+        hcgb_compress_tiles: one batched pipeline launch per chunk, same rule per tile as from_dense.
+        Returns the ranks."""
+        n = len(dense)
+        if n != len(out):
+            raise ValueError("one output tile per dense tile")
+        if n == 0:
+            return []
+        rows, cols = out[0].rows, out[0].cols
+        for d, t in zip(dense, out):
+            if d.dtype != torch.float64 or not d.is_cuda or d.numel() != rows * cols or not d.is_contiguous():
+                raise ValueError("dense tiles: contiguous float64 device tensors of rows x cols values")
+        ptrs = (C.c_void_p * n)(*[d.data_ptr() for d in dense])
+        tiles = (L.Tile * n)(*[t.c_tile() for t in out])
+        ranks = (C.c_int * n)()
+        ctx = run_context()
+        p = params.c()
+        ctx.check(L.lib().hcgb_compress_tiles(ctx.handle, n, ptrs, rows, cols, tiles, C.byref(p), ranks),
+                  allow=(L.HCGB_OK, L.HCGB_NOT_CONVERGED))
+        return list(ranks)
+
     def set_factors(self, u, v):
         """Tile = u v (v: rank x cols); stored as W = v^T on a ``vt`` tile."""
         u = np.asarray(u, dtype=np.float64)
@@ -361,6 +385,8 @@ class TileMatrix:
     ``kinds[i][j]`` is DENSE or COMPRESSED; compressed tiles get capacity ``max_rank``.
     Ranks live in one device int array (``ranks``), so a whole multiply runs without the host.
     ``vt=True`` lays the compressed tiles out for a Cholesky flow (V region = W = V^T).
+    A kind of ``None`` is a tile that is never referenced (the upper triangle of a Cholesky
+    factor): it holds no storage and its descriptor has no data pointer.
     """
 
     def __init__(self, mt: int, nt: int, nb: int, kinds, max_rank: int, device="cuda", vt: bool = False):
@@ -370,7 +396,8 @@ class TileMatrix:
         sizes = []
         for j in range(nt):
             for i in range(mt):
-                sizes.append(nb * nb if self.kinds[i][j] == L.DENSE else 2 * nb * max_rank)
+                kind = self.kinds[i][j]
+                sizes.append(0 if kind is None else nb * nb if kind == L.DENSE else 2 * nb * max_rank)
         self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
         self.arena = torch.zeros(int(self.offsets[-1]), dtype=torch.float64, device=device)
         self.ranks = torch.zeros(mt * nt, dtype=torch.int32, device=device)
@@ -385,6 +412,8 @@ class TileMatrix:
     def tile(self, i, j):
         nb = self.nb
         idx = self.index(i, j)
+        if self.kinds[i][j] is None:
+            raise ValueError(f"tile ({i}, {j}) is not stored")
         if self.kinds[i][j] == L.DENSE:
             return DenseTile(nb, nb, buffer=self._view(i, j))
         return CompressedTile(nb, nb, rank=0, max_rank=self.max_rank, buffer=self._view(i, j),
@@ -408,7 +437,9 @@ class TileMatrix:
             for i in range(self.mt):
                 idx = self.index(i, j)
                 ptr = base + 8 * int(self.offsets[idx])
-                if self.kinds[i][j] == L.DENSE:
+                if self.kinds[i][j] is None:
+                    arr[idx] = L.Tile(None, None, nb, nb, 0, L.DENSE)
+                elif self.kinds[i][j] == L.DENSE:
                     arr[idx] = L.Tile(ptr, None, nb, nb, 0, L.DENSE)
                 else:
                     arr[idx] = L.Tile(ptr, rbase + 4 * idx, nb, nb, self.max_rank,
@@ -438,6 +469,8 @@ class TileMatrix:
         for idx in range(self.mt * self.nt):
             i, j = idx % self.mt, idx // self.mt
             o = int(self.offsets[idx])
+            if self.kinds[i][j] is None:
+                continue
             if self.kinds[i][j] == L.DENSE:
                 parts.append(arena[o:o + nb * nb])
             else:
@@ -463,6 +496,8 @@ class TileMatrix:
             for i in range(self.mt):
                 idx = self.index(i, j)
                 seg = arena[self.offsets[idx]:self.offsets[idx + 1]]
+                if self.kinds[i][j] is None:
+                    continue
                 if self.kinds[i][j] == L.DENSE:
                     blk = seg.reshape((nb, nb), order="F")
                 else:
@@ -485,6 +520,8 @@ class TileMatrix:
                 idx = self.index(i, j)
                 o = int(self.offsets[idx])
                 dst = out[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb]
+                if self.kinds[i][j] is None:
+                    continue
                 if self.kinds[i][j] == L.DENSE:
                     dst.copy_(self.arena[o:o + nb * nb].view(nb, nb).t())
                     continue

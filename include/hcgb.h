@@ -210,6 +210,17 @@ int hcgb_tile_gemm(hcgb_context *ctx, double alpha, const hcgb_tile *a, int op_a
 int hcgb_compress_tile(hcgb_context *ctx, const double *dense, int rows, int cols, hcgb_tile *out,
                        const hcgb_params *params, int *rank);
 
+/* Batched form of hcgb_compress_tile: `count` dense tiles dense[i] (host array of device pointers,
+ * each rows x cols, ld rows) compressed into out[i] (host array of compressed tile descriptors of
+ * that shape) by one batched pipeline launch per chunk of tiles instead of one call per tile (the
+ * reference constructs its input tiles one by one, Compressed.cpp:75-146, TileMatrix.cpp:17-185).
+ * Same arithmetic and rank rule per tile as hcgb_compress_tile.  The chunk is sized so that the
+ * workspace stays within half of the device's free memory.  Synchronous; ranks (host array of
+ * `count`, or NULL) receives the ranks.  Returns HCGB_NOT_CONVERGED if any tile's core did not
+ * converge (the tiles are still written). */
+int hcgb_compress_tiles(hcgb_context *ctx, int count, const double *const *dense, int rows, int cols,
+                        hcgb_tile *out, const hcgb_params *params, int *ranks);
+
 /* ---- Dense per-tile building blocks of a tile Cholesky (device pointers, column-major) ---- */
 typedef enum { HCGB_LOWER = 0, HCGB_UPPER = 1 } hcgb_uplo;
 typedef enum { HCGB_LEFT = 0, HCGB_RIGHT = 1 } hcgb_side;

@@ -172,10 +172,14 @@ class CompressedTile:
         return cls(u, v, max_rank=rank)
 
     @classmethod
-    def from_dense(cls, dense: np.ndarray, params: CompressionParameters) -> "CompressedTile":
-        """Compressed.cpp:75-146: truncated SVD of a dense tile; max_rank = max(min(m,n)/3, 1)."""
+    def from_dense(cls, dense: np.ndarray, params: CompressionParameters,
+                   max_rank: int | None = None) -> "CompressedTile":
+        """Compressed.cpp:75-146: truncated SVD of a dense tile; max_rank = max(min(m,n)/3, 1) (the
+        reference's clamp, Compressed.cpp:83) unless a capacity is given (no counterpart in the
+        reference: the capacity-nb runs of a tile Cholesky)."""
         m, n = dense.shape
-        max_rank = max(min(m, n) // MAX_RANK_RATIO, 1)
+        if max_rank is None:
+            max_rank = max(min(m, n) // MAX_RANK_RATIO, 1)
         min_mn = min(m, n)
         u, s, vt = svd(dense, params.op_type)
         if params.fixed_rank:
