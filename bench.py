@@ -120,6 +120,19 @@ def cpu_measure(w, a, b, c, n_tiles, processes, results=None):
     return updates, wall, sample
 
 
+def port_calibration():
+    """The port's speed against the reference's own compiled CPU path on the same cores and sample,
+    measured where the reference's sources were available (oracle/calibrate_port.py), or None."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle", "port_calibration.json")
+    try:
+        with open(path) as f:
+            cal = json.load(f)
+    except (OSError, ValueError):
+        return None
+    return {k: cal[k] for k in ("machine", "cores", "sample", "port_updates_per_s", "reference_updates_per_s",
+                                "port_over_reference", "final_rank_max_abs_diff") if k in cal}
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return 0
@@ -142,7 +155,8 @@ def reference_arm(args, rank, world):
         "config": {"workload": args.workload, "n": w["n"], "nb": w["nb"], "accuracy": w["accuracy"],
                    "updates_per_multiply": nt ** 3},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                         "sample": f"{n_tiles} seeded C tiles x {nt} k-updates each per step"},
+                         "sample": f"{n_tiles} seeded C tiles x {nt} k-updates each per step",
+                         "calibration": port_calibration()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -622,7 +636,8 @@ def gpu_arm(args, rank, world, local):
         cpu_results = {}
         upd, wall, sample = cpu_measure(wb.w, wb.a_t, wb.b_t, wb.c_t, n_tiles, procs, cpu_results)
         cpu = {"value": upd / wall, "unit": UNIT, "cores": procs, "kind": "port",
-               "sample": f"{n_tiles} seeded C tiles x {nt} k-updates = {upd} updates, {wall:.1f} s wall"}
+               "sample": f"{n_tiles} seeded C tiles x {nt} k-updates = {upd} updates, {wall:.1f} s wall",
+               "calibration": port_calibration()}
         if not args.no_parity and exact is not None:
             parity = parity_block(wb, cpu_results, args, exact)
     exact = None
