@@ -6,6 +6,8 @@ Knobs (all schedule / routing choices; results are the same up to rounding order
   wy_min   reflectors a side needs for the tensor-core WY Q application (plain form; hcgb_set_tuning)
   oz_min   outputs a factor product needs to go to the FP64-accurate tensor-core kernel (hcgb_set_tuning)
   graph    the whole multiply captured once as a CUDA graph and replayed (hcgb_set_graph)
+  precond  core columns from which the plain form's core SVD runs FP32 preconditioning sweeps first
+           (hcgb_set_precond)
 
 `tune()` times candidates on the caller's own multiply by coordinate descent (one knob at a time,
 the others at their current best), restoring C before every trial.  `python -m hcorepp_gb300.autotune`
@@ -21,10 +23,11 @@ import os
 import numpy as np
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_cache.json")
-DEFAULT = {"groups": 8, "wy_min": 48, "oz_min": 2048, "graph": 0}
+DEFAULT = {"groups": 8, "wy_min": 48, "oz_min": 2048, "graph": 0, "precond": 16}
 CANDIDATES = {"groups": [4, 8, 16], "wy_min": [32, 48, 96, 1 << 30], "oz_min": [2048, 4096, 8192],
-              "graph": [0, 1]}
-ORDER = ["groups", "wy_min", "oz_min", "graph"]
+              "graph": [0, 1], "precond": [16, 32, 64, 1 << 30]}
+ORDER = ["groups", "wy_min", "oz_min", "graph", "precond"]
+FORM_KNOBS = {"mixed_ff48": ["groups", "wy_min", "oz_min", "graph"]}  # precond acts on the plain form only
 
 
 def stack_class(mean_k: float) -> int:
@@ -65,7 +68,7 @@ def lookup(key: str, cache: dict | None = None) -> dict:
 
 def store(key: str, config: dict, timings: dict, path: str = CACHE) -> None:
     cache = load(path)
-    cache[key] = {"config": {k: config[k] for k in DEFAULT}, "ms_per_multiply": timings}
+    cache[key] = {"config": {k: config.get(k, DEFAULT[k]) for k in DEFAULT}, "ms_per_multiply": timings}
     with open(path, "w") as f:
         json.dump(cache, f, indent=1, sort_keys=True)
         f.write("\n")
@@ -75,11 +78,13 @@ def apply(ctx, config: dict) -> None:
     ctx.set_concurrency(int(config["groups"]))
     ctx.set_tuning(int(config["oz_min"]), int(config["wy_min"]))
     ctx.set_graph(bool(config["graph"]))
+    ctx.set_precond(int(config["precond"]))
 
 
-def tune(run_multiply, ctx, steps: int = 2, warmup: int = 1, start: dict | None = None):
-    """Coordinate descent over CANDIDATES.  run_multiply() restores C and runs one multiply on the
-    context's stream.  Returns (best config, {config label: ms per multiply})."""
+def tune(run_multiply, ctx, steps: int = 2, warmup: int = 1, start: dict | None = None, knobs=None):
+    """Coordinate descent over CANDIDATES (the knobs in `knobs`, default all).  run_multiply() restores C
+    and runs one multiply on the context's stream.  Returns (best config, {config label: ms per
+    multiply})."""
     import torch
     best = dict(start or DEFAULT)
     seen = {}
@@ -102,7 +107,7 @@ def tune(run_multiply, ctx, steps: int = 2, warmup: int = 1, start: dict | None 
         return seen[label]
 
     best_ms = time_cfg(best)
-    for knob in ORDER:
+    for knob in (knobs or ORDER):
         for v in CANDIDATES[knob]:
             cfg = dict(best)
             cfg[knob] = v
@@ -161,7 +166,7 @@ def main():
             C.ranks.copy_(C0.ranks)
             T.tlr_gemm(1.0, A, A, 1.0, C, params)
 
-        best, seen = tune(run, ctx, steps=args.steps)
+        best, seen = tune(run, ctx, steps=args.steps, knobs=FORM_KNOBS.get(form))
         key = cache_key(nb, mean_k, form)
         store(key, best, seen, args.cache)
         print(json.dumps({"key": key, "best": best, "ms": seen}), flush=True)

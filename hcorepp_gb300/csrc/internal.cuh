@@ -175,7 +175,11 @@ struct Params {
     int oz;          // 1: large factor products on the 16-bit tensor cores (FP64-accurate splitting)
     int oz_min;      // outputs a product needs to go to the tensor cores (OZ_MIN_OUTPUTS by default)
     int wy_min;      // reflectors a side needs for the WY Q application (WY_MIN_REFLECTORS by default)
+    int precond_min; // plain form: Jacobi columns a core needs for the FP32 preconditioning sweeps
 };
+
+// Default of Params::precond_min.
+constexpr int PRECOND_MIN_COLS = 16;
 
 // ---- launchers (stream-ordered, asynchronous) ----
 void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p, GemmJob *jobs,

@@ -139,6 +139,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     prm.oz = 1;
     prm.oz_min = OZ_MIN_OUTPUTS;
     prm.wy_min = WY_MIN_REFLECTORS;
+    prm.precond_min = PRECOND_MIN_COLS;
 
     // GEMM grid bounds from the tile kinds and capacities (ranks are read on the device).
     int pm[3] = {0, 0, 0}, pn[3] = {0, 0, 0};

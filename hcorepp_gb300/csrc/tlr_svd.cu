@@ -24,8 +24,6 @@ namespace hcgb {
 namespace {
 
 constexpr int SVD_THREADS = 512;
-// Plain form: cores with at least this many Jacobi columns get the FP32 preconditioning sweeps.
-constexpr int PRECOND_MIN_COLS = 16;
 constexpr float PRECOND_TOL32 = 1e-6f;
 constexpr int PRECOND_MAX_SWEEPS = 12;
 constexpr int SVD_RED_DOUBLES = 64, SVD_REDI_INTS = 128;  // reduction area (up to 32 warps)
@@ -962,13 +960,16 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
         }
         tm.sync();
     } else {
-        // X32 (kV x rk floats) and J (rk x rk float-float) in the float region of the slot
+        // X32 (kV x rk floats) and J (rk x rk float-float): in shared memory behind X when they fit
+        // the team's pool, else in the float region of the slot.
         const size_t x32_floats = ((size_t) kV * rk + 1) & ~size_t(1);
-        const bool fits = x32_floats + 2 * (size_t) rk * rk <= (size_t) ws.kmax * (ws.kmax + ws.ld);
-        if (rk >= PRECOND_MIN_COLS && fits) {
+        const size_t pre_doubles = x32_floats / 2 + (size_t) rk * rk;
+        const bool in_smem = Mw == pool && (size_t) kV * rk + pre_doubles <= (size_t) pool_doubles;
+        const bool fits = in_smem || x32_floats + 2 * (size_t) rk * rk <= (size_t) ws.kmax * (ws.kmax + ws.ld);
+        if (rk >= p.precond_min && fits) {
             // FP32 sweeps with accumulated rotations (FP32 pipe), then X <- X J in FP64: the FP64
             // sweeps below start from a nearly orthogonal X and need about half as many.
-            float *X32 = reinterpret_cast<float *>(base + ws.off_mixed);
+            float *X32 = reinterpret_cast<float *>(in_smem ? pool + (size_t) kV * rk : base + ws.off_mixed);
             df *J32 = reinterpret_cast<df *>(X32 + x32_floats);
             if (tm.tid == 0) s_emax = 0;
             tm.sync();

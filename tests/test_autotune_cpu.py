@@ -19,7 +19,7 @@ def test_classes_and_keys():
 def test_lookup_falls_back_and_round_trips(tmp_path):
     path = str(tmp_path / "cache.json")
     assert A.lookup("nb512-k64-plain_fp64", A.load(path)) == A.DEFAULT
-    cfg = {"groups": 16, "wy_min": 96, "oz_min": 4096, "graph": 1}
+    cfg = {"groups": 16, "wy_min": 96, "oz_min": 4096, "graph": 1, "precond": 32}
     A.store("nb512-k64-plain_fp64", cfg, {"groups=16": 800.0}, path)
     A.store("nb1024-k128-mixed_ff48", A.DEFAULT, {}, path)
     cache = A.load(path)
@@ -31,7 +31,7 @@ def test_lookup_falls_back_and_round_trips(tmp_path):
 def test_committed_cache_is_well_formed():
     for key, ent in A.load().items():
         assert key.startswith("nb") and "-k" in key
-        assert set(ent["config"]) == set(A.DEFAULT)
+        assert set(ent["config"]) <= set(A.DEFAULT)  # knobs added later fall back to their defaults
         for knob, v in ent["config"].items():
             assert v in A.CANDIDATES[knob]
 
@@ -50,10 +50,14 @@ def test_coordinate_descent_picks_the_fastest(monkeypatch):
         def set_graph(self, on):
             applied.append(("graph", on))
 
+        def set_precond(self, m):
+            applied.append(("precond", m))
+
     state = {}
 
     def cost(cfg):
-        return abs(cfg["groups"] - 16) + abs(cfg["wy_min"] - 96) / 10 + (cfg["oz_min"] != 4096) + (1 - cfg["graph"])
+        return (abs(cfg["groups"] - 16) + abs(cfg["wy_min"] - 96) / 10 + (cfg["oz_min"] != 4096) + (1 - cfg["graph"])
+                + (cfg["precond"] != 64))
 
     real_apply = A.apply
 
@@ -75,5 +79,5 @@ def test_coordinate_descent_picks_the_fastest(monkeypatch):
     monkeypatch.setitem(sys.modules, "torch", fake_torch)
     monkeypatch.setattr(A, "apply", fake_apply)
     best, seen = A.tune(lambda: None, Ctx(), steps=1, warmup=0)
-    assert best == {"groups": 16, "wy_min": 96, "oz_min": 4096, "graph": 1}
+    assert best == {"groups": 16, "wy_min": 96, "oz_min": 4096, "graph": 1, "precond": 64}
     assert len(seen) <= 1 + sum(len(v) for v in A.CANDIDATES.values())

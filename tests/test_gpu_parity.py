@@ -430,3 +430,47 @@ def test_tensor_core_products_fp64_accurate(T, scaled):
     for oz, got in out.items():
         err = np.abs(got.astype(np.longdouble) - exact) / (bound + np.abs(0.25 * c))
         assert float(err.max()) < 2e-14, (oz, float(err.max()))
+
+
+@pytest.mark.parametrize("precond", [1 << 30, 16, 2])
+def test_plain_core_preconditioning_changes_rounding_only(T, precond):
+    """hcgb_set_precond: with the plain form's FP32 preconditioning sweeps off, from 16 core columns
+    (the default) or on every core of 2 columns and more, the multiply has the same ranks and the
+    same product to rounding (the accumulated rotations are orthogonal to ~1e-13), and each is
+    within the oracle's accuracy bound."""
+    import torch
+    from hcorepp_gb300 import _lib as L
+    from hcorepp_gb300.problems import KernelMatrix
+    nt, nb, acc = 4, 256, 1e-8
+    km = KernelMatrix(nt * nb, nb, 2, 0.1, 1)
+    kc = KernelMatrix(nt * nb, nb, 2, 0.1, 2)
+    kinds = [[L.COMPRESSED] * nt for _ in range(nt)]
+    oa = [[compressed_from_dense(km.tile(i, j), acc) for j in range(nt)] for i in range(nt)]
+    oc = [[compressed_from_dense(kc.tile(i, j), acc) for j in range(nt)] for i in range(nt)]
+    A = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+    C0 = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+    for i in range(nt):
+        for j in range(nt):
+            A.set_tile(i, j, u=oa[i][j].u, v=oa[i][j].v)
+            C0.set_tile(i, j, u=oc[i][j].u, v=oc[i][j].v)
+    exact = (np.block([[t.to_dense() for t in r] for r in oa]) @ np.block([[t.to_dense() for t in r] for r in oa])
+             + np.block([[t.to_dense() for t in r] for r in oc]))
+    ctx = T.run_context()
+    params = T.CompressionParameters(acc, truncated_svd=True, mode=L.PLAIN_FP64)
+    outs = {}
+    try:
+        for setting in (1 << 30, precond):
+            ctx.set_precond(setting)
+            C = T.TileMatrix(nt, nt, nb, kinds, nb // 3)
+            C.arena.copy_(C0.arena)
+            C.ranks.copy_(C0.ranks)
+            T.tlr_gemm(1.0, A, A, 1.0, C, params)
+            torch.cuda.synchronize()
+            outs[setting] = (C.rank_grid(), C.to_dense())
+    finally:
+        ctx.set_precond(0)
+    np.testing.assert_array_equal(outs[precond][0], outs[1 << 30][0])
+    assert rel_fro(outs[precond][1], outs[1 << 30][1]) <= 1e-12
+    O.tile_matrix_multiply(oa, oa, oc, 1.0, 1.0, O.CompressionParameters(acc, truncated_svd=True))
+    e_o = rel_fro(np.block([[t.to_dense() for t in r] for r in oc]), exact)
+    assert rel_fro(outs[precond][1], exact) <= 2 * max(e_o, acc)
