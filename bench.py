@@ -83,6 +83,8 @@ def parse():
     ap.add_argument("--lowp", default="1e-4,1e-6,1e-8",
                     help="accuracies of the TF32 / BF16 low-precision sweep ('' to skip)")
     ap.add_argument("--lowp-steps", type=int, default=2, help="timed steps per low-precision run")
+    ap.add_argument("--config4", action="store_true",
+                    help="also run the n = 32768, nb = 1024 multiply in every form (hcorepp_gb300/learned_bench.py)")
     ap.add_argument("--no-tuning", action="store_true",
                     help="default launch shapes instead of the autotuner's cache (hcorepp_gb300/tuning_cache.json)")
     return ap.parse_args()
@@ -483,6 +485,26 @@ def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, step
     return out
 
 
+def core_cycle_classes(info_h):
+    """Where the core's SM cycles go: per class of core width (columns the Jacobi rotates), the
+    updates, their summed core kcycles and the mean kcycles of each core phase."""
+    comp = info_h[:, 4] > 0
+    cols = info_h[:, 8]
+    out = {}
+    lo = 0
+    for hi in (16, 32, 64, 128, 256, 1 << 30):
+        sel = comp & (cols > lo) & (cols <= hi)
+        if sel.any():
+            kc = info_h[sel, 9:13].astype(np.float64)
+            out[f"{lo + 1}-{hi if hi < (1 << 30) else 'max'}"] = {
+                "updates": int(sel.sum()), "kcycles_sum": float(kc.sum()),
+                "mean_kcycles": {nm: float(kc[:, q].mean()) for q, nm in
+                                 enumerate(["product", "qrcp", "jacobi", "factors"])},
+                "mean_sweeps": float(info_h[sel, 6].mean())}
+        lo = hi
+    return out
+
+
 def roofline_of(wb, res, form, dmma_peak, dfma_peak, args):
     stages = res["stages"]
     info_h = res["info"]
@@ -708,6 +730,7 @@ def gpu_arm(args, rank, world, local):
                   "mean_core_cols": float(info_h[info_h[:, 4] > 0, 8].mean())},
         "core_kcycles_mean": {nm: float(info_h[info_h[:, 4] > 0, 9 + q].mean())
                               for q, nm in enumerate(["product", "qrcp", "jacobi", "factors"])},
+        "core_kcycles_by_core_cols": core_cycle_classes(info_h),
         "check": {"rel_fro_err_vs_fp64_dense_product": head.get("rel_fro_err_vs_fp64_dense_product")},
         "parity": parity,
         "forms": form_blocks,
@@ -719,6 +742,11 @@ def gpu_arm(args, rank, world, local):
         "cpu_baseline": cpu,
         "clocks": head["clocks"],
     }
+    if args.config4:
+        from hcorepp_gb300 import learned_bench
+        del wb
+        torch.cuda.empty_cache()
+        line["config4"] = learned_bench.run(steps=1, warmup=1)
     print(json.dumps(line), flush=True)
     return 0
 

@@ -4,8 +4,8 @@
 
 Matrix: n points uniform in [0,1]^3 (seeded), Morton-sorted; a_ij = exp(-|x_i - x_j| / 0.2) with
 1e-2 added to the diagonal (SPD).  Diagonal tiles dense, tiles below the diagonal compressed on the
-GPU at 1e-8 relative accuracy with the reference's capacity nb/3 (one hcgb_compress_tiles batch per
-tile column), in the Cholesky-flow layout (tile = U W^T); tiles above the diagonal are not stored.
+GPU at 1e-8 relative accuracy with the reference's capacity nb/3 (hcgb_compress_tiles over groups
+of tile columns), in the Cholesky-flow layout (tile = U W^T); tiles above the diagonal are not stored.
 One step = one factorization A = L L^T (nt potrf, nt(nt-1)/2 panel solves, nt(nt^2-1)/6 trailing
 Syrk/Gemm updates), restarted from the same tiles every step.
 
@@ -72,18 +72,30 @@ def kernel_tile_device(km: KernelMatrix, pts: torch.Tensor, i: int, j: int) -> t
     return blk
 
 
-def build_matrix(km: KernelMatrix, acc: float, cap: int) -> T.TileMatrix:
+def build_matrix(km: KernelMatrix, acc: float, cap: int, batch_bytes: float = 16e9) -> T.TileMatrix:
     """Dense diagonal tiles; the tiles below the diagonal generated on the GPU and compressed straight
-    into the arena (compressed_vt), one hcgb_compress_tiles batch per tile column."""
+    into the arena (compressed_vt) by hcgb_compress_tiles, whole tile columns per call up to
+    `batch_bytes` of dense input (the call itself splits its launches to fit the free memory)."""
     nt, nb = km.nt, km.nb
     tm = T.TileMatrix(nt, nt, nb, cholesky_kinds(nt), cap, vt=True)
     params = T.CompressionParameters(acc, truncated_svd=True)
     pts = torch.from_numpy(km.points).cuda()
+    pending, dense = [], []
+
+    def flush():
+        if pending:
+            T.CompressedTile.compress_batch(dense, [tm.tile(i, j) for (i, j) in pending], params)
+            pending.clear()
+            dense.clear()
+
     for j in range(nt):
         tm.tile(j, j).buffer.copy_(kernel_tile_device(km, pts, j, j).t().reshape(-1))
-        dense = [kernel_tile_device(km, pts, i, j).t().contiguous().view(-1) for i in range(j + 1, nt)]
-        T.CompressedTile.compress_batch(dense, [tm.tile(i, j) for i in range(j + 1, nt)], params)
-        del dense
+        for i in range(j + 1, nt):
+            pending.append((i, j))
+            dense.append(kernel_tile_device(km, pts, i, j).t().contiguous().view(-1))
+        if len(dense) * nb * nb * 8 >= batch_bytes:
+            flush()
+    flush()
     torch.cuda.synchronize()
     return tm
 
