@@ -1236,7 +1236,7 @@ extern "C" int hcgb_tile_cholesky(hcgb_context *ctx, int nt, const hcgb_tile *gr
                 DevTile db = to_dev(tb);
                 std::swap(db.data, db.v);
                 std::swap(db.rows, db.cols);
-                dv.push_back(DevUpdate{to_dev(ta), db, to_dev(tc), uid++});
+                dv.push_back(DevUpdate{to_dev(ta), db, to_dev(tc), uid++, i - j});
             }
         const int chunk = updates_per_launch(ctx, shape_of(hu.data(), (int) hu.size()), p.mode, max_chunk);
         for (size_t off = 0; off < dv.size(); off += chunk) {

@@ -117,6 +117,26 @@ def feature_sink(feats: torch.Tensor | None, ctx: L.Context | None = None):
     ctx.check(L.lib().hcgb_set_feature_sink(ctx.handle, C.c_void_p(feats.data_ptr() if feats is not None else 0)))
 
 
+def harvest_cholesky(a: "T.TileMatrix", params: "T.CompressionParameters", ctx: L.Context | None = None):
+    """One tile Cholesky (hcgb_tile_cholesky) of the Cholesky-flow tile matrix `a` in the context's
+    current form with the features and records of every trailing update kept: returns (features
+    (n, 12) float32, records (n, fields) int32) on the device, n = nt (nt^2 - 1) / 6."""
+    ctx = ctx or T.run_context()
+    nt = a.mt
+    n = max(nt * (nt * nt - 1) // 6, 1)
+    feats = torch.zeros((n, FEATURES), dtype=torch.float32, device="cuda")
+    info = T.info_buffer(n)
+    feature_sink(feats, ctx)
+    try:
+        res = T.tile_cholesky(a, params, batched=True, info=info)
+        torch.cuda.synchronize()
+    finally:
+        feature_sink(None, ctx)
+    if res != 0:
+        raise RuntimeError(f"tile Cholesky stopped: not positive definite at {res}")
+    return feats, info
+
+
 def harvest_multiply(a: "T.TileMatrix", b: "T.TileMatrix", c: "T.TileMatrix", params: "T.CompressionParameters",
                      ctx: L.Context | None = None):
     """One multiply C <- A B + C in the context's current form with the features and records of

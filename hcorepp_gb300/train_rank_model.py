@@ -2,13 +2,19 @@
 
     python -m hcorepp_gb300.train_rank_model [--out hcorepp_gb300/rank_model_weights.npy]
 
-Training data: (features, new rank) of every recompression in plain FP64 multiplies C <- A B + C of
-Morton-sorted exponential-kernel matrices (2-D points, length scale 0.1, dense diagonal tiles,
-inputs compressed at 1e-8 relative) -- the 32 x 32-tile layout at n = 8192 (16 x 16 tiles of 512)
-and the 4 x 4-tile one (n = 2048, nb = 512, every tile compressed) -- over seeds that the benchmark
-does not use (the benchmark's inputs are seeds 1 and 2), at accuracies 1e-8, 1e-6 and 1e-4.  The
-features are recorded on the device by the pipeline itself (hcgb_set_feature_sink), the targets
-come from the per-update records; training runs the library's own forward / backward / Adam kernels.
+Training data: (features, new rank) of every recompression in plain FP64 runs over seeds that the
+benchmarks do not use (their inputs are seeds 1 and 2), in three families:
+  multiply, nb = 512   C <- A B + C of Morton-sorted exponential-kernel matrices (2-D points, length
+                       scale 0.1, inputs compressed at 1e-8 relative): n = 8192 (16 x 16 tiles, dense
+                       diagonal) and n = 2048 (4 x 4 tiles, every tile compressed), accuracies 1e-8,
+                       1e-6, 1e-4
+  multiply, nb = 1024  the same family at n = 8192 (8 x 8 tiles, dense diagonal)
+  Cholesky, nb = 1024  the trailing updates of a tile Cholesky of the 3-D kernel matrix (length scale
+                       0.2, +1e-2 on the diagonal) at n = 16384 (16 x 16 tiles), accuracy 1e-8
+The two smaller families are replicated so that each carries about a fifth of the training pairs.  The
+features are recorded on the device by the pipeline itself (hcgb_set_feature_sink), the targets come
+from the per-update records; training runs the library's own forward / backward / Adam kernels.  The
+last seed of every family is held out for the report.
 """
 from __future__ import annotations
 
@@ -65,6 +71,44 @@ def harvest(seeds, accuracies, sizes):
     return torch.cat(feats), torch.cat(infos), torch.cat(tags)
 
 
+def harvest_cholesky(seeds, n=16384, nb=1024, acc=1e-8):
+    import torch
+    from hcorepp_gb300 import rank_model as RM
+    from hcorepp_gb300 import tiles as T
+    from hcorepp_gb300.cholesky_bench import build_matrix
+    from hcorepp_gb300.problems import KernelMatrix
+    feats, infos, tags = [], [], []
+    ctx = T.run_context()
+    RM.learned_off(ctx)
+    for s in seeds:
+        km = KernelMatrix(n, nb, 3, 0.2, s, diag_shift=1e-2)
+        tm = build_matrix(km, acc, max(nb // 3, 1))
+        f, i = RM.harvest_cholesky(tm, T.CompressionParameters(acc, truncated_svd=True))
+        feats.append(f)
+        infos.append(i)
+        tags.append(torch.full((f.shape[0],), s, dtype=torch.int32, device=f.device))
+        del tm
+        torch.cuda.empty_cache()
+    return torch.cat(feats), torch.cat(infos), torch.cat(tags)
+
+
+def held_out_report(m, feats, info):
+    import numpy as np
+    hold = info.cpu().numpy()
+    keep = (hold[:, 4] > 0) & ((hold[:, 0] == 0) | (hold[:, 0] == 5))
+    pred = m.predict(feats).cpu().numpy()[keep]
+    true = np.log2(1.0 + hold[keep, 5])
+    ra, rb, rc = hold[keep, 1], hold[keep, 2], hold[keep, 3]
+    add = np.where((ra > 0) & (rb > 0), np.minimum(ra, rb), np.maximum(ra, rb))
+    rule = np.log2(1.0 + np.maximum(rc, add))
+    return {"held_out_pairs": int(keep.sum()),
+            "held_out_mean_abs_log2rank_error": {"network": float(np.abs(pred - true).mean()),
+                                                 "input_rank_rule": float(np.abs(rule - true).mean())},
+            "held_out_rank_within_8": {"network": float(np.mean(np.abs(np.exp2(pred) - np.exp2(true)) <= 8)),
+                                       "input_rank_rule": float(np.mean(np.abs(np.exp2(rule) - np.exp2(true)) <= 8))},
+            "held_out_underpredicted_by_more_than_8": float(np.mean(np.exp2(true) - np.exp2(pred) > 8))}
+
+
 def main():
     import torch
     from hcorepp_gb300 import rank_model as RM
@@ -81,29 +125,27 @@ def main():
     accs = [float(a) for a in args.accuracies.split(",")]
     t0 = time.time()
     sizes = [(8192, 512, True), (2048, 512, False)]
-    feats, info, tag = harvest(seeds, accs, sizes)
+    fam = {"multiply_nb512": harvest(seeds, accs, sizes),
+           "multiply_nb1024": harvest(seeds[:3] + seeds[-1:], accs, [(8192, 1024, True)]),
+           "cholesky_nb1024": harvest_cholesky(seeds[:3] + seeds[-1:])}
     t1 = time.time()
-    # the last seed's pairs are held out for the report
-    n = feats.shape[0]
-    held = tag == seeds[-1]
-    train = ~held
+    # the last seed's pairs of every family are held out for the report; the smaller families are
+    # replicated to about a quarter of the largest one's training pairs each
+    big = int((fam["multiply_nb512"][2] != seeds[-1]).sum())
+    tr_f, tr_i = [], []
+    for name, (f, i, tag) in fam.items():
+        train = tag != seeds[-1]
+        reps = max(1, round(big / 4 / max(int(train.sum()), 1))) if name != "multiply_nb512" else 1
+        tr_f.append(f[train].repeat(reps, 1))
+        tr_i.append(i[train].repeat(reps, 1))
     m = RM.RankModel(seed=1)
-    loss, used = m.train(feats[train], info[train], epochs=args.epochs, batch=args.batch, lr=args.lr)
+    loss, used = m.train(torch.cat(tr_f), torch.cat(tr_i), epochs=args.epochs, batch=args.batch, lr=args.lr)
     t2 = time.time()
     m.save(args.out)
-    hold = info[held].cpu().numpy()
-    keep = (hold[:, 4] > 0) & ((hold[:, 0] == 0) | (hold[:, 0] == 5))
-    pred = m.predict(feats[held]).cpu().numpy()[keep]
-    true = np.log2(1.0 + hold[keep, 5])
-    ra, rb, rc = hold[keep, 1], hold[keep, 2], hold[keep, 3]
-    add = np.where((ra > 0) & (rb > 0), np.minimum(ra, rb), np.maximum(ra, rb))
-    rule = np.log2(1.0 + np.maximum(rc, add))
-    summary = {"pairs_harvested": int(n), "pairs_trained": int(used), "final_train_mse_log2rank": loss,
-               "held_out_pairs": int(keep.sum()),
-               "held_out_mean_abs_log2rank_error": {"network": float(np.abs(pred - true).mean()),
-                                                    "input_rank_rule": float(np.abs(rule - true).mean())},
-               "held_out_rank_within_8": {"network": float(np.mean(np.abs(np.exp2(pred) - np.exp2(true)) <= 8)),
-                                          "input_rank_rule": float(np.mean(np.abs(np.exp2(rule) - np.exp2(true)) <= 8))},
+    summary = {"pairs_harvested": {k: int(v[0].shape[0]) for k, v in fam.items()}, "pairs_trained": int(used),
+               "final_train_mse_log2rank": loss,
+               "held_out": {k: held_out_report(m, f[tag == seeds[-1]], i[tag == seeds[-1]])
+                            for k, (f, i, tag) in fam.items()},
                "seconds": {"harvest": t1 - t0, "train": t2 - t1}, "seeds": seeds, "accuracies": accs,
                "sizes": [list(s) for s in sizes]}
     print(json.dumps(summary), flush=True)
