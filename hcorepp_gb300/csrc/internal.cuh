@@ -178,8 +178,10 @@ struct Params {
     int precond_min; // plain form: Jacobi columns a core needs for the FP32 preconditioning sweeps
 };
 
-// Default of Params::precond_min.
-constexpr int PRECOND_MIN_COLS = 16;
+// Default of Params::precond_min: off.  Measured on the 32 x 32-tile nb = 512 multiply, the FP32
+// preconditioning sweeps cut the FP64 sweeps from ~4.7 to ~3 but cost more than they save
+// (918-925 ms per multiply from 16, 32 or 64 core columns on, 844 ms off).
+constexpr int PRECOND_MIN_COLS = 1 << 30;
 
 // ---- launchers (stream-ordered, asynchronous) ----
 void launch_plan(const DevUpdate *ups, int n, double alpha, double beta, Workspace ws, Params p, GemmJob *jobs,

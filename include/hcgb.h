@@ -185,8 +185,7 @@ int hcgb_set_tuning(hcgb_context *ctx, int oz_min_outputs, int wy_min_reflectors
 /* Plain form: a core SVD with at least min_cols Jacobi columns first runs one-sided Jacobi sweeps in
  * FP32 with the rotations accumulated in float-float (J orthogonal to ~1e-13), then X <- X J in FP64
  * and FP64 sweeps to working precision; smaller cores run FP64 sweeps only.  min_cols = 0 restores
- * the default (16); a value above every core width turns the preconditioning off.  Same results up to
- * rounding. */
+ * the default (off: a value above every core width); same results up to rounding. */
 int hcgb_set_precond(hcgb_context *ctx, int min_cols);
 
 /* Factor products of k >= 16 with at least 2048 outputs run on the 16-bit tensor cores by

@@ -434,8 +434,8 @@ def test_tensor_core_products_fp64_accurate(T, scaled):
 
 @pytest.mark.parametrize("precond", [1 << 30, 16, 2])
 def test_plain_core_preconditioning_changes_rounding_only(T, precond):
-    """hcgb_set_precond: with the plain form's FP32 preconditioning sweeps off, from 16 core columns
-    (the default) or on every core of 2 columns and more, the multiply has the same ranks and the
+    """hcgb_set_precond: with the plain form's FP32 preconditioning sweeps off (the default), from 16
+    core columns or on every core of 2 columns and more, the multiply has the same ranks and the
     same product to rounding (the accumulated rotations are orthogonal to ~1e-13), and each is
     within the oracle's accuracy bound."""
     import torch
