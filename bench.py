@@ -81,7 +81,7 @@ def parse():
     ap.add_argument("--k-order", type=int, default=1, choices=[0, 1],
                     help="0: ascending k per C tile (reference order); 1: costliest updates first")
     ap.add_argument("--lowp", default="1e-4,1e-6,1e-8",
-                    help="accuracies of the TF32 / BF16 low-precision sweep ('' to skip)")
+                    help="accuracies of the TF32 / BF16 low-precision sweep ('' or none to skip)")
     ap.add_argument("--lowp-steps", type=int, default=2, help="timed steps per low-precision run")
     ap.add_argument("--config4", action="store_true",
                     help="also run the n = 32768, nb = 1024 multiply in every form (hcorepp_gb300/learned_bench.py)")
@@ -613,7 +613,7 @@ def gpu_arm(args, rank, world, local):
     # truncation test in FP64) at several accuracies, each beside the plain FP64 form at the same
     # accuracy: throughput, error against the FP64 dense product, rank growth.
     lowp = {}
-    for acc_s in [a for a in args.lowp.split(",") if a]:
+    for acc_s in [a for a in args.lowp.split(",") if a and a != "none"]:
         acc = float(acc_s)
         runs = {}
         for name, mode in (("plain_fp64", L.PLAIN_FP64), ("tf32", L.TF32), ("bf16", L.BF16)):
