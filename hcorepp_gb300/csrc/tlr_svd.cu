@@ -382,8 +382,12 @@ __device__ void jacobi_dispatch(const TM &tm, double *X, int ldx, int rows, int 
                                 double *s_amax, int *sweeps, bool *conv, double tol, int max_sweeps, double *dsc,
                                 int dstride) {
     // Fewer lanes per pair put more pairs in one warp instruction, so the per-pair scalar work
-    // (tangent, tests, norm updates) is shared by 2-4 pairs; RPL rows per lane stay in registers.
+    // (tangent, tests, norm updates), which runs as full-width FP64 warp instructions on a pipe that
+    // issues one of them per ~19 cycles per SM, is shared by 4-8 pairs; RPL rows per lane stay in
+    // registers.  (Two lanes per pair for columns of up to 32 rows, one warp taking every pair of a
+    // step, measured slower: 760 vs 673 kcycles per 17-32-column core.)
     if (rows <= 32) jacobi<4, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 64 && MAXRPL >= 16) jacobi<4, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 64) jacobi<8, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 128 && MAXRPL >= 16) jacobi<8, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 128) jacobi<16, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
@@ -464,6 +468,48 @@ __device__ int jacobi_precond32(const TM &tm, float *X, int rows, int ncols, df 
         if (done) break;
     }
     return sweeps;
+}
+
+// One step of qrcp_truncated after the reflector of column s is formed (x = column s, v = [1; x[s+1:]],
+// tau): H = I - tau v v^T applied to columns s+1 .. ncols-1 by groups of G lanes (32 / G columns per
+// warp at a time), the squared norms below row s downdated and recomputed exactly when the downdate
+// loses four or more digits (LAPACK dlaqp2's guard).
+template <int G, class TM>
+__device__ __forceinline__ void qrcp_apply(const TM &tm, double *A, int lda, int mrows, int ncols, int s,
+                                           const double *x, double tau, double *nrm, double *nref) {
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
+    constexpr int CPW = 32 / G;
+    const int gl = lane % G, grp = lane / G;
+    for (int j0 = s + 1 + warp * CPW; j0 < ncols; j0 += nw * CPW) {
+        const int j = j0 + grp;
+        const bool act = j < ncols;
+        double *y = A + (size_t) (act ? j : s) * lda;  // idle groups read column s and write nothing
+        double w = 0.0;
+        if (tau != 0.0) {
+            w = gl == 0 ? y[s] : 0.0;
+            for (int i = s + 1 + gl; i < mrows; i += G) w = fma(x[i], y[i], w);
+            w = group_sum(w, G) * tau;
+            if (act)
+                for (int i = s + 1 + gl; i < mrows; i += G) y[i] = fma(-w, x[i], y[i]);
+        }
+        const double ys = y[s] - w;  // every lane of the group reads the old y[s] before lane 0 writes it
+        __syncwarp();
+        if (act && gl == 0) y[s] = ys;
+        double nn = act ? nrm[j] - ys * ys : 0.0;
+        const bool exact = act && !(nn > 1e-8 * nref[j]);
+        if (__any_sync(0xffffffffu, exact)) {
+            double e = 0.0;
+            if (exact)
+                for (int i = s + 1 + gl; i < mrows; i += G) e = fma(y[i], y[i], e);
+            e = group_sum(e, G);
+            if (exact) nn = e;
+        }
+        __syncwarp();
+        if (act && gl == 0) {
+            nrm[j] = nn;
+            if (exact) nref[j] = nn;
+        }
+    }
 }
 
 // Householder QR with column pivoting of A (mrows x ncols, ld lda) in place, stopped early once
@@ -578,31 +624,12 @@ __device__ int qrcp_truncated(const TM &tm, double *A, int lda, int mrows, int n
         tm.sync();
         // Apply H to the remaining columns; downdate their squared norms below row s
         // (nrm -= y_s^2) and recompute exactly when the downdate cancels (LAPACK dlaqp2's guard).
-        for (int j = s + 1 + warp; j < ncols; j += nw) {
-            double *y = A + (size_t) j * lda;
-            double w = 0.0;
-            if (tau != 0.0) {
-                w = lane == 0 ? y[s] : 0.0;
-                for (int i = s + 1 + lane; i < mrows; i += 32) w = fma(x[i], y[i], w);
-                w = warp_sum(w) * tau;
-                for (int i = s + 1 + lane; i < mrows; i += 32) y[i] = fma(-w, x[i], y[i]);
-            }
-            const double ys = y[s] - w;  // all lanes read the old y[s] before lane 0 writes it
-            __syncwarp();
-            if (lane == 0) y[s] = ys;
-            double nn = nrm[j] - ys * ys;
-            const bool exact = !(nn > 1e-8 * nref[j]);  // lost 4+ digits of the norm since the last exact value
-            if (exact) {
-                nn = 0.0;
-                for (int i = s + 1 + lane; i < mrows; i += 32) nn = fma(y[i], y[i], nn);
-                nn = warp_sum(nn);
-            }
-            __syncwarp();
-            if (lane == 0) {
-                nrm[j] = nn;
-                if (exact) nref[j] = nn;
-            }
-        }
+        // Columns of up to 32, 64 or 128 rows are handled by groups of 4, 8 or 16 lanes, several
+        // columns per warp instruction, so the reductions and the per-column scalar work are shared.
+        if (mrows <= 32) qrcp_apply<4>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
+        else if (mrows <= 64) qrcp_apply<8>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
+        else if (mrows <= 128) qrcp_apply<16>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
+        else qrcp_apply<32>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
         tm.sync();
     }
     return rkeep;
