@@ -83,8 +83,9 @@ def parse():
     ap.add_argument("--lowp", default="1e-4,1e-6,1e-8",
                     help="accuracies of the TF32 / BF16 low-precision sweep ('' or none to skip)")
     ap.add_argument("--lowp-steps", type=int, default=2, help="timed steps per low-precision run")
-    ap.add_argument("--config4", action="store_true",
-                    help="also run the n = 32768, nb = 1024 multiply in every form (hcorepp_gb300/learned_bench.py)")
+    ap.add_argument("--no-config4", action="store_true",
+                    help="skip the n = 32768, nb = 1024 multiply (plain, float-float and learned forms; "
+                         "hcorepp_gb300/learned_bench.py)")
     ap.add_argument("--no-tuning", action="store_true",
                     help="default launch shapes instead of the autotuner's cache (hcorepp_gb300/tuning_cache.json)")
     return ap.parse_args()
@@ -742,11 +743,12 @@ def gpu_arm(args, rank, world, local):
         "cpu_baseline": cpu,
         "clocks": head["clocks"],
     }
-    if args.config4:
+    if not args.no_config4 and world == 1:
         from hcorepp_gb300 import learned_bench
         del wb
         torch.cuda.empty_cache()
-        line["config4"] = learned_bench.run(steps=1, warmup=1)
+        c4_forms = ["plain_fp64", "mixed_ff48"] + (["learned_ff48"] if os.path.exists(RM.WEIGHTS) else [])
+        line["config4"] = learned_bench.run(steps=1, warmup=1, forms=c4_forms)
     print(json.dumps(line), flush=True)
     return 0
 
