@@ -673,6 +673,7 @@ def gpu_arm(args, rank, world, local):
                "speedup_over_plain_fp64": res["value"] / head["value"],
                "gpu_launches_per_step": res["gpu_launches_per_step"], "clocks": res["clocks"],
                "tuning": res["tuning"],
+               "stages_ms_serial_step": {st: v[0] for st, v in res["stages"].items()},
                "updates_sketched": int(np.count_nonzero(res["info"][:, 13] > 0)),
                "sketches_accepted": int(np.count_nonzero(res["info"][:, 14] > 0)),
                "rel_fro_err_vs_fp64_dense_product": res.get("rel_fro_err_vs_fp64_dense_product"),

@@ -155,8 +155,79 @@ __device__ int jacobi_sweep(const TM &tm, double *X, int ldx, int rows, int ncol
     return rotations;
 }
 
+// The same sweep with the column pairs read from memory by G-lane groups in a loop over the rows
+// instead of register tiles (rows of any length, 32 / G pairs per warp): for long columns it packs
+// more pairs into each warp instruction than the register tiles can, which shares the per-pair
+// scalar FP64 work among more pairs at the price of reading the columns twice.
+template <int G, class TM>
+__device__ int jacobi_sweep_loop(const TM &tm, double *X, int ldx, int rows, int ncols, double *nrm, double tol2,
+                                 double tiny, int n2, double *dsc, int dstride) {
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
+    constexpr int PPW = 32 / G;
+    const int gl = lane % G, grp = lane / G;
+    const int npairs = n2 / 2;
+    const int nchunks = (npairs + PPW - 1) / PPW;
+    int rotations = 0;
+    for (int t = 0; t < n2 - 1; t++) {
+        for (int ch = warp; ch < nchunks; ch += nw) {
+            const int pp = ch * PPW + grp;
+            int i = 0, j = 0;
+            bool act = pp < npairs;
+            if (act) {
+                jacobi_pair(t, pp, n2, i, j);
+                act = i < ncols && j < ncols;
+            }
+            double *x = X + (size_t) (act ? i : 0) * ldx;
+            double *y = X + (size_t) (act ? j : 0) * ldx;
+            double c0 = 0.0, c1 = 0.0;
+            if (act) {
+                int r = gl;
+                for (; r + G < rows; r += 2 * G) {
+                    c0 = fma(x[r], y[r], c0);
+                    c1 = fma(x[r + G], y[r + G], c1);
+                }
+                if (r < rows) c0 = fma(x[r], y[r], c0);
+            }
+            const double c = group_sum(c0 + c1, G);
+            const double a = act ? nrm[i] : 0.0, b = act ? nrm[j] : 0.0;
+            double di = 1.0, dj = 1.0;
+            if (act) {
+                di = dsc[i];
+                dj = dsc[j];
+            }
+            const double cd = c * di * dj;  // true inner product
+            const bool rot = act && a > tiny && b > tiny && cd * cd > tol2 * a * b;
+            if (rot) {
+                const double tt = (double) jacobi_tangent(a, b, cd);
+                const double q = fma(tt, tt, 1.0);
+                const double cs = rsqrt(q);
+                const double dvi = dsc[dstride + i], dvj = dsc[dstride + j];
+                const double t1 = tt * dj * dvi, t2 = tt * di * dvj;
+#pragma unroll 4
+                for (int r = gl; r < rows; r += G) {
+                    const double xv = x[r], yv = y[r];
+                    x[r] = fma(-t1, yv, xv);
+                    y[r] = fma(t2, xv, yv);
+                }
+                if (gl == 0) {
+                    nrm[i] = a - tt * cd;
+                    nrm[j] = b + tt * cd;
+                    dsc[i] = di * cs;
+                    dsc[j] = dj * cs;
+                    dsc[dstride + i] = dvi * q * cs;
+                    dsc[dstride + j] = dvj * q * cs;
+                    rotations++;
+                }
+            }
+        }
+        tm.sync();
+    }
+    return rotations;
+}
+
 // Jacobi iteration on X: exact squared column norms at the start of every sweep (the scales of
 // the previous sweep folded into the columns), then sweeps until no pair rotates (or max_sweeps).
+// RPL = 0 selects the looped sweep.
 template <int G, int RPL, class TM>
 __device__ void jacobi(const TM &tm, double *X, int ldx, int rows, int ncols, double *nrm, int *s_rot,
                        double *s_amax, int *sweeps_out, bool *converged_out, double tol, int max_sweeps, double *dsc,
@@ -201,7 +272,11 @@ __device__ void jacobi(const TM &tm, double *X, int ldx, int rows, int ncols, do
         if (lane == 0) atomicMax(reinterpret_cast<unsigned long long *>(s_amax), __double_as_longlong(amax));
         tm.sync();
         const double tiny = *s_amax * noise * noise;
-        const int rot = jacobi_sweep<G, RPL>(tm, X, ldx, rows, ncols, nrm, tol2, tiny, n2, dsc, dstride);
+        int rot;
+        if constexpr (RPL == 0)
+            rot = jacobi_sweep_loop<G>(tm, X, ldx, rows, ncols, nrm, tol2, tiny, n2, dsc, dstride);
+        else
+            rot = jacobi_sweep<G, RPL>(tm, X, ldx, rows, ncols, nrm, tol2, tiny, n2, dsc, dstride);
         if (rot) atomicAdd(s_rot, rot);
         tm.sync();
         sweeps++;
@@ -386,14 +461,12 @@ __device__ void jacobi_dispatch(const TM &tm, double *X, int ldx, int rows, int 
     // issues one of them per ~19 cycles per SM, is shared by 4-8 pairs; RPL rows per lane stay in
     // registers.  (Two lanes per pair for columns of up to 32 rows, one warp taking every pair of a
     // step, measured slower: 760 vs 673 kcycles per 17-32-column core.)
+    // Longer columns: four lanes per pair in a loop over the rows (eight pairs per warp instruction).
     if (rows <= 32) jacobi<4, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 64 && MAXRPL >= 16) jacobi<4, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 64) jacobi<8, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
-    else if (rows <= 128 && MAXRPL >= 16) jacobi<8, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
-    else if (rows <= 128) jacobi<16, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
-    else if (rows <= 256 && MAXRPL >= 16) jacobi<16, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
-    else if (rows <= 256 || MAXRPL <= 8) jacobi<32, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
-    else jacobi<32, MAXRPL>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 128) jacobi<4, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else jacobi<8, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
 }
 
 // ---------------------------------------------------------------------------------------------
