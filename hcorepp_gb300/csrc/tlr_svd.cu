@@ -466,6 +466,9 @@ __device__ void jacobi_dispatch(const TM &tm, double *X, int ldx, int rows, int 
     else if (rows <= 64 && MAXRPL >= 16) jacobi<4, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 64) jacobi<8, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 128) jacobi<4, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    // The widest cores own a whole CTA, whose 16 warps the looped sweep does not keep busy (more pairs
+    // per warp, fewer warps): register tiles of 16 lanes measured faster there (60 vs 67 Mcycles).
+    else if (rows <= 256 && MAXRPL >= 16) jacobi<16, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else jacobi<8, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
 }
 
@@ -607,39 +610,31 @@ __device__ int qrcp_truncated(const TM &tm, double *A, int lda, int mrows, int n
     const int kk = mrows < ncols ? mrows : ncols;
     int rkeep = kk;
     for (int s = 0; s < kk; s++) {
-        // pivot = argmax of the remaining squared norms (ties to the lower index)
+        // pivot = argmax of the remaining squared norms (ties to the lower index), by the first warp
+        // alone: the scan is short, and one warp's reduction costs an eighth of the FP64 instructions
+        // of a team-wide one, whose barrier it also saves
         double bv = -1.0;
         int bi = s;
-        for (int j = s + tm.tid; j < ncols; j += tm.nth)
-            if (nrm[j] > bv) {
-                bv = nrm[j];
-                bi = j;
-            }
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov > bv || (ov == bv && oi < bi)) {
-                bv = ov;
-                bi = oi;
-            }
-        }
-        if (lane == 0) {
-            red[warp] = bv;
-            redi[warp] = bi;
-        }
-        tm.sync();
-        if (tm.tid == 0) {
-            double v = red[0];
-            int b = redi[0];
-            for (int w = 1; w < nw; w++)
-                if (red[w] > v || (red[w] == v && redi[w] < b)) {
-                    v = red[w];
-                    b = redi[w];
+        if (warp == 0) {
+            for (int j = s + lane; j < ncols; j += 32)
+                if (nrm[j] > bv) {
+                    bv = nrm[j];
+                    bi = j;
                 }
-            red[32] = v;
-            redi[32] = b;
-            if (s == 0 && stop2 == 0.0 && rel > 0.0) red[33] = rel * rel * v;
-            else if (s == 0) red[33] = stop2;
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) {
+                red[32] = bv;
+                redi[32] = bi;
+                if (s == 0 && stop2 == 0.0 && rel > 0.0) red[33] = rel * rel * bv;
+                else if (s == 0) red[33] = stop2;
+            }
         }
         tm.sync();
         bv = red[32];
@@ -669,17 +664,14 @@ __device__ int qrcp_truncated(const TM &tm, double *A, int lda, int mrows, int n
             }
         }
         tm.sync();
-        // Householder vector of column s (rows s..mrows-1), dlarfg convention.
+        // Householder vector of column s (rows s..mrows-1), dlarfg convention, by the first warp.
         double *x = A + (size_t) s * lda;
-        double ss = 0.0;
-        for (int i = s + 1 + tm.tid; i < mrows; i += tm.nth) ss = fma(x[i], x[i], ss);
-        ss = warp_sum(ss);
-        tm.sync();
-        if (lane == 0) red[warp] = ss;
-        tm.sync();
+        double t = 0.0;
+        if (warp == 0) {
+            for (int i = s + 1 + lane; i < mrows; i += 32) t = fma(x[i], x[i], t);
+            t = warp_sum(t);
+        }
         if (tm.tid == 0) {
-            double t = 0.0;
-            for (int w = 0; w < nw; w++) t += red[w];
             const double alpha = x[s];
             double tau = 0.0, scale = 0.0, beta = alpha;
             if (t != 0.0) {
@@ -697,12 +689,11 @@ __device__ int qrcp_truncated(const TM &tm, double *A, int lda, int mrows, int n
         tm.sync();
         // Apply H to the remaining columns; downdate their squared norms below row s
         // (nrm -= y_s^2) and recompute exactly when the downdate cancels (LAPACK dlaqp2's guard).
-        // Columns of up to 32, 64 or 128 rows are handled by groups of 4, 8 or 16 lanes, several
+        // Columns of up to 64, 256 or more rows are handled by groups of 4, 8 or 16 lanes, several
         // columns per warp instruction, so the reductions and the per-column scalar work are shared.
-        if (mrows <= 32) qrcp_apply<4>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
-        else if (mrows <= 64) qrcp_apply<8>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
-        else if (mrows <= 128) qrcp_apply<16>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
-        else qrcp_apply<32>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
+        if (mrows <= 64) qrcp_apply<4>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
+        else if (mrows <= 256) qrcp_apply<8>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
+        else qrcp_apply<16>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
         tm.sync();
     }
     return rkeep;
