@@ -699,6 +699,48 @@ __device__ int qrcp_truncated(const TM &tm, double *A, int lda, int mrows, int n
     return rkeep;
 }
 
+// qrcp_apply in float-float arithmetic (mixed form): H applied to columns s+1 .. ncols-1 by groups of
+// G lanes with Dot2 accumulation, squared norms downdated and recomputed when the downdate cancels.
+template <int G, class TM>
+__device__ __forceinline__ void qrcp_apply_df(const TM &tm, df *A, int lda, int mrows, int ncols, int s, const df *x,
+                                              df tau, df *nrm, df *nref) {
+    const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
+    constexpr int CPW = 32 / G;
+    const int gl = lane % G, grp = lane / G;
+    const bool has_tau = tau.h != 0.f;
+    for (int j0 = s + 1 + warp * CPW; j0 < ncols; j0 += nw * CPW) {
+        const int j = j0 + grp;
+        const bool act = j < ncols;
+        df *y = A + (size_t) (act ? j : s) * lda;  // idle groups read column s and write nothing
+        df w = df_f(0.f);
+        if (has_tau) {
+            df_acc wa = df_acc_init(gl == 0 ? y[s] : df_f(0.f));
+            for (int i = s + 1 + gl; i < mrows; i += G) df_acc_fma(wa, x[i], y[i]);
+            w = df_mul(group_sum(df_acc_value(wa), G), tau);
+            const df mw = -w;
+            if (act)
+                for (int i = s + 1 + gl; i < mrows; i += G) y[i] = df_fma(mw, x[i], y[i]);
+        }
+        const df ys = df_add(y[s], -w);  // every lane of the group reads the old y[s] before lane 0 writes it
+        __syncwarp();
+        if (act && gl == 0) y[s] = ys;
+        df nn = act ? df_add(nrm[j], -df_mul(ys, ys)) : df_f(0.f);
+        const bool exact = act && !(nn.h > 1e-8f * nref[j].h);  // lost 4+ digits since the last exact value
+        if (__any_sync(0xffffffffu, exact)) {
+            df e = df_f(0.f);
+            if (exact)
+                for (int i = s + 1 + gl; i < mrows; i += G) e = df_fma(y[i], y[i], e);
+            e = group_sum(e, G);
+            if (exact) nn = e;
+        }
+        __syncwarp();
+        if (act && gl == 0) {
+            nrm[j] = nn;
+            if (exact) nref[j] = nn;
+        }
+    }
+}
+
 // Float-float version of qrcp_truncated (mixed form), on a matrix scaled so that its entries are
 // near 1: same pivoting, early stop (stop2 on squared norms; stop2 == 0 with rel2 > 0 sets
 // stop2 = rel2 * |r_00|^2 after the first pivot; stop2 < 0 disables it) and norm downdating with
@@ -720,37 +762,28 @@ __device__ int qrcp_truncated_df(const TM &tm, df *A, int lda, int mrows, int nc
     const int kk = mrows < ncols ? mrows : ncols;
     int rkeep = kk;
     for (int s = 0; s < kk; s++) {
-        int bv = -1, bi = s;  // float bits of the largest remaining squared norm
-        for (int j = s + tm.tid; j < ncols; j += tm.nth) {
-            const int v = __float_as_int(nrm[j].h);
-            if (v > bv) {
-                bv = v;
-                bi = j;
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const int ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov > bv || (ov == bv && oi < bi)) {
-                bv = ov;
-                bi = oi;
-            }
-        }
-        if (lane == 0) {
-            redi[warp] = bv;
-            redi[32 + warp] = bi;
-        }
-        tm.sync();
-        if (tm.tid == 0) {
-            int v = redi[0], b = redi[32];
-            for (int w = 1; w < nw; w++)
-                if (redi[w] > v || (redi[w] == v && redi[32 + w] < b)) {
-                    v = redi[w];
-                    b = redi[32 + w];
+        int bv = -1, bi = s;  // float bits of the largest remaining squared norm (first warp only)
+        if (warp == 0) {
+            for (int j = s + lane; j < ncols; j += 32) {
+                const int v = __float_as_int(nrm[j].h);
+                if (v > bv) {
+                    bv = v;
+                    bi = j;
                 }
-            redi[64] = v;
-            redi[65] = b;
-            if (s == 0) red[33] = (stop2 == 0.f && rel2 > 0.f) ? rel2 * __int_as_float(v) : stop2;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const int ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) {
+                redi[64] = bv;
+                redi[65] = bi;
+                if (s == 0) red[33] = (stop2 == 0.f && rel2 > 0.f) ? rel2 * __int_as_float(bv) : stop2;
+            }
         }
         tm.sync();
         const float bvf = __int_as_float(redi[64]);
@@ -780,19 +813,15 @@ __device__ int qrcp_truncated_df(const TM &tm, df *A, int lda, int mrows, int nc
             }
         }
         tm.sync();
-        // Householder vector of column s (rows s..mrows-1), dlarfg convention.
+        // Householder vector of column s (rows s..mrows-1), dlarfg convention, by the first warp.
         df *x = A + (size_t) s * lda;
-        df ss = df_f(0.f);
-        for (int i = s + 1 + tm.tid; i < mrows; i += tm.nth) ss = df_fma(x[i], x[i], ss);
-        ss = group_sum(ss, 32);
-        tm.sync();
-        df *redd = reinterpret_cast<df *>(red + 64);  // per-warp partials (floats 64..127)
-        df *rts = reinterpret_cast<df *>(red + 40);   // tau and scale
-        if (lane == 0) redd[warp] = ss;
-        tm.sync();
+        df *rts = reinterpret_cast<df *>(red + 40);  // tau and scale
+        df t = df_f(0.f);
+        if (warp == 0) {
+            for (int i = s + 1 + lane; i < mrows; i += 32) t = df_fma(x[i], x[i], t);
+            t = group_sum(t, 32);
+        }
         if (tm.tid == 0) {
-            df t = df_f(0.f);
-            for (int w = 0; w < nw; w++) t = df_add(t, redd[w]);
             const df alpha = x[s];
             df tau = df_f(0.f), scale = df_f(0.f), beta = alpha;
             if (t.h != 0.f) {
@@ -809,33 +838,9 @@ __device__ int qrcp_truncated_df(const TM &tm, df *A, int lda, int mrows, int nc
         const df tau = rts[0], scale = rts[1];
         for (int i = s + 1 + tm.tid; i < mrows; i += tm.nth) x[i] = df_mul(x[i], scale);
         tm.sync();
-        const bool has_tau = tau.h != 0.f;
-        for (int j = s + 1 + warp; j < ncols; j += nw) {
-            df *y = A + (size_t) j * lda;
-            df w = df_f(0.f);
-            if (has_tau) {
-                df_acc wa = df_acc_init(lane == 0 ? y[s] : df_f(0.f));
-                for (int i = s + 1 + lane; i < mrows; i += 32) df_acc_fma(wa, x[i], y[i]);
-                w = df_mul(group_sum(df_acc_value(wa), 32), tau);
-                const df mw = -w;
-                for (int i = s + 1 + lane; i < mrows; i += 32) y[i] = df_fma(mw, x[i], y[i]);
-            }
-            const df ys = df_add(y[s], -w);  // all lanes read the old y[s] before lane 0 writes it
-            __syncwarp();
-            if (lane == 0) y[s] = ys;
-            df nn = df_add(nrm[j], -df_mul(ys, ys));
-            const bool exact = !(nn.h > 1e-8f * nref[j].h);  // lost 4+ digits since the last exact value
-            if (exact) {
-                nn = df_f(0.f);
-                for (int i = s + 1 + lane; i < mrows; i += 32) nn = df_fma(y[i], y[i], nn);
-                nn = group_sum(nn, 32);
-            }
-            __syncwarp();
-            if (lane == 0) {
-                nrm[j] = nn;
-                if (exact) nref[j] = nn;
-            }
-        }
+        if (mrows <= 64) qrcp_apply_df<4>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
+        else if (mrows <= 256) qrcp_apply_df<8>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
+        else qrcp_apply_df<16>(tm, A, lda, mrows, ncols, s, x, tau, nrm, nref);
         tm.sync();
     }
     return rkeep;
