@@ -31,22 +31,6 @@ __host__ __device__ __forceinline__ int qr_w_cols(int kmax) {
     return w < 512 ? w : 512;
 }
 
-// Block-wide sum; `red` holds >= 33 doubles.  Must be called by all threads.
-__device__ double block_sum(double v, double *red) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    v = warp_sum(v);
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (warp == 0) {
-        double t = lane < nw ? red[lane] : 0.0;
-        t = warp_sum(t);
-        if (lane == 0) red[32] = t;
-    }
-    __syncthreads();
-    return red[32];
-}
-
 // Householder QR of the panel in shared memory: column c at Ps + c*ldp, rows 0..mr-1.
 // LAPACK dlarfg convention: beta = -sign(alpha) * ||x||, tau = (beta - alpha) / beta,
 // v = x / (alpha - beta) with v_0 = 1 implicit; tau = 0 when the tail is zero.
@@ -54,9 +38,13 @@ __device__ void factor_panel(double *Ps, int ldp, int mr, int nbp, double *tau_s
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int j = 0; j < nbp; j++) {
         double *x = Ps + (size_t) j * ldp;
+        // the reflector's norm on the first warp alone: a block-wide sum would issue eight warps'
+        // reductions on the FP64 pipe and cost two more barriers
         double ss = 0.0;
-        for (int r = j + 1 + threadIdx.x; r < mr; r += blockDim.x) ss = fma(x[r], x[r], ss);
-        ss = block_sum(ss, red);
+        if (warp == 0) {
+            for (int r = j + 1 + lane; r < mr; r += 32) ss = fma(x[r], x[r], ss);
+            ss = warp_sum(ss);
+        }
         if (threadIdx.x == 0) {
             const double alpha = x[j];
             double tau = 0.0, scale = 0.0, beta = alpha;

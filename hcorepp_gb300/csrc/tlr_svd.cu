@@ -466,9 +466,8 @@ __device__ void jacobi_dispatch(const TM &tm, double *X, int ldx, int rows, int 
     else if (rows <= 64 && MAXRPL >= 16) jacobi<4, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 64) jacobi<8, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 128) jacobi<4, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
-    // The widest cores own a whole CTA, whose 16 warps the looped sweep does not keep busy (more pairs
-    // per warp, fewer warps): register tiles of 16 lanes measured faster there (60 vs 67 Mcycles).
-    else if (rows <= 256 && MAXRPL >= 16) jacobi<16, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    // (16-lane register tiles for 129-256 rows: the widest cores' Jacobi 60 instead of 67 Mcycles, but
+    // the whole core stage 367 instead of 352 ms, since most such cores are narrower.)
     else jacobi<8, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
 }
 
