@@ -674,6 +674,7 @@ def gpu_arm(args, rank, world, local):
                "gpu_launches_per_step": res["gpu_launches_per_step"], "clocks": res["clocks"],
                "tuning": res["tuning"],
                "stages_ms_serial_step": {st: v[0] for st, v in res["stages"].items()},
+               "core_kcycles_by_core_cols": core_cycle_classes(res["info"]),
                "updates_sketched": int(np.count_nonzero(res["info"][:, 13] > 0)),
                "sketches_accepted": int(np.count_nonzero(res["info"][:, 14] > 0)),
                "rel_fro_err_vs_fp64_dense_product": res.get("rel_fro_err_vs_fp64_dense_product"),
