@@ -125,6 +125,8 @@ def lib():
         L.hcgb_set_tuning.restype = C.c_int
         L.hcgb_set_precond.argtypes = [vp, ip]
         L.hcgb_set_precond.restype = C.c_int
+        L.hcgb_set_sketch_limit.argtypes = [vp, ip]
+        L.hcgb_set_sketch_limit.restype = C.c_int
         for nm in ("hcgb_rank_model_create", "hcgb_rank_model_destroy", "hcgb_rank_model_params",
                    "hcgb_rank_model_predict", "hcgb_rank_model_gradient", "hcgb_rank_model_train",
                    "hcgb_set_rank_model", "hcgb_set_feature_sink"):
@@ -194,6 +196,9 @@ class Context:
 
     def set_precond(self, min_cols: int = 0):
         self.check(lib().hcgb_set_precond(self._h, int(min_cols)))
+
+    def set_sketch_limit(self, percent: int = 0):
+        self.check(lib().hcgb_set_sketch_limit(self._h, int(percent)))
 
     def set_concurrency(self, groups: int):
         self.check(lib().hcgb_set_concurrency(self._h, int(groups)))

@@ -46,6 +46,7 @@ struct hcgb_context {
     int oz_min = OZ_MIN_OUTPUTS;     // tuning: outputs a product needs for the tensor cores
     int wy_min = WY_MIN_REFLECTORS;  // tuning: reflectors a side needs for the WY Q application
     int precond_min = PRECOND_MIN_COLS;  // tuning: core columns for the plain form's FP32 preconditioning
+    int sk_pct = SKETCH_MAX_PCT;         // learned form: widest sketch, in percent of the stack width
     std::vector<cudaStream_t> group_streams;
     std::vector<cudaEvent_t> group_events;  // [0] fork, [1..] joins
     void *pack_desc = nullptr;  // DevTile[] of hcgb_pack_tiles / hcgb_unpack_tiles
@@ -202,6 +203,7 @@ Params to_params(const hcgb_params *p, const hcgb_context *ctx) {
     q.oz_min = ctx ? ctx->oz_min : OZ_MIN_OUTPUTS;
     q.wy_min = ctx ? ctx->wy_min : WY_MIN_REFLECTORS;
     q.precond_min = ctx ? ctx->precond_min : PRECOND_MIN_COLS;
+    q.sk_pct = ctx ? ctx->sk_pct : SKETCH_MAX_PCT;
     q.accuracy = p ? p->accuracy : 1e-9;
     q.truncated = p ? p->truncated_svd : 0;
     q.fixed_rank = p ? p->fixed_rank : 0;
@@ -488,7 +490,7 @@ int hcgb_tlr_gemm(hcgb_context *ctx, int mt, int nt, int kt, double alpha, const
     if (ctx->graph_mode) {
         auto put = [&](const void *p, size_t b) { key.append(static_cast<const char *>(p), b); };
         const int ints[] = {mt, nt, kt, ctx->groups, ctx->k_order, ctx->oz, ctx->learned ? 1 : 0, ctx->sk_policy,
-                            ctx->oz_min, ctx->wy_min, ctx->precond_min};
+                            ctx->oz_min, ctx->wy_min, ctx->precond_min, ctx->sk_pct};
         put(ints, sizeof(ints));
         put(&alpha, sizeof(alpha));
         put(&beta, sizeof(beta));
@@ -1606,6 +1608,12 @@ extern "C" int hcgb_set_tuning(hcgb_context *ctx, int oz_min_outputs, int wy_min
     if (!ctx || oz_min_outputs < 1 || wy_min_reflectors < 1) return HCGB_BAD_ARG;
     ctx->oz_min = oz_min_outputs;
     ctx->wy_min = wy_min_reflectors;
+    return HCGB_OK;
+}
+
+extern "C" int hcgb_set_sketch_limit(hcgb_context *ctx, int percent) {
+    if (!ctx || percent < 0 || percent > 100) return HCGB_BAD_ARG;
+    ctx->sk_pct = percent ? percent : SKETCH_MAX_PCT;
     return HCGB_OK;
 }
 

@@ -176,7 +176,13 @@ struct Params {
     int oz_min;      // outputs a product needs to go to the tensor cores (OZ_MIN_OUTPUTS by default)
     int wy_min;      // reflectors a side needs for the WY Q application (WY_MIN_REFLECTORS by default)
     int precond_min; // plain form: Jacobi columns a core needs for the FP32 preconditioning sweeps
+    int sk_pct;      // learned form: sketch an update only when its sketch (with probes) is at most
+                     // this percentage of its stack width
 };
+
+// Default of Params::sk_pct: a sketch of half the stack width halves the QR and Q-application work,
+// which pays for the sketch products and its own QR; wider sketches cost more than they save.
+constexpr int SKETCH_MAX_PCT = 50;
 
 // Default of Params::precond_min: off.  Measured on the 32 x 32-tile nb = 512 multiply, the FP32
 // preconditioning sweeps cut the FP64 sweeps from ~4.7 to ~3 but cost more than they save

@@ -7,7 +7,8 @@
 //   features   12 inputs of the predictor (ranks, leading singular-value ratios of the factors,
 //              norms, tile distance, accuracy; below)
 //   predict    y = MLP(features) ~ log2(1 + new rank)  (mlp.cu)
-//   plan       l = ceil(2^y - 1) + 8 (oversampling), taken when l + 4 <= k; Omega = [Omega_l | 4 probe
+//   plan       l = ceil(2^y - 1) + 8 (oversampling), taken when l + 4 <= k * sk_pct / 100 (half the
+//              stack width by default); Omega = [Omega_l | 4 probe
 //              columns], seeded N(0, 1) entries
 //   products   Z = V_s^T Omega, Y = P Omega = U_s Z
 //   sketch QR  Householder QR of Y[:, :l], its reflectors applied to the probe columns, whose parts
@@ -184,7 +185,8 @@ __global__ void sketch_plan_kernel(const DevUpdate *ups, int n, Workspace ws, Pa
     int l = (int) ceilf(rhat) + SK_OVERSAMPLE;
     if (l < 1 + SK_OVERSAMPLE) l = 1 + SK_OVERSAMPLE;
     const int mn = m < nn ? m : nn;
-    if (l + SK_PROBES > k || l > mn) return;  // no smaller than the stacks: the plain recompression
+    // not narrow enough to pay for itself (or no smaller than the stacks): the plain recompression
+    if (100 * (l + SK_PROBES) > p.sk_pct * k || l > mn) return;
     meta[META_LSK] = l;
     double *base = ws.slot(s);
     const int ld = ws.ld, lk = ws.kmax;

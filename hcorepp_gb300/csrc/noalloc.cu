@@ -140,6 +140,7 @@ extern "C" int hcgb_tile_gemm_noalloc(double alpha, const hcgb_tile *a, const hc
     prm.oz_min = OZ_MIN_OUTPUTS;
     prm.wy_min = WY_MIN_REFLECTORS;
     prm.precond_min = PRECOND_MIN_COLS;
+    prm.sk_pct = SKETCH_MAX_PCT;
 
     // GEMM grid bounds from the tile kinds and capacities (ranks are read on the device).
     int pm[3] = {0, 0, 0}, pn[3] = {0, 0, 0};

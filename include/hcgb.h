@@ -188,6 +188,12 @@ int hcgb_set_tuning(hcgb_context *ctx, int oz_min_outputs, int wy_min_reflectors
  * the default (off: a value above every core width); same results up to rounding. */
 int hcgb_set_precond(hcgb_context *ctx, int min_cols);
 
+/* Learned form: an update is sketched only when its sketch (predicted rank + 8 oversampling + 4
+ * probe columns) is at most `percent` of its stack width (1..100; 0 restores the default, 50).  A
+ * narrower limit keeps the sketch to the updates where it halves the QR and Q-application work; 100
+ * sketches every update whose sketch is narrower than its stacks. */
+int hcgb_set_sketch_limit(hcgb_context *ctx, int percent);
+
 /* Factor products of k >= 16 with at least 2048 outputs run on the 16-bit tensor cores by
  * error-free splitting (each FP64 operand cut into eight 7-bit integer digit planes relative to its
  * row / column maximum, plane products accumulated exactly in FP32 and combined in FP64; result

@@ -128,11 +128,14 @@ def test_learned_multiply_vs_oracle(env, trained, policy):
     else:
         RM.learned_without_network()
     info = T.info_buffer(nt ** 3)
+    ctx = T.run_context()
+    ctx.set_sketch_limit(100)  # every update whose sketch is narrower than its stacks: the sketch path under test
     try:
         T.tlr_gemm(1.0, A, A, 1.0, Cm, T.CompressionParameters(ACC, truncated_svd=True), info)
         torch.cuda.synchronize()
     finally:
         RM.learned_off()
+        ctx.set_sketch_limit(0)
     rec = info.cpu().numpy()
     assert int(rec[:, 0].max()) == 0
     sketched = int(np.count_nonzero(rec[:, 13] > 0))
@@ -149,3 +152,28 @@ def test_learned_multiply_vs_oracle(env, trained, policy):
             assert rel_fro(g[sl], exact[sl]) <= 2 * max(e_o, ACC), (i, j)
             if gc[i][j].kind != "dense":
                 assert abs(int(ranks[i, j]) - gc[i][j].rank) <= 1, (i, j, ranks[i, j], gc[i][j].rank)
+
+
+def test_default_sketch_limit_keeps_sketches_to_half_the_stack(env, trained):
+    """hcgb_set_sketch_limit: by default an update is sketched only when its sketch (with the probe
+    columns) is at most half its stack width; the result keeps the same accuracy bar."""
+    torch, L, T, RM = env
+    m = trained[0]
+    ga, gc, nt, nb = _problem(env, 13)
+    A = load_tile_matrix(T, L, ga, nb, nb // 3)
+    Cm = load_tile_matrix(T, L, gc, nb, nb // 3)
+    exact = A.to_dense() @ A.to_dense() + Cm.to_dense()
+    m.enable()
+    info = T.info_buffer(nt ** 3)
+    try:
+        T.tlr_gemm(1.0, A, A, 1.0, Cm, T.CompressionParameters(ACC, truncated_svd=True), info)
+        torch.cuda.synchronize()
+    finally:
+        RM.learned_off()
+    rec = info.cpu().numpy()
+    assert int(rec[:, 0].max()) == 0
+    sk = rec[:, 13] > 0
+    assert np.all(2 * (rec[sk, 13] + 4) <= rec[sk, 4]), rec[sk][:, [4, 13]]
+    O.tile_matrix_multiply(ga, ga, gc, 1.0, 1.0, O.CompressionParameters(ACC, truncated_svd=True))
+    o = np.block([[t.to_dense() for t in row] for row in gc])
+    assert rel_fro(Cm.to_dense(), exact) <= 2 * max(rel_fro(o, exact), ACC)
