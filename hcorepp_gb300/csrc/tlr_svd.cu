@@ -458,20 +458,26 @@ __device__ void jacobi_df_dispatch(const TM &tm, df *X, int ldx, int rows, int n
 template <int MAXRPL, class TM>
 __device__ void jacobi_dispatch(const TM &tm, double *X, int ldx, int rows, int ncols, double *nrm, int *s_rot,
                                 double *s_amax, int *sweeps, bool *conv, double tol, int max_sweeps, double *dsc,
-                                int dstride) {
+                                int dstride, bool x_in_smem) {
     // Fewer lanes per pair put more pairs in one warp instruction, so the per-pair scalar work
     // (tangent, tests, norm updates), which runs as full-width FP64 warp instructions on a pipe that
     // issues one of them per ~19 cycles per SM, is shared by 4-8 pairs; RPL rows per lane stay in
     // registers.  (Two lanes per pair for columns of up to 32 rows, one warp taking every pair of a
     // step, measured slower: 760 vs 673 kcycles per 17-32-column core.)
-    // Longer columns: four lanes per pair in a loop over the rows (eight pairs per warp instruction).
+    // Longer columns held in shared memory: 4- or 8-lane groups in a loop over the rows (8 or 4 pairs
+    // per warp instruction; each pair is read twice).  Columns in the workspace (cores too wide for
+    // the team's shared memory) keep register tiles, which read them once: the loop measured 15-35 %
+    // slower there (long-scoreboard stalls on the second read).
     if (rows <= 32) jacobi<4, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 64 && MAXRPL >= 16) jacobi<4, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
     else if (rows <= 64) jacobi<8, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
-    else if (rows <= 128) jacobi<4, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
-    // (16-lane register tiles for 129-256 rows: the widest cores' Jacobi 60 instead of 67 Mcycles, but
-    // the whole core stage 367 instead of 352 ms, since most such cores are narrower.)
-    else jacobi<8, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (x_in_smem && rows <= 128) jacobi<4, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (x_in_smem) jacobi<8, 0>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 128 && MAXRPL >= 16) jacobi<8, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 128) jacobi<16, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 256 && MAXRPL >= 16) jacobi<16, 16>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else if (rows <= 256 || MAXRPL <= 8) jacobi<32, 8>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
+    else jacobi<32, MAXRPL>(tm, X, ldx, rows, ncols, nrm, s_rot, s_amax, sweeps, conv, tol, max_sweeps, dsc, dstride);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1105,7 +1111,7 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
             tm.sync();
         }
         jacobi_dispatch<RPL>(tm, X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64, MAX_JACOBI_SWEEPS,
-                             dsc, ws.kmax);
+                             dsc, ws.kmax, Mw == pool);
     }
 
     const long long t3 = clock64();
