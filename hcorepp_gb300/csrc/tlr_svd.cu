@@ -866,57 +866,80 @@ __device__ __forceinline__ int order_key(const Workspace &ws, int slot) {
     return m[META_CKIND] ? m[META_K] : 0;
 }
 
-// CTA of SVD_THREADS threads.  Updates with k > kthr ("heavy": their core does not fit half of the
-// shared memory) get a whole CTA each; the others are paired, one per half-CTA team of
-// SVD_THREADS / 2 threads with its own half of the shared memory and its own named barrier.  With
-// ws.order (sorted by decreasing k) the heavy updates are its first H entries: CTA b < H takes
-// order[b], CTA H + i takes order[H + 2i] and order[H + 2i + 1].  Without an order (one update per
-// CTA) the team size follows the same class rule, so an update's arithmetic never depends on the
-// launch it is part of.
+// CTA of SVD_THREADS threads, in one of three team layouts chosen by the update's stack width k:
+// heavy (k > kthr: the core does not fit half of the shared memory) — the whole CTA for one update;
+// light (kthr4 < k <= kthr) — two half-CTA teams of SVD_THREADS / 2 threads, one update each, each
+// with half of the shared memory and its own named barrier; small (k <= kthr4: the core fits a
+// quarter) — four teams of SVD_THREADS / 4 threads.  Small cores are latency-bound (per-step
+// barriers, dependent FP64 chains), so four of them per SM hide each other's latency.  With ws.order
+// (sorted by decreasing k) the classes are contiguous: CTA b < H takes order[b]; the next ceil(L / 2)
+// CTAs take the L light updates in pairs; the rest take the small ones in fours.  Without an order
+// (one update per CTA) the team size follows the same class rule, so an update's arithmetic never
+// depends on the launch it is part of.
 template <int RPL>
 __global__ void __launch_bounds__(SVD_THREADS, 1) core_svd_kernel(const DevUpdate *ups, int nup, Workspace ws,
-                                                               Params p, int team_doubles, int kthr) {
+                                                               Params p, int team_doubles, int kthr, int kthr4) {
     extern __shared__ double smem_all[];
-    __shared__ int s_rot_a[2], s_rank_a[2], s_emax_a[2], s_nheavy;
-    __shared__ double s_amax_a[2];
+    __shared__ int s_rot_a[4], s_rank_a[4], s_emax_a[4], s_nheavy, s_nlight;
+    __shared__ double s_amax_a[4];
     if (threadIdx.x == 0) {
-        int h = -1;
+        int h = -1, h2 = -1;
         if (ws.order) {
-            int lo = 0, hi = nup;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (order_key(ws, ws.order[mid]) > kthr) lo = mid + 1;
-                else hi = mid;
-            }
-            h = lo;
+            auto count_above = [&](int thr) {  // entries with key > thr (keys descending)
+                int lo = 0, hi = nup;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (order_key(ws, ws.order[mid]) > thr) lo = mid + 1;
+                    else hi = mid;
+                }
+                return lo;
+            };
+            h = count_above(kthr);
+            h2 = count_above(kthr4);
         }
         s_nheavy = h;
+        s_nlight = h2 - h;
     }
     __syncthreads();
-    const int H = s_nheavy;
-    constexpr int HALF = SVD_THREADS / 2;
-    int idx, half = 0;
-    bool heavy;
+    const int H = s_nheavy, NL = s_nlight;
+    constexpr int HALF = SVD_THREADS / 2, QUART = SVD_THREADS / 4;
+    const int quarter_doubles = team_doubles / 2;
+    int idx, part = 0, cls;  // cls 0 heavy, 1 light, 2 small
     if (H < 0) {
         idx = blockIdx.x;
-        heavy = order_key(ws, idx) > kthr;
-        if (!heavy && threadIdx.x >= HALF) return;
-    } else if ((int) blockIdx.x < H) {
-        idx = blockIdx.x;
-        heavy = true;
+        if (idx >= nup) return;
+        const int key = order_key(ws, idx);
+        cls = key > kthr ? 0 : (key > kthr4 ? 1 : 2);
+        if (cls == 1 && threadIdx.x >= HALF) return;
+        if (cls == 2 && threadIdx.x >= QUART) return;
     } else {
-        heavy = false;
-        half = threadIdx.x / HALF;
-        idx = H + 2 * ((int) blockIdx.x - H) + half;
+        const int b = blockIdx.x, nlb = (NL + 1) / 2;
+        if (b < H) {
+            idx = b;
+            cls = 0;
+        } else if (b < H + nlb) {
+            cls = 1;
+            part = threadIdx.x / HALF;
+            idx = H + 2 * (b - H) + part;
+            if (idx >= H + NL) return;  // the odd light update's partner slot stays idle
+        } else {
+            cls = 2;
+            part = threadIdx.x / QUART;
+            idx = H + NL + 4 * (b - H - nlb) + part;
+        }
     }
     if (idx >= nup) return;
-    double *sm = smem_all + (size_t) half * team_doubles;
-    if (heavy)
-        core_update<RPL>(Team<SVD_THREADS>{(int) threadIdx.x, 1}, ups, ws, p, ws.heavy(idx), sm, 2 * team_doubles,
-                         s_rot_a[0], s_rank_a[0], s_emax_a[0], s_amax_a[0]);
+    if (cls == 0)
+        core_update<RPL>(Team<SVD_THREADS>{(int) threadIdx.x, 1}, ups, ws, p, ws.heavy(idx), smem_all,
+                         2 * team_doubles, s_rot_a[0], s_rank_a[0], s_emax_a[0], s_amax_a[0]);
+    else if (cls == 1)
+        core_update<RPL>(Team<HALF>{(int) threadIdx.x % HALF, 1 + part}, ups, ws, p, ws.heavy(idx),
+                         smem_all + (size_t) part * team_doubles, team_doubles, s_rot_a[part], s_rank_a[part],
+                         s_emax_a[part], s_amax_a[part]);
     else
-        core_update<RPL>(Team<HALF>{(int) threadIdx.x % HALF, 1 + half}, ups, ws, p, ws.heavy(idx), sm, team_doubles,
-                         s_rot_a[half], s_rank_a[half], s_emax_a[half], s_amax_a[half]);
+        core_update<RPL>(Team<QUART>{(int) threadIdx.x % QUART, 1 + part}, ups, ws, p, ws.heavy(idx),
+                         smem_all + (size_t) part * quarter_doubles, quarter_doubles, s_rot_a[part], s_rank_a[part],
+                         s_emax_a[part], s_amax_a[part]);
 }
 
 // The recompression core of one update (slot) by one team, with `smem_doubles` of shared memory at sm.
@@ -1235,12 +1258,15 @@ template <int RPL>
 static void launch_core_svd_t(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st) {
     const int team = svd_team_doubles(ws.kmax);
     const size_t smem = 2 * sizeof(double) * (size_t) team;
-    // Heavy: a core of k columns (k x k working copy) does not fit the team's pool.
-    const long pool = (long) team - 6L * ws.kmax - SVD_AUX_FIXED;
-    int kthr = 0;
+    // Heavy: a core of k columns (k x k working copy) does not fit the half-CTA team's pool; small: it
+    // fits a quarter-CTA team's pool (a quarter of the shared memory less the same aux arrays).
+    const long aux = 6L * ws.kmax + SVD_AUX_FIXED;
+    const long pool = (long) team - aux, pool4 = (long) (team / 2) - aux;
+    int kthr = 0, kthr4 = 0;
     while ((long) (kthr + 1) * (kthr + 1) <= pool) kthr++;
+    while (pool4 > 0 && (long) (kthr4 + 1) * (kthr4 + 1) <= pool4) kthr4++;
     cudaFuncSetAttribute(core_svd_kernel<RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    { core_svd_kernel<RPL><<<n, SVD_THREADS, smem, st>>>(ups, n, ws, p, team, kthr); note_launch(); }
+    { core_svd_kernel<RPL><<<n, SVD_THREADS, smem, st>>>(ups, n, ws, p, team, kthr, kthr4); note_launch(); }
 }
 
 // Rows of M are at most min(ld, kmax); the register tile of a rotation covers 32 * RPL rows.
