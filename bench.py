@@ -384,6 +384,32 @@ class Workbench:
         moved["d2h"] = total * 8 + 4 * e["outr_pin"].numel() + 8
         moved["total"] = total
 
+    def copy_rates(self, moved):
+        """The e2e step's host <-> device copies timed alone (CUDA events, same pinned buffers and sizes):
+        the part of the e2e gap that is transfer, the rest being the pack / unpack kernels and the one
+        host synchronisation that reads the packed size before the device -> host copy."""
+        torch = self.torch
+        e = self._e2e_buffers()
+        stream = torch.cuda.current_stream()
+        total = moved["total"]
+        out = {}
+        for name, fn, nbytes in (
+                ("h2d", lambda: (e["a_dev"].copy_(e["a_pk"], non_blocking=True),
+                                 e["c_dev"].copy_(e["c_pk"], non_blocking=True)),
+                 8 * (e["a_pk"].numel() + e["c_pk"].numel())),
+                ("d2h", lambda: e["out_pin"][:total].copy_(e["out_dev"][:total], non_blocking=True), 8 * total)):
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(3):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 3
+            out[name] = {"ms": ms, "gb_per_s": nbytes / (ms * 1e-3) / 1e9}
+        return out
+
     def e2e_matches_device_run(self, moved):
         """The host copy of the e2e result against the device-resident run's result (same multiply)."""
         e = self._e2e_buffers()
@@ -476,7 +502,8 @@ def measure_form(wb, form, mode, args, world, with_e2e=True, accuracy=None, step
                       "d2h_bytes_per_step": int(moved["d2h"]), "ms_per_step": e2e_ms,
                       "transfer": "rank-trimmed packed tiles (hcgb_pack_tiles / hcgb_unpack_tiles), pinned host "
                                   "buffers",
-                      "result_matches_device_run": wb.e2e_matches_device_run(moved)}
+                      "result_matches_device_run": wb.e2e_matches_device_run(moved),
+                      "copies_alone": wb.copy_rates(moved)}
     out["info"] = info_h
     autotune.apply(ctx, autotune.DEFAULT)
     if model is not None:
