@@ -83,15 +83,13 @@ __device__ void factor_panel_df(const TM &tm, df *Ps, int ldp, int mr, int nbp, 
     df *redd = reinterpret_cast<df *>(red);
     for (int j = 0; j < nbp; j++) {
         df *x = Ps + (size_t) j * ldp;
-        df ss = df_f(0.f);
-        for (int r = j + 1 + tm.tid; r < mr; r += tm.nth) ss = df_fma(x[r], x[r], ss);
-        ss = df_group_sum(ss, 32);
-        tm.sync();
-        if (lane == 0) redd[warp] = ss;
-        tm.sync();
+        // the reflector's norm on the first warp alone (no team-wide reduction, two barriers fewer)
+        df t = df_f(0.f);
+        if (warp == 0) {
+            for (int r = j + 1 + lane; r < mr; r += 32) t = df_fma(x[r], x[r], t);
+            t = df_group_sum(t, 32);
+        }
         if (tm.tid == 0) {
-            df t = df_f(0.f);
-            for (int w = 0; w < nw; w++) t = df_add(t, redd[w]);
             const df alpha = x[j];
             df tau = df_f(0.f), scale = df_f(0.f), beta = alpha;
             if (t.h != 0.f) {
