@@ -24,7 +24,7 @@ import numpy as np
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_cache.json")
 DEFAULT = {"groups": 8, "wy_min": 48, "oz_min": 2048, "graph": 0, "precond": 1 << 30}
-CANDIDATES = {"groups": [4, 8, 16], "wy_min": [32, 48, 96, 1 << 30], "oz_min": [2048, 4096, 8192],
+CANDIDATES = {"groups": [4, 8, 16], "wy_min": [32, 48, 96, 1 << 30], "oz_min": [512, 1024, 2048, 4096],
               "graph": [0, 1], "precond": [16, 32, 64, 1 << 30]}
 ORDER = ["groups", "wy_min", "oz_min", "graph", "precond"]
 FORM_KNOBS = {"mixed_ff48": ["groups", "wy_min", "oz_min", "graph"]}  # precond acts on the plain form only
