@@ -74,7 +74,7 @@ typedef struct {
  * significand) on the FP32 pipe, each block scaled by an exact power of two first; the core
  * product, the new factors, the truncation test and all factor products stay in double precision.
  * Backward error of the float-float stages ~2^-48 relative: same ranks and product accuracy as the
- * plain form at the accuracies this path is used at (>= 1e-12 relative), about 1.7x as fast.
+ * plain form at the accuracies this path is used at (>= 1e-12 relative), about 1.6x as fast.
  * In both forms the larger factor products run on the 16-bit tensor cores by FP64-accurate
  * error-free splitting unless hcgb_set_tensor_products(ctx, 0). */
 typedef enum { HCGB_PLAIN_FP64 = 0, HCGB_MIXED = 1, HCGB_TF32 = 2, HCGB_BF16 = 3 } hcgb_mode;
