@@ -958,15 +958,17 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
     const double *RU = base + ws.off_ustack;
     const double *RV = base + ws.off_vstack;
     double *Mc = base + ws.off_mcopy;
-    // Aux arrays at the start of the team's shared memory: sorted sigma, scratch, column norms,
-    // the sort permutation, the QR pivots and a reduction area (64 doubles + 128 ints).
+    // Aux arrays at the start of the team's shared memory, sized by this update's stack width ka
+    // (every index below is < k): sorted sigma, scratch, column norms, the sort permutation, the QR
+    // pivots, the Jacobi scales and a reduction area (64 doubles + 128 ints).
+    const int ka = k > 0 ? k : 1;
     double *sig = sm;
-    double *inv = sig + ws.kmax;
-    double *nrm = inv + ws.kmax;
-    int *perm = reinterpret_cast<int *>(nrm + ws.kmax);
-    int *pvt = perm + ws.kmax;
-    double *dsc = nrm + ws.kmax + ws.kmax + 1;  // Jacobi column scales d and 1/d (2 kmax)
-    double *red = dsc + 2 * ws.kmax;
+    double *inv = sig + ka;
+    double *nrm = inv + ka;
+    int *perm = reinterpret_cast<int *>(nrm + ka);
+    int *pvt = perm + ka;
+    double *dsc = nrm + ka + ka + 1;  // Jacobi column scales d and 1/d (2 ka)
+    double *red = dsc + 2 * ka;
     int *redi = reinterpret_cast<int *>(red + SVD_RED_DOUBLES);
     double *pool = red + SVD_RED_DOUBLES + SVD_REDI_INTS / 2;
     const int pool_doubles = smem_doubles - (int) (pool - sm);
@@ -1080,7 +1082,7 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
         const float tol_df = 16.f * 3.5527137e-15f * (float) (kV > 1 ? kV : 1);
         // norms and scales as float-float values in the (double-sized) nrm and dsc arrays
         jacobi_df_dispatch<RPL>(tm, Xd, ldx, kV, rk, reinterpret_cast<df *>(nrm), reinterpret_cast<df *>(dsc),
-                                reinterpret_cast<df *>(dsc + ws.kmax), &s_rot, reinterpret_cast<float *>(&s_amax),
+                                reinterpret_cast<df *>(dsc + ka), &s_rot, reinterpret_cast<float *>(&s_amax),
                                 &sweeps, &converged, tol_df, MAX_JACOBI_SWEEPS);
         for (int e = tm.tid; e < kV * rk; e += tm.nth) {
             const size_t o = (e % kV) + (size_t) (e / kV) * ldx;
@@ -1135,7 +1137,7 @@ __device__ void core_update(const TM &tm, const DevUpdate *ups, const Workspace 
             tm.sync();
         }
         jacobi_dispatch<RPL>(tm, X, ldx, kV, rk, nrm, &s_rot, &s_amax, &sweeps, &converged, tol64, MAX_JACOBI_SWEEPS,
-                             dsc, ws.kmax, Mw == pool);
+                             dsc, ka, Mw == pool);
     }
 
     const long long t3 = clock64();
@@ -1259,13 +1261,12 @@ template <int RPL>
 static void launch_core_svd_t(const DevUpdate *ups, int n, Workspace ws, Params p, cudaStream_t st) {
     const int team = svd_team_doubles(ws.kmax);
     const size_t smem = 2 * sizeof(double) * (size_t) team;
-    // Heavy: a core of k columns (k x k working copy) does not fit the half-CTA team's pool; small: it
-    // fits a quarter-CTA team's pool (a quarter of the shared memory less the same aux arrays).
-    const long aux = 6L * ws.kmax + SVD_AUX_FIXED;
-    const long pool = (long) team - aux, pool4 = (long) (team / 2) - aux;
+    // Heavy: a core of k columns (its aux arrays, 6 k + SVD_AUX_FIXED doubles, and a k x k working
+    // copy) does not fit the half-CTA team's shared memory; small: it fits a quarter-CTA team's.
+    auto fits = [](long k, long doubles) { return k * k + 6 * k + SVD_AUX_FIXED <= doubles; };
     int kthr = 0, kthr4 = 0;
-    while ((long) (kthr + 1) * (kthr + 1) <= pool) kthr++;
-    while (pool4 > 0 && (long) (kthr4 + 1) * (kthr4 + 1) <= pool4) kthr4++;
+    while (fits(kthr + 1, team)) kthr++;
+    while (fits(kthr4 + 1, team / 2)) kthr4++;
     cudaFuncSetAttribute(core_svd_kernel<RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     { core_svd_kernel<RPL><<<n, SVD_THREADS, smem, st>>>(ups, n, ws, p, team, kthr, kthr4); note_launch(); }
 }
