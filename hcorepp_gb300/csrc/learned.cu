@@ -229,7 +229,6 @@ __global__ void __launch_bounds__(256) sketch_qr_kernel(Workspace ws) {
     extern __shared__ double skq_smem[];
     double *tau = skq_smem;            // kmax
     double *red = tau + ws.kmax;       // 8 warps
-    __shared__ double s_beta;
     const int s = blockIdx.x;
     const int *meta = ws.meta + (size_t) s * META_INTS;
     const int l = meta[META_LSK];
@@ -254,7 +253,6 @@ __global__ void __launch_bounds__(256) sketch_qr_kernel(Workspace ws) {
         if (threadIdx.x == 0) {
             yi[i] = beta;
             tau[i] = t;
-            s_beta = beta;
         }
         __syncthreads();
         if (t != 0.0)

@@ -35,6 +35,7 @@ namespace {
 constexpr int OZ_S = 8;                 // digit planes per operand
 constexpr int OZ_B = 7;                 // bits per digit
 constexpr int OZ_W = OZ_S * OZ_B;       // fixed-point width (56 bits)
+static_assert(OZ_W >= 53, "the digit planes must cover a double's 53-bit significand");
 constexpr int OZ_TM = 128, OZ_TN = 64;  // output tile per CTA (UMMA M = 128, N = 64)
 constexpr int OZ_KC = 32;               // K elements per shared-memory stage (64 bytes per row and plane)
 constexpr int OZ_KB = OZ_KC * 2 / 16;   // core matrices along K per stage (4)
