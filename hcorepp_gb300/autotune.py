@@ -81,9 +81,15 @@ def apply(ctx, config: dict) -> None:
     ctx.set_precond(int(config["precond"]))
 
 
+# A knob moves off its current value only for a gain above the run-to-run noise of a timed multiply.
+MIN_GAIN = 0.005
+
+
 def tune(run_multiply, ctx, steps: int = 2, warmup: int = 1, start: dict | None = None, knobs=None):
     """Coordinate descent over CANDIDATES (the knobs in `knobs`, default all).  run_multiply() restores C
-    and runs one multiply on the context's stream.  Returns (best config, {config label: ms per
+    and runs one multiply on the context's stream.  A candidate replaces the current choice only when it
+    is faster by more than MIN_GAIN (relative), so ties keep the defaults (the tensor-core WY Q
+    application and product routing among them).  Returns (best config, {config label: ms per
     multiply})."""
     import torch
     best = dict(start or DEFAULT)
@@ -112,7 +118,7 @@ def tune(run_multiply, ctx, steps: int = 2, warmup: int = 1, start: dict | None 
             cfg = dict(best)
             cfg[knob] = v
             ms = time_cfg(cfg)
-            if ms < best_ms:
+            if ms < best_ms * (1.0 - MIN_GAIN):
                 best, best_ms = cfg, ms
     apply(ctx, best)
     return best, seen
