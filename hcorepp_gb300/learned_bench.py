@@ -80,7 +80,7 @@ def apply_tlr(tm: T.TileMatrix, x: torch.Tensor) -> torch.Tensor:
     """The tile matrix times x (n x p), tile by tile."""
     nb = tm.nb
     f = tile_factors(tm)
-    y = torch.zeros_like(x)
+    y = torch.zeros((tm.mt * nb, x.shape[1]), dtype=x.dtype, device=x.device)
     for (i, j), t in f.items():
         xs = x[j * nb:(j + 1) * nb]
         y[i * nb:(i + 1) * nb] += (t[0] @ (t[1] @ xs)) if isinstance(t, tuple) else t @ xs
