@@ -68,6 +68,27 @@ __device__ __forceinline__ float jacobi_tangent(double a, double b, double c) {
     return copysignf(1.0f, zf) / (fabsf(zf) + sqrtf(fmaf(zf, zf, 1.0f)));
 }
 
+// A rotated pair's bookkeeping (tracked squared norms a - t cd, b + t cd; scales d cos; inverse scales
+// (1/d) q cos) spread over the first four lanes of its group: every lane evaluates the same three FP64
+// instructions on operands it selects, instead of one lane issuing six or seven (the FP64 pipe, one
+// warp-wide instruction per ~19 cycles per SM on GB300, bounds the plain core).  Lanes 0 / 1 store
+// column i's / j's norm and inverse scale, lanes 2 / 3 its scale.
+__device__ __forceinline__ void pair_bookkeeping(int gl, int i, int j, double a, double b, double tt, double cd,
+                                                 double cs, double q, double di, double dj, double dvi, double dvj,
+                                                 double *nrm, double *dsc, int dstride) {
+    const bool second = gl & 1, norm_lane = gl < 2;
+    const int col = second ? j : i;
+    const double m1 = norm_lane ? (second ? tt : -tt) : (second ? dj : di);
+    const double v = fma(m1, norm_lane ? cd : cs, norm_lane ? (second ? b : a) : 0.0);
+    const double w = (second ? dvj : dvi) * (q * cs);
+    if (norm_lane) {
+        nrm[col] = v;
+        dsc[dstride + col] = w;
+    } else if (gl < 4) {
+        dsc[col] = v;
+    }
+}
+
 // One sweep of one-sided Jacobi over the `ncols` columns (length `rows`) of X (ld ldx), with G
 // lanes per column pair (32/G pairs per warp at a time) and up to RPL rows per lane in registers.
 // Squared column norms are tracked in nrm[] (a' = a - t c, b' = b + t c), so each pair costs one
@@ -83,6 +104,7 @@ __device__ __forceinline__ float jacobi_tangent(double a, double b, double c) {
 template <int G, int RPL, class TM>
 __device__ int jacobi_sweep(const TM &tm, double *X, int ldx, int rows, int ncols, double *nrm, double tol2,
                             double tiny, int n2, double *dsc, int dstride) {
+    static_assert(G >= 4, "pair_bookkeeping spreads a pair's bookkeeping over four lanes");
     const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     constexpr int PPW = 32 / G;
     const int gl = lane % G, grp = lane / G;
@@ -139,15 +161,8 @@ __device__ int jacobi_sweep(const TM &tm, double *X, int ldx, int rows, int ncol
                         }
                     }
                 }
-                if (gl == 0) {
-                    nrm[i] = a - tt * cd;
-                    nrm[j] = b + tt * cd;
-                    dsc[i] = di * cs;
-                    dsc[j] = dj * cs;
-                    dsc[dstride + i] = dvi * q * cs;
-                    dsc[dstride + j] = dvj * q * cs;
-                    rotations++;
-                }
+                pair_bookkeeping(gl, i, j, a, b, tt, cd, cs, q, di, dj, dvi, dvj, nrm, dsc, dstride);
+                if (gl == 0) rotations++;
             }
         }
         tm.sync();
@@ -162,6 +177,7 @@ __device__ int jacobi_sweep(const TM &tm, double *X, int ldx, int rows, int ncol
 template <int G, class TM>
 __device__ int jacobi_sweep_loop(const TM &tm, double *X, int ldx, int rows, int ncols, double *nrm, double tol2,
                                  double tiny, int n2, double *dsc, int dstride) {
+    static_assert(G >= 4, "pair_bookkeeping spreads a pair's bookkeeping over four lanes");
     const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     constexpr int PPW = 32 / G;
     const int gl = lane % G, grp = lane / G;
@@ -209,15 +225,8 @@ __device__ int jacobi_sweep_loop(const TM &tm, double *X, int ldx, int rows, int
                     x[r] = fma(-t1, yv, xv);
                     y[r] = fma(t2, xv, yv);
                 }
-                if (gl == 0) {
-                    nrm[i] = a - tt * cd;
-                    nrm[j] = b + tt * cd;
-                    dsc[i] = di * cs;
-                    dsc[j] = dj * cs;
-                    dsc[dstride + i] = dvi * q * cs;
-                    dsc[dstride + j] = dvj * q * cs;
-                    rotations++;
-                }
+                pair_bookkeeping(gl, i, j, a, b, tt, cd, cs, q, di, dj, dvi, dvj, nrm, dsc, dstride);
+                if (gl == 0) rotations++;
             }
         }
         tm.sync();
