@@ -81,3 +81,52 @@ def test_coordinate_descent_picks_the_fastest(monkeypatch):
     best, seen = A.tune(lambda: None, Ctx(), steps=1, warmup=0)
     assert best == {"groups": 16, "wy_min": 96, "oz_min": 4096, "graph": 1, "precond": 64}
     assert len(seen) <= 1 + sum(len(v) for v in A.CANDIDATES.values())
+
+
+def test_ties_keep_the_defaults(monkeypatch):
+    """A candidate faster by less than MIN_GAIN (run-to-run noise) does not replace the default."""
+    state = {}
+
+    class Ctx:
+        def set_concurrency(self, g):
+            pass
+
+        def set_tuning(self, oz, wy):
+            pass
+
+        def set_graph(self, on):
+            pass
+
+        def set_precond(self, m):
+            pass
+
+    def cost(cfg):  # wy_min = off is 0.2 % faster, groups = 16 is 5 % faster
+        c = 1000.0
+        if cfg["wy_min"] == 1 << 30:
+            c *= 0.998
+        if cfg["groups"] == 16:
+            c *= 0.95
+        return c
+
+    real_apply = A.apply
+
+    def fake_apply(ctx, cfg):
+        state["cfg"] = dict(cfg)
+        real_apply(ctx, cfg)
+
+    class Ev:
+        def __init__(self, **kw):
+            pass
+
+        def record(self):
+            pass
+
+        def elapsed_time(self, other):
+            return cost(state["cfg"])
+
+    fake_torch = types.SimpleNamespace(cuda=types.SimpleNamespace(Event=Ev, synchronize=lambda: None))
+    monkeypatch.setitem(sys.modules, "torch", fake_torch)
+    monkeypatch.setattr(A, "apply", fake_apply)
+    best, _ = A.tune(lambda: None, Ctx(), steps=1, warmup=0)
+    assert best["groups"] == 16
+    assert best["wy_min"] == A.DEFAULT["wy_min"]
