@@ -310,6 +310,7 @@ __device__ void jacobi(const TM &tm, double *X, int ldx, int rows, int ncols, do
 template <int G, int RPL, class TM>
 __device__ int jacobi_sweep_df(const TM &tm, df *X, int ldx, int rows, int ncols, df *nrm, df *ds, df *dv, float tol, float tiny,
                                int n2) {
+    static_assert(G >= 4, "a pair's bookkeeping is spread over four lanes of its group");
     const int warp = tm.warp(), lane = threadIdx.x & 31, nw = tm.nw();
     constexpr int PPW = 32 / G;
     const int gl = lane % G, grp = lane / G;
@@ -372,17 +373,25 @@ __device__ int jacobi_sweep_df(const TM &tm, df *X, int ldx, int rows, int ncols
                         }
                     }
                 }
-                if (gl == 0) {
-                    const df tc = df_mul(df_f(tt), cd);
-                    nrm[i] = df_add(a, -tc);
-                    nrm[j] = df_add(b, tc);
-                    ds[i] = df_mul(di, cs);
-                    ds[j] = df_mul(dj, cs);
-                    const df qcs = df_mul(q, cs);
-                    dv[i] = df_mul(dvi, qcs);
-                    dv[j] = df_mul(dvj, qcs);
-                    rotations++;
+                // the pair's bookkeeping spread over the first four lanes of its group (as the FP64
+                // sweep's pair_bookkeeping): each evaluates the same float-float operations on
+                // operands it selects, which shortens the dependent chain one lane would otherwise run
+                {
+                    const bool second = gl & 1, norm_lane = gl < 2;
+                    const int col = second ? j : i;
+                    // lanes 0 / 1: norm a - t cd, b + t cd; lanes 2 / 3: scale d cs
+                    const df m1 = norm_lane ? (second ? df_f(tt) : df_f(-tt)) : (second ? dj : di);
+                    const df prod = df_mul(m1, norm_lane ? cd : cs);
+                    const df v = norm_lane ? df_add(second ? b : a, prod) : prod;
+                    const df w = df_mul(second ? dvj : dvi, df_mul(q, cs));  // inverse scale, lanes 0 / 1
+                    if (norm_lane) {
+                        nrm[col] = v;
+                        dv[col] = w;
+                    } else if (gl < 4) {
+                        ds[col] = v;
+                    }
                 }
+                if (gl == 0) rotations++;
             }
         }
         tm.sync();
