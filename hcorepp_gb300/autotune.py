@@ -27,7 +27,9 @@ DEFAULT = {"groups": 8, "wy_min": 48, "oz_min": 2048, "graph": 0, "precond": 1 <
 CANDIDATES = {"groups": [4, 8, 16], "wy_min": [32, 48, 96, 1 << 30], "oz_min": [512, 1024, 2048, 4096],
               "graph": [0, 1], "precond": [16, 32, 64, 1 << 30]}
 ORDER = ["groups", "wy_min", "oz_min", "graph", "precond"]
-FORM_KNOBS = {"mixed_ff48": ["groups", "wy_min", "oz_min", "graph"]}  # precond acts on the plain form only
+# The float-float form applies Q in float-float panels on every side (no WY form) and has no FP32
+# preconditioning, so wy_min and precond do not act on it.
+FORM_KNOBS = {"mixed_ff48": ["groups", "oz_min", "graph"]}
 
 
 def stack_class(mean_k: float) -> int:
