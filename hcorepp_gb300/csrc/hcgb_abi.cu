@@ -1034,11 +1034,15 @@ extern "C" int hcgb_compress_tiles(hcgb_context *ctx, int count, const double *c
     { identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf, cols, cols); note_launch(); }
     { identity_kernel<<<64, 256, 0, ctx->stream>>>(ibuf + n * n, cols, cols); note_launch(); }
     const int ncols = cols;
-    HCGB_CUDA(ctx, cudaMemcpyAsync(irank, &ncols, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    auto failed = [&](cudaError_t e) {  // a CUDA call failed: release what this call allocated
+        return done(fail(ctx, HCGB_CUDA_ERROR, std::string("hcgb_compress_tiles: ") + cudaGetErrorString(e)));
+    };
+    cudaError_t ce = cudaMemcpyAsync(irank, &ncols, sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    if (ce != cudaSuccess) return failed(ce);
     const hcgb_tile ident{ibuf, irank, cols, cols, cols, HCGB_COMPRESSED};
     std::vector<hcgb_update> ups(count);
     for (int i = 0; i < count; i++) {
-        HCGB_CUDA(ctx, cudaMemsetAsync(out[i].rank, 0, sizeof(int), ctx->stream));
+        if ((ce = cudaMemsetAsync(out[i].rank, 0, sizeof(int), ctx->stream)) != cudaSuccess) return failed(ce);
         ups[i] = hcgb_update{hcgb_tile{const_cast<double *>(dense[i]), nullptr, rows, cols, 0, HCGB_DENSE}, ident,
                              out[i]};
     }
@@ -1052,9 +1056,10 @@ extern "C" int hcgb_compress_tiles(hcgb_context *ctx, int count, const double *c
         const int nb = std::min(chunk, count - off);
         int rc = hcgb_gemm_batch(ctx, 1.0, 0.0, nb, ups.data() + off, params, dinfo);
         if (rc) return done(rc);
-        HCGB_CUDA(ctx, cudaMemcpyAsync(hinfo.data(), dinfo, sizeof(hcgb_update_info) * (size_t) nb,
-                                       cudaMemcpyDeviceToHost, ctx->stream));
-        HCGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if ((ce = cudaMemcpyAsync(hinfo.data(), dinfo, sizeof(hcgb_update_info) * (size_t) nb,
+                                  cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+            (ce = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+            return failed(ce);
         for (int i = 0; i < nb; i++) {
             const int st = hinfo[i].status;
             if (st == HCGB_NOT_CONVERGED) not_converged = true;
